@@ -1,0 +1,93 @@
+"""ctypes binding of `libbte_gb300.so` (the C ABI of include/bte_gb300.h).
+
+There is no fallback: if the library is missing or fails to load, every entry point
+raises. Build it with `python -m boltzmann_gb300._build` (or `__graft_entry__.build()`).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libbte_gb300.so")
+
+PROC = {"ELASTIC": 0, "EXCITATION": 1, "IONIZATION": 2, "ATTACHMENT": 3}
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+OP = dict(KNOTS=0, MASS=1, MINV=2, ADV_RAW=3, COL_RAW=4, COL_GT_RAW=5, MASS_VEC=6, TEMP_VEC=7,
+          MOBILITY=8, DIFFUSION=9, RATES=10, HL=11, GL=12, CC_A=13, CC_B=14)
+
+STATUS = {0: "converged", 1: "roundoff", 2: "max_iter", 3: "line_search", 4: "non_finite", 5: "singular"}
+
+EXPORTED = ["bte_grid_create", "bte_grid_destroy", "bte_grid_info", "bte_grid_export", "bte_initialize",
+            "bte_solve_steady", "bte_qoi", "bte_lu_factor", "bte_lu_solve", "bte_last_error",
+            "bte_radial_components"]
+
+
+class GridDesc(C.Structure):
+    _fields_ = [
+        ("n_sp", C.c_int), ("l_max", C.c_int), ("spline_qpts", C.c_int), ("vspace_ext", C.c_int),
+        ("ee", C.c_int), ("ev_max", C.c_double), ("Te", C.c_double), ("mByM", C.c_double),
+        ("n_processes", C.c_int), ("n_species", C.c_int),
+        ("proc_type", C.POINTER(C.c_int)), ("proc_species", C.POINTER(C.c_int)),
+        ("proc_threshold", C.POINTER(C.c_double)), ("proc_attach", C.POINTER(C.c_double)),
+        ("sigma_offsets", C.POINTER(C.c_int)), ("sigma_energy", C.POINTER(C.c_double)),
+        ("sigma_values", C.POINTER(C.c_double)), ("device", C.c_int),
+    ]
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [
+        ("atol", C.c_double), ("rtol", C.c_double), ("max_iter", C.c_int),
+        ("alpha_min", C.c_double), ("alpha_rho", C.c_double), ("line_search_c", C.c_double),
+        ("ee", C.c_int), ("precision", C.c_int), ("reserved", C.c_int * 6),
+    ]
+
+
+class TransientOpts(C.Structure):
+    _fields_ = [
+        ("atol", C.c_double), ("rtol", C.c_double), ("max_iter", C.c_int), ("ee", C.c_int),
+        ("precision", C.c_int), ("dt", C.c_double), ("tau", C.c_double), ("efreq", C.c_double),
+        ("t0", C.c_double), ("n_steps", C.c_int), ("reserved", C.c_int * 5),
+    ]
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Load the library once; raise with a clear message when it is not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libbte_gb300.so is not built (%s); run `python -m boltzmann_gb300._build`" % LIB_PATH)
+    lib = C.CDLL(LIB_PATH)
+    vp, i32p = C.c_void_p, C.POINTER(C.c_int32)
+    lib.bte_grid_create.argtypes = [C.POINTER(GridDesc), C.POINTER(C.c_void_p), vp]
+    lib.bte_grid_destroy.argtypes = [vp]
+    lib.bte_grid_info.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_double)]
+    lib.bte_grid_export.argtypes = [vp, C.c_int, vp, C.c_size_t, vp]
+    lib.bte_initialize.argtypes = [vp, C.c_int, vp, vp]
+    lib.bte_solve_steady.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, C.POINTER(SolveOpts), vp]
+    lib.bte_qoi.argtypes = [vp, C.c_int, vp, vp, vp, C.c_int, vp, vp, vp, vp, vp]
+    lib.bte_lu_factor.argtypes = [C.c_int, C.c_int, C.c_int, vp, C.c_int, C.c_longlong, vp, vp, vp]
+    lib.bte_lu_solve.argtypes = [C.c_int, C.c_int, C.c_int, vp, C.c_int, C.c_longlong, vp, vp, vp]
+    lib.bte_last_error.restype = C.c_char_p
+    for name in EXPORTED:
+        if not hasattr(lib, name):
+            raise RuntimeError("libbte_gb300.so does not export %s" % name)
+    if hasattr(lib, "bte_radial_components"):
+        lib.bte_radial_components.argtypes = [vp, C.c_int, vp, C.c_int, vp, vp, vp]
+    if hasattr(lib, "bte_solve_transient"):
+        lib.bte_solve_transient.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
+                                            C.POINTER(TransientOpts), vp]
+    _lib = lib
+    return lib
+
+
+def check(rc: int, what: str) -> None:
+    if rc != 0:
+        msg = load().bte_last_error().decode(errors="replace")
+        raise RuntimeError("%s failed (code %d): %s" % (what, rc, msg))

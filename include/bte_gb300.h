@@ -1,0 +1,148 @@
+/*
+ * bte_gb300.h — C ABI of the GB300 (sm_103a) batched velocity-space Boltzmann library.
+ *
+ * Drop-in boundary for the hot path of Boltzsim (ut-padas/boltzmann), whose public
+ * interface is the Python class `bte_0d3v_batched` (BESolver/python/bte_0d3v_batched.py).
+ * Every entry point names the reference interface it replaces. Conventions:
+ *   - plain pointers and sizes only; batch arrays are caller-owned DEVICE buffers
+ *     unless the parameter says "host";
+ *   - distributions are stored point-major: f[point * n + (p * num_sh + l)], with
+ *     n = n_sp * (l_max + 1) and the reference's radial-major coefficient order
+ *     (BESolver/python/spec_spherical.py:219-221);
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream);
+ *   - every function returns 0 on success or a negative BTE_ERR_* code, and never
+ *     exits the process; per-point solver outcomes go to an int32 status array.
+ *   - one grid handle must not be used from two host threads at once.
+ */
+#ifndef BTE_GB300_H
+#define BTE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct BteGrid bte_grid;
+
+/* process kinds (reference: collisions.py:400-430, CollisionType EAR_G0..G3) */
+#define BTE_PROC_ELASTIC 0
+#define BTE_PROC_EXCITATION 1
+#define BTE_PROC_IONIZATION 2
+#define BTE_PROC_ATTACHMENT 3
+
+/* arithmetic of the Newton linear solves */
+#define BTE_PREC_FP64 0   /* plain: FP64 Jacobian, FP64 LU, FP64 residual            */
+#define BTE_PREC_MIXED 1  /* FP32 Jacobian + FP32 LU, corrections against the FP64 residual */
+
+typedef struct {
+    int n_sp;                     /* number of cubic B-splines (reference argument Nr + 1)   */
+    int l_max;                    /* spherical-harmonic modes l = 0..l_max, m = 0             */
+    int spline_qpts;              /* Gauss points per knot interval, collision rule (5)      */
+    int vspace_ext;               /* 0 = none, 1 = linear x1.2 (vspace_grid_extension)        */
+    int ee;                       /* 1 = assemble the e-e Coulomb operators                   */
+    double ev_max;                /* grid energy, eV                                         */
+    double Te;                    /* normalisation temperature, eV (sets vth)                 */
+    double mByM;                  /* m_e / M of the elastic process                           */
+    int n_processes;
+    int n_species;
+    const int* proc_type;         /* host [n_processes] BTE_PROC_*                             */
+    const int* proc_species;      /* host [n_processes] species index                          */
+    const double* proc_threshold; /* host [n_processes] eV (ignored for elastic)               */
+    const double* proc_attach;    /* host [n_processes] attachment energy, eV                  */
+    const int* sigma_offsets;     /* host [n_processes + 1] offsets into the two tables below  */
+    const double* sigma_energy;   /* host, eV, increasing per process                          */
+    const double* sigma_values;   /* host, m^2                                                 */
+    int device;                   /* CUDA device ordinal                                       */
+} bte_grid_desc;
+
+typedef struct {
+    double atol, rtol;            /* stop when ||r|| <= atol + rtol * ||r0|| (per point)       */
+    int max_iter;
+    double alpha_min, alpha_rho, line_search_c;  /* Armijo backtracking                       */
+    int ee;                       /* include the e-e Coulomb term                              */
+    int precision;                /* BTE_PREC_FP64 or BTE_PREC_MIXED                           */
+    int reserved[6];
+} bte_solve_opts;
+
+/* Build a grid and assemble every operator on the device (FP64).
+ * Replaces bte_0d3v_batched.__init__ + assemble_operators
+ * (BESolver/python/bte_0d3v_batched.py:138-306, 310-479). */
+int bte_grid_create(const bte_grid_desc* desc, bte_grid** out, void* stream);
+
+/* Release a grid and all its device memory. */
+int bte_grid_destroy(bte_grid* g);
+
+/* Sizes and scalars of a grid: ints = {n_sp, l_max, num_sh, n, n_intervals, n_triples,
+ * n_processes, n_species}, dbls = {vth, maxwellian(0), v_max/vth, mByM}.
+ * Replaces the attributes _par_vth / _op_spec_sp read by callers (bte_0d3v_batched.py:155-160). */
+int bte_grid_info(const bte_grid* g, int* ints8, double* dbls4);
+
+/* Copy one assembled operator, expanded to the reference's dense layout, into the
+ * caller's device buffer `out` of `count` doubles. `which`: see BTE_OP_*.
+ * Replaces reading _op_mass_mat, _op_advection, _op_col_en, ... (bte_0d3v_batched.py:359-476). */
+#define BTE_OP_KNOTS 0      /* n_sp + 4                                              */
+#define BTE_OP_MASS 1       /* n x n        spec_spherical.compute_mass_matrix       */
+#define BTE_OP_MINV 2       /* n x n        spec_spherical.inverse_mass_mat          */
+#define BTE_OP_ADV_RAW 3    /* n x n        compute_advection_matix (unscaled)       */
+#define BTE_OP_COL_RAW 4    /* n_species x n x n  sum of assemble_mat per species     */
+#define BTE_OP_COL_GT_RAW 5 /* n x n        electron_gas_temperature                 */
+#define BTE_OP_MASS_VEC 6   /* n            utils.mass_op                            */
+#define BTE_OP_TEMP_VEC 7   /* n            utils.temp_op * 0.5 m_e (2/3/k_B) / K_1eV */
+#define BTE_OP_MOBILITY 8   /* n_sp         utils.mobility_op                        */
+#define BTE_OP_DIFFUSION 9  /* n_sp         utils.diffusion_op                       */
+#define BTE_OP_RATES 10     /* n_proc x n_sp utils.reaction_rates_op per process     */
+#define BTE_OP_HL 11        /* n x n        compute_rosenbluth_potentials_op (hl)    */
+#define BTE_OP_GL 12        /* n x n        compute_rosenbluth_potentials_op (gl)    */
+#define BTE_OP_CC_A 13      /* n x n x n    coulomb_collision_op_assembly (cc_a)     */
+#define BTE_OP_CC_B 14      /* n x n x n    coulomb_collision_op_assembly (cc_b)     */
+int bte_grid_export(const bte_grid* g, int which, double* out, size_t count, void* stream);
+
+/* Maxwellian initial state for P points (device f, P x n).
+ * Replaces bte_0d3v_batched.initialize(grid, n_pts, "maxwellian") (bte_0d3v_batched.py:481-520). */
+int bte_initialize(const bte_grid* g, int P, double* f, void* stream);
+
+/* Steady-state solve of P independent points. Device inputs n0, ne, Tg, E [P],
+ * ns_by_n0 [n_species x P]; f [P x n] in: initial state (any positive multiple),
+ * out: the normalized distribution (normalized_distribution). status/iters [P] int32.
+ * Replaces bte_0d3v_batched.solve(..., "steady-state") / steady_state_solve
+ * (bte_0d3v_batched.py:882-979, 1034-1047). */
+int bte_solve_steady(bte_grid* g, int P, const double* n0, const double* ne, const double* ns_by_n0,
+                     const double* Tg, const double* E, double* f, int32_t* status, int32_t* iters,
+                     const bte_solve_opts* opts, void* stream);
+
+/* Quantities of interest of P normalized distributions (device f [P x n]); outputs
+ * [P] each and rates [n_proc x P]. effective_mobility as in the reference.
+ * Replaces bte_0d3v_batched.compute_QoIs (bte_0d3v_batched.py:1163-1202). */
+int bte_qoi(const bte_grid* g, int P, const double* f, const double* n0, const double* E,
+            int effective_mobility, double* energy, double* mobility, double* diffusion,
+            double* rates, void* stream);
+
+/* Batched dense LU with partial pivoting, in place, on P ROW-major N x N matrices
+ * (A[r * ld + c]) with matrix stride `stride` (elements). dtype 0 = FP64, 1 = FP32.
+ * piv [P x N] int32 receives the 0-based row interchanges in LAPACK order (row k was
+ * swapped with piv[k], applied to every column); info [P] = 0 or the 1-based index of
+ * the first zero pivot.
+ * Replaces the xp.linalg.inv call of bte_0d3v_batched.batched_inv (bte_0d3v_batched.py:856-880). */
+int bte_lu_factor(int dtype, int P, int N, void* A, int ld, long long stride, int32_t* piv,
+                  int32_t* info, void* stream);
+
+/* Solve A x = b for one right-hand side per matrix using bte_lu_factor's output;
+ * b [P x N] (contiguous per point) is overwritten by x. Same dtype as the factors. */
+int bte_lu_solve(int dtype, int P, int N, const void* A, int ld, long long stride,
+                 const int32_t* piv, void* b, void* stream);
+
+/* Radial components f_l(eps) of P distributions (device f [P x n]) at n_ev energies
+ * (device ev, eV): out [P x num_sh x n_ev], out[pt][l][e] = sum_p f[pt][p, l] B_p(v(eps_e)).
+ * Replaces bte_0d3v_batched.compute_radial_components (bte_0d3v_batched.py:1219-1239). */
+int bte_radial_components(const bte_grid* g, int P, const double* f, int n_ev, const double* ev, double* out,
+                          void* stream);
+
+/* Last CUDA error string seen by the library on this thread (never NULL). */
+const char* bte_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BTE_GB300_H */

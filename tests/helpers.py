@@ -1,0 +1,47 @@
+"""Shared test helpers: build the drop-in solver and the CPU oracle on the same inputs."""
+import types
+
+import numpy as np
+
+from boltzmann_gb300.workloads import EV_MAX, TE_NORM, batch_parameters, config_parameters
+
+
+def make_args(n_sp, l_max, ee, n_pts, precision="fp64"):
+    return types.SimpleNamespace(threads=1, sp_order=3, spline_qpts=5, ee_collisions=int(ee), verbose=0, use_gpu=1,
+                                 Efreq=0.0, dt=1e-3, cycles=1, solver_type="steady-state", l_max=l_max, Nr=n_sp - 1,
+                                 n_pts=n_pts, precision=precision)
+
+
+def params_for(ee, n_pts, seed=20261203):
+    if ee:
+        return batch_parameters(n_pts, seed)
+    p = config_parameters("c1", n_pts)
+    return p
+
+
+def gpu_solver(xs, n_sp, l_max, ee, n_pts, precision="fp64", ext=0):
+    from boltzmann_gb300.bte_0d3v_batched import bte_0d3v_batched, vspace_grid_extension
+    args = make_args(n_sp, l_max, ee, n_pts, precision)
+    s = bte_0d3v_batched(args, np.array([EV_MAX]), np.array([TE_NORM]), np.array([n_sp - 1]),
+                         [[[l, 0] for l in range(l_max + 1)]], 1, [xs])
+    s.assemble_operators(0, vspace_ext=vspace_grid_extension(ext))
+    return s, args
+
+
+def oracle_ops(xs, n_sp, l_max, ee, ext=False, dense=True):
+    from oracle import bte_oracle as O
+    return O.Operators(O.processes_from_lxcat(xs), EV_MAX, TE_NORM, n_sp, l_max, ee=ee, extend_linear=ext,
+                       dense_coulomb=dense)
+
+
+def relmax(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def rel_l2_cols(a, b):
+    """Per-column relative L2 error of (n, P) arrays."""
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return np.linalg.norm(a - b, axis=0) / np.linalg.norm(b, axis=0)

@@ -1,0 +1,46 @@
+"""The C-ABI library builds for sm_103a, loads, and exports every declared symbol (no GPU calls)."""
+import re
+import os
+import ctypes
+
+import pytest
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "bte_gb300.h")).read()
+    return sorted(set(re.findall(r"^(?:int|const char\*)\s+(bte_\w+)\s*\(", src, flags=re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from boltzmann_gb300 import _build
+    path = _build.build()
+    return ctypes.CDLL(path)
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    for s in ["bte_grid_create", "bte_solve_steady", "bte_qoi", "bte_lu_factor", "bte_lu_solve"]:
+        assert s in syms
+
+
+def test_every_declared_symbol_is_exported(lib):
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_python_binding_loads(lib):
+    from boltzmann_gb300 import _lib
+    l = _lib.load()
+    assert l.bte_last_error() is not None
+
+
+def test_argument_errors_without_gpu(lib):
+    """Argument validation happens before any CUDA call."""
+    from boltzmann_gb300 import _lib
+    l = _lib.load()
+    rc = l.bte_grid_create(None, None, None)
+    assert rc == -1
+    assert b"null" in l.bte_last_error()
