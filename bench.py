@@ -1,0 +1,357 @@
+"""Benchmark: batched 0D3V steady-state EDF solves on GB300.
+
+Workload (default): 4096 independent points, 128 cubic B-splines x l_max 2 (n = 384
+unknowns, 385 x 385 bordered Newton systems), e-e Coulomb collisions on, E/N log-uniform
+in [1, 1000] Td, ionization degree log-uniform in [1e-8, 1e-3] (seed 20261203), synthetic
+analytic argon-like cross sections. One step = one full EDF solve of the whole batch as
+the reference driver does it (Maxwellian start, e-e-off warm start, e-e-on solve, QoIs).
+
+Headline: solves/s of the mixed form (FP32 Jacobian factorizations against the FP64
+residual). The plain FP64 form runs the same workload for the ratio and the error check
+(max relative L2 difference of the EDFs <= 1e-8).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+import types
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "EDF solves/s (batched 0D3V steady state, e-e on, mixed precision, <=1e-8 rel err vs plain FP64)"
+UNIT = "solves/s"
+ATOL, RTOL, MAXIT = 1e-20, 1e-14, 100
+ALPHA_MIN, ALPHA_RHO, LS_C = 1e-16, 0.5, 1e-4
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n-pts", type=int, default=4096)
+    ap.add_argument("--n-sp", type=int, default=128)
+    ap.add_argument("--l-max", type=int, default=2)
+    ap.add_argument("--seed", type=int, default=20261203)
+    ap.add_argument("--plain-steps", type=int, default=1, help="timed steps of the plain FP64 form")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-points", type=int, default=2)
+    return ap.parse_args()
+
+
+def workload_config(a, precision):
+    return {
+        "workload": "batched 0D3V steady-state EDF solve: %d points, %d B-splines x l_max %d (n=%d), e-e Coulomb on, "
+                    "E/N log-uniform [1,1000] Td, ionization degree log-uniform [1e-8,1e-3], seed %d"
+                    % (a.n_pts, a.n_sp, a.l_max, a.n_sp * (a.l_max + 1), a.seed),
+        "n_pts_per_gpu": a.n_pts, "n_sp": a.n_sp, "l_max": a.l_max, "precision": precision,
+        "step": "maxwellian init + e-e-off warm start + e-e-on Newton solve + QoIs",
+        "cache": "inputs larger than L2: each step streams %.1f GB of Jacobians" % (
+            a.n_pts * (a.n_sp * (a.l_max + 1) + 1) ** 2 * (4 if precision == "mixed" else 8) / 1e9),
+        "parallelism": "points sharded across GPUs, no collective on the data path",
+    }
+
+
+def dist_init(n):
+    if n <= 1 or "RANK" not in os.environ:
+        return 0, 1
+    import torch.distributed as dist
+    backend = "nccl"
+    dist.init_process_group(backend=backend)
+    return dist.get_rank(), dist.get_world_size()
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def make_solver(xs, a, precision, dev):
+    from boltzmann_gb300.bte_0d3v_batched import bte_0d3v_batched, vspace_grid_extension
+    from boltzmann_gb300.workloads import EV_MAX, TE_NORM
+    args = types.SimpleNamespace(threads=1, sp_order=3, spline_qpts=5, ee_collisions=1, verbose=0, use_gpu=1,
+                                 Efreq=0.0, dt=1e-3, cycles=1, solver_type="steady-state", l_max=a.l_max,
+                                 Nr=a.n_sp - 1, n_pts=a.n_pts, precision=precision)
+    s = bte_0d3v_batched(args, np.array([EV_MAX]), np.array([TE_NORM]), np.array([a.n_sp - 1]),
+                         [[[l, 0] for l in range(a.l_max + 1)]], 1, [xs])
+    s._dev_id = dev
+    t0 = time.perf_counter()
+    s.assemble_operators(0, vspace_ext=vspace_grid_extension.NONE)
+    return s, args, time.perf_counter() - t0
+
+
+def full_solve(s, args, f0):
+    """One EDF solve of the batch: e-e-off warm start then e-e-on (bte_0d3v_batched_driver.py:192-204)."""
+    args.ee_collisions = 0
+    ff, _ = s.solve(0, f0, ATOL, RTOL, MAXIT, "steady-state", ALPHA_MIN, ALPHA_RHO, LS_C)
+    args.ee_collisions = 1
+    return s.solve(0, ff, ATOL, RTOL, MAXIT, "steady-state", ALPHA_MIN, ALPHA_RHO, LS_C)
+
+
+def run_gb300(a, rank, ws):
+    import torch
+    from boltzmann_gb300 import _lib
+    from boltzmann_gb300.workloads import write_synthetic_lxcat, batch_parameters
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    xs = write_synthetic_lxcat()
+    prm = batch_parameters(a.n_pts, a.seed + 7919 * rank)
+    s, args, t_setup = make_solver(xs, a, "mixed", dev)
+    for k in ["n0", "ne", "ns_by_n0", "Tg", "E"]:
+        s.set_boltzmann_parameter(0, k, prm[k])
+    f0_host = s.initialize(0, a.n_pts)
+    s.host_to_device_setup(dev, 0)
+    f0 = torch.as_tensor(f0_host, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    for _ in range(a.warmup):
+        ff, q = full_solve(s, args, f0)
+    torch.cuda.synchronize()
+    barrier(ws)
+    _lib.stats_reset(timing=True)
+    clocks = Clocks(dev)
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    step_ms = []
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(a.steps):
+        e_a = torch.cuda.Event(enable_timing=True)
+        e_b = torch.cuda.Event(enable_timing=True)
+        e_a.record(stream)
+        ff, q = full_solve(s, args, f0)
+        e_b.record(stream)
+        step_ms.append((e_a, e_b))
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier(ws)
+    st = _lib.stats()
+    ms = ev0.elapsed_time(ev1) / a.steps
+    ms = max_over_ranks(ms, ws)
+    steps_ms = [x.elapsed_time(y) for x, y in step_ms]
+    value = a.n_pts * ws / (ms / 1e3)
+    status = q["status"].cpu().numpy()
+    iters = q["iters"].cpu().numpy()
+    ff_mixed = ff.detach().cpu().numpy()
+
+    # end to end through the public API with host buffers (H2D of inputs, D2H of results inside)
+    s2_params = {k: prm[k] for k in ["n0", "ne", "ns_by_n0", "Tg", "E"]}
+    for k, v in s2_params.items():
+        s.set_boltzmann_parameter(0, k, v)
+    s.xp_module = np
+    full_solve(s, args, f0_host)
+    torch.cuda.synchronize()
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        ff_h, q_h = full_solve(s, args, f0_host)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / a.steps, ws)
+    n = f0_host.shape[0]
+    h2d = f0_host.nbytes * 2 + 8 * (4 + 1) * a.n_pts * 2  # f0 + parameters, two solves per step
+    d2h = (n * a.n_pts * 8 + (3 + len(q_h["rates"])) * a.n_pts * 8 + 2 * 4 * a.n_pts) * 2
+    e2e = {"value": a.n_pts * ws / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+           "path": "bte_0d3v_batched.solve() with NumPy host arrays"}
+
+    # plain FP64 form on the same batch: throughput and the error of the mixed form against it
+    plain = None
+    if not a.no_plain:
+        sp, argsp, _ = make_solver(xs, a, "fp64", dev)
+        for k in ["n0", "ne", "ns_by_n0", "Tg", "E"]:
+            sp.set_boltzmann_parameter(0, k, prm[k])
+        sp.host_to_device_setup(dev, 0)
+        full_solve(sp, argsp, f0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(a.plain_steps):
+            ffp, qp = full_solve(sp, argsp, f0)
+        torch.cuda.synchronize()
+        pms = (time.perf_counter() - t0) / a.plain_steps * 1e3
+        ffp = ffp.detach().cpu().numpy()
+        err = np.linalg.norm(ff_mixed - ffp, axis=0) / np.linalg.norm(ffp, axis=0)
+        qerr = {k: float(np.max(np.abs(q[k].cpu().numpy() - qp[k].cpu().numpy()) / np.abs(qp[k].cpu().numpy())))
+                for k in ("energy", "mobility", "diffusion")}
+        plain = {"value": a.n_pts * ws / (pms / 1e3), "ms_per_step": pms,
+                 "mixed_speedup": (a.n_pts * ws / (ms / 1e3)) / (a.n_pts * ws / (pms / 1e3)),
+                 "edf_max_rel_err_mixed_vs_fp64": float(np.max(err)), "qoi_max_rel_err_mixed_vs_fp64": qerr,
+                 "status_counts": {str(k): int(v) for k, v in zip(*np.unique(qp["status"].cpu().numpy(), return_counts=True))}}
+        del sp
+    os.unlink(xs)
+    return dict(value=value, ms=ms, steps_ms=steps_ms, stats=st, clocks=clk, status=status, iters=iters, e2e=e2e,
+                plain=plain, setup_s=t_setup)
+
+
+def roofline(st, peaks):
+    fams = {k: v for k, v in st.items() if isinstance(v, dict)}
+    dom = max(fams, key=lambda k: fams[k]["ms"])
+    v = fams[dom]
+    hbm = peaks.get("hbm_gbs")
+    per_launch_s = v["ms"] / 1e3 / max(v["launches"], 1)
+    bytes_pl = v["bytes"] / max(v["launches"], 1)
+    flops_pl = v["flops"] / max(v["launches"], 1)
+    achieved = bytes_pl / per_launch_s / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get(dom)
+        except Exception:
+            traffic = None
+    return {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm if hbm else None, "traffic": traffic,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if hbm else "fallback 6800 GB/s",
+            "alg_bytes_per_launch": bytes_pl, "avg_launch_ms": per_launch_s * 1e3,
+            "tflops_achieved": flops_pl / per_launch_s / 1e12,
+            "families_ms": {k: round(f["ms"], 3) for k, f in fams.items()}}
+
+
+def cpu_sample(a, n_pts, iters_per_phase=3):
+    """Time the oracle (the reference's algorithm restated in NumPy) on a bounded sample of the
+    same workload: n_pts points, `iters_per_phase` Newton iterations of each phase, extrapolated
+    to the reference's budget of max_iter = 100 iterations per phase (its batch-global loop runs
+    to the cap on this workload)."""
+    import multiprocessing
+    from oracle import bte_oracle as O
+    from boltzmann_gb300.workloads import write_synthetic_lxcat, batch_parameters, EV_MAX, TE_NORM
+    xs = write_synthetic_lxcat()
+    t0 = time.perf_counter()
+    ops = O.Operators(O.processes_from_lxcat(xs), EV_MAX, TE_NORM, a.n_sp, a.l_max, ee=True)
+    t_setup = time.perf_counter() - t0
+    prm = batch_parameters(n_pts, a.seed)
+    P = O.Params(prm["n0"], prm["ne"], prm["Tg"], prm["E"], prm["ns_by_n0"])
+    f0 = O.maxwellian_initial(ops, n_pts)
+    t0 = time.perf_counter()
+    O.steady_state_solve(ops, P, f0, ATOL, RTOL, iters_per_phase, False, ALPHA_MIN, ALPHA_RHO, LS_C)
+    t_off = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.steady_state_solve(ops, P, f0, ATOL, RTOL, iters_per_phase, True, ALPHA_MIN, ALPHA_RHO, LS_C)
+    t_on = time.perf_counter() - t0
+    os.unlink(xs)
+    per_point = (t_off + t_on) / iters_per_phase * MAXIT / n_pts
+    return {"value": 1.0 / per_point, "unit": UNIT, "cores": multiprocessing.cpu_count(), "kind": "port",
+            "sample": "%d points x %d Newton iterations per phase (e-e off, e-e on) of the same workload, "
+                      "extrapolated to %d iterations per phase; NumPy/OpenBLAS threads = all host cores; "
+                      "oracle setup %.1f s not counted" % (n_pts, iters_per_phase, MAXIT, t_setup),
+            "seconds": t_off + t_on}
+
+
+def main():
+    a = parse()
+    rank, ws = dist_init(a.gpus)
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    if a.impl == "reference":
+        if rank != 0:
+            return
+        steps = []
+        for _ in range(a.warmup):
+            cpu_sample(a, a.cpu_points, 1)
+        for _ in range(a.steps):
+            steps.append(cpu_sample(a, a.cpu_points, 2))
+        v = float(np.median([s["value"] for s in steps]))
+        line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+                "ms_per_step": 1e3 * a.n_pts / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic", "impl": "reference",
+                "config": workload_config(a, "fp64"),
+                "cpu_baseline": {**steps[-1], "value": v},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+    r = run_gb300(a, rank, ws)
+    if rank != 0:
+        return
+    cpu = None if a.no_cpu else cpu_sample(a, a.cpu_points, 3)
+    st = r["stats"]
+    steps_ms = sorted(r["steps_ms"])
+    line = {
+        "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "mixed: f32 Jacobian+LU, f64 residual/state", "data": "synthetic",
+        "config": workload_config(a, "mixed"),
+        "latency_ms": {"p50": float(np.percentile(steps_ms, 50)), "p99": float(np.percentile(steps_ms, 99)),
+                       "unit": "batch solve of %d points" % a.n_pts},
+        "e2e": r["e2e"], "gpu_launches": st["launches"],
+        "fp64_fallback_points_per_step": st["fp64_fallback_points"] / a.steps,
+        "roofline": roofline(st, peaks), "cpu_baseline": cpu, "clocks": r["clocks"],
+        "plain_fp64": r["plain"], "setup_s": r["setup_s"],
+        "newton_iters": {"mean": float(np.mean(r["iters"])), "max": int(np.max(r["iters"]))},
+        "status_counts": {str(k): int(v) for k, v in zip(*np.unique(r["status"], return_counts=True))},
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -22,7 +22,9 @@ STATUS = {0: "converged", 1: "roundoff", 2: "max_iter", 3: "line_search", 4: "no
 
 EXPORTED = ["bte_grid_create", "bte_grid_destroy", "bte_grid_info", "bte_grid_export", "bte_initialize",
             "bte_solve_steady", "bte_qoi", "bte_lu_factor", "bte_lu_solve", "bte_last_error",
-            "bte_radial_components"]
+            "bte_radial_components", "bte_stats_reset", "bte_stats", "bte_solve_info"]
+
+STAT_FAMILIES = ["residual", "jacobian", "lu_factor", "lu_solve", "refine", "other"]
 
 
 class GridDesc(C.Structure):
@@ -41,7 +43,7 @@ class SolveOpts(C.Structure):
     _fields_ = [
         ("atol", C.c_double), ("rtol", C.c_double), ("max_iter", C.c_int),
         ("alpha_min", C.c_double), ("alpha_rho", C.c_double), ("line_search_c", C.c_double),
-        ("ee", C.c_int), ("precision", C.c_int), ("reserved", C.c_int * 6),
+        ("ee", C.c_int), ("precision", C.c_int), ("refine", C.c_int), ("reserved", C.c_int * 5),
     ]
 
 
@@ -75,6 +77,9 @@ def load() -> C.CDLL:
     lib.bte_lu_factor.argtypes = [C.c_int, C.c_int, C.c_int, vp, C.c_int, C.c_longlong, vp, vp, vp]
     lib.bte_lu_solve.argtypes = [C.c_int, C.c_int, C.c_int, vp, C.c_int, C.c_longlong, vp, vp, vp]
     lib.bte_last_error.restype = C.c_char_p
+    lib.bte_stats_reset.argtypes = [C.c_int]
+    lib.bte_solve_info.argtypes = [vp, C.c_int, vp, vp, vp]
+    lib.bte_stats.argtypes = [C.POINTER(C.c_double), C.c_int]
     for name in EXPORTED:
         if not hasattr(lib, name):
             raise RuntimeError("libbte_gb300.so does not export %s" % name)
@@ -91,3 +96,19 @@ def check(rc: int, what: str) -> None:
     if rc != 0:
         msg = load().bte_last_error().decode(errors="replace")
         raise RuntimeError("%s failed (code %d): %s" % (what, rc, msg))
+
+
+def stats_reset(timing: bool) -> None:
+    check(load().bte_stats_reset(int(timing)), "bte_stats_reset")
+
+
+def stats() -> dict:
+    """Kernel launches and per-family (launches, device ms, algorithmic flops, bytes)."""
+    nb = 2 + 4 * len(STAT_FAMILIES)
+    buf = (C.c_double * nb)()
+    check(load().bte_stats(buf, nb), "bte_stats")
+    out = {"launches": int(buf[0])}
+    for i, f in enumerate(STAT_FAMILIES):
+        out[f] = dict(launches=int(buf[1 + 4 * i]), ms=buf[2 + 4 * i], flops=buf[3 + 4 * i], bytes=buf[4 + 4 * i])
+    out["fp64_fallback_points"] = int(buf[1 + 4 * len(STAT_FAMILIES)])
+    return out

@@ -299,7 +299,8 @@ class bte_0d3v_batched:
         iters = torch.empty(n_pts, dtype=torch.int32, device="cuda")
         opts = _lib.SolveOpts(atol=float(atol), rtol=float(rtol), max_iter=int(max_iter), alpha_min=float(alpha_min),
                               alpha_rho=float(alpha_rho), line_search_c=float(line_search_c),
-                              ee=int(getattr(self._args, "ee_collisions", 0)), precision=self._precision())
+                              ee=int(getattr(self._args, "ee_collisions", 0)), precision=self._precision(),
+                              refine=int(getattr(self._args, "refine", 2)))
         stream = torch.cuda.current_stream().cuda_stream
         _lib.check(_lib.load().bte_solve_steady(self._grid[grid_idx], n_pts, _ptr(n0), _ptr(ne), _ptr(ns), _ptr(Tg),
                                                 _ptr(E), _ptr(f), _ptr(status), _ptr(iters), C.byref(opts),
@@ -307,6 +308,12 @@ class bte_0d3v_batched:
         qoi = self._qoi_dev(grid_idx, f, n0, E, effective_mobility=True)
         qoi["status"] = status
         qoi["iters"] = iters
+        rf = torch.empty(n_pts, dtype=torch.float64, device="cuda")
+        r0 = torch.empty_like(rf)
+        _lib.check(_lib.load().bte_solve_info(self._grid[grid_idx], n_pts, _ptr(rf), _ptr(r0), C.c_void_p(stream)),
+                   "bte_solve_info")
+        qoi["abs_error"] = rf
+        qoi["rel_error"] = rf / r0
         ff = f.t()
         torch.cuda.synchronize()
         prof[pp.SOLVE].stop()

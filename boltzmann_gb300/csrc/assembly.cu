@@ -416,6 +416,23 @@ __global__ void k_derived(int nsp, int nsh, int nspecies, double mw0, double vth
     }
 }
 
+// merit vectors: invMd = 1 / diag(M), vD = D M p / |D M p|
+__global__ void k_merit_vectors(int nsp, int nsh, const double* __restrict__ Mr, const double* __restrict__ Mp,
+                                double* invMd, double* vD) {
+    __shared__ double red[32];
+    int n = nsp * nsh;
+    double ss = 0.0;
+    for (int a = threadIdx.x; a < n; a += blockDim.x) {
+        double d = 1.0 / Mr[(a / nsh) * BTE_NB + BTE_BAND];
+        invMd[a] = d;
+        double v = Mp[a] * d;
+        vD[a] = v;
+        ss += v * v;
+    }
+    double nrm = sqrt(block_sum(ss, red));
+    for (int a = threadIdx.x; a < n; a += blockDim.x) vD[a] /= nrm;
+}
+
 __global__ void k_to_float(const double* __restrict__ in, float* out, size_t n) {
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (i < n) out[i] = (float)in[i];
@@ -660,6 +677,9 @@ int bte_assemble(BteGrid* g, cudaStream_t s) {
         GALLOC(scratch, nsp);
         k_derived<<<1, 512, 0, s>>>(nsp, nsh, g->nspecies, g->mw0, g->vth, g->d_mass, g->d_Mr, g->d_Minv, g->d_q0,
                                     g->d_u, g->d_p, g->d_Mp, g->d_W, scratch);
+        CK(cudaGetLastError());
+        GALLOC(g->d_invMd, n); GALLOC(g->d_vD, n);
+        k_merit_vectors<<<1, 512, 0, s>>>(nsp, nsh, g->d_Mr, g->d_Mp, g->d_invMd, g->d_vD);
         CK(cudaGetLastError());
     }
     // Coulomb operators

@@ -29,6 +29,7 @@
 #define BTE_ST_LINESEARCH 3     // step length fell below alpha_min
 #define BTE_ST_NONFINITE 4      // residual or Jacobian became NaN / Inf
 #define BTE_ST_SINGULAR 5       // zero pivot in the Jacobian factorization
+#define BTE_ST_NEED_FP64 6      // internal: the mixed form hands the point to the FP64 path
 
 // ----------------------------------------------------------------------------------
 // Cubic B-spline evaluation: values and first/second derivatives of the 4 nonzero

@@ -64,6 +64,8 @@ struct BteGrid {
     double* d_p = nullptr;               // n
     double* d_Mp = nullptr;              // n
     double* d_W = nullptr;               // nspecies x n
+    double* d_invMd = nullptr;           // n, 1 / diag(M)
+    double* d_vD = nullptr;              // n, D M p / |D M p| with D = diag(M)^-1
 
     // device: Coulomb (FP64)
     double* d_HL = nullptr;              // nsh x nsp x nsp
@@ -90,3 +92,4 @@ void bte_work_release(BteWork* w);
 int bte_solve_impl(BteGrid* g, int P, const double* n0, const double* ne, const double* ns_by_n0,
                    const double* Tg, const double* E, double* f, int32_t* status, int32_t* iters,
                    const bte_solve_opts* opts, cudaStream_t s);
+int bte_solve_info_impl(BteGrid* g, int P, double* r_final, double* r_initial, cudaStream_t s);

@@ -401,6 +401,14 @@ int bte_solve_steady(bte_grid* g, int P, const double* n0, const double* ne, con
     return BTE_OK;
 }
 
+int bte_solve_info(bte_grid* g, int P, double* r_final, double* r_initial, void* stream) {
+    if (!g || P < 0 || !r_final || !r_initial) return fail(BTE_ERR_ARG, "bad argument");
+    cudaSetDevice(g->device);
+    int rc = bte_solve_info_impl(g, P, r_final, r_initial, (cudaStream_t)stream);
+    if (rc) return fail(rc, "no steady solve of that size has run on this grid");
+    return BTE_OK;
+}
+
 int bte_qoi(const bte_grid* g, int P, const double* f, const double* n0, const double* E, int effective_mobility,
             double* energy, double* mobility, double* diffusion, double* rates, void* stream) {
     if (!g || P < 0) return fail(BTE_ERR_ARG, "bad argument");

@@ -19,6 +19,7 @@
 namespace {
 
 constexpr int LU_THREADS = 256;
+constexpr int LU_MAX_N = LU_THREADS * 8;  // panel rows per thread (ROWS) are 2, 4 or 8
 
 template <typename T> __device__ inline T tabs(T v) { return v < T(0) ? -v : v; }
 
@@ -42,8 +43,13 @@ __device__ inline void ld8(const double* p, double v[8]) {
     }
 }
 
-template <typename T, int NB>
-__global__ void __launch_bounds__(LU_THREADS)
+// FP32: two CTAs per SM (the panel factorization of one overlaps the other's update);
+// FP64: one, the FP64 pipe is the bound and the register tile needs the room
+template <typename T> struct LuOcc { static constexpr int value = 1; };
+template <> struct LuOcc<float> { static constexpr int value = 2; };
+
+template <typename T, int NB, int LU_ROWS>
+__global__ void __launch_bounds__(LU_THREADS, LuOcc<T>::value)
 k_lu_factor(int N, int NC, T* __restrict__ A, int ld, long long stride, int32_t* __restrict__ piv,
             int32_t* __restrict__ info) {
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -58,7 +64,6 @@ k_lu_factor(int N, int NC, T* __restrict__ A, int ld, long long stride, int32_t*
     T* U = sm + (((size_t)ldp * NB + 7) & ~(size_t)7);    // NB x ldu
     __shared__ T redv[LU_THREADS / 32];
     __shared__ int redi[LU_THREADS / 32];
-    __shared__ int s_piv;
     int inf = 0;
 
     for (int k0 = 0; k0 < N; k0 += NB) {
@@ -70,13 +75,19 @@ k_lu_factor(int N, int NC, T* __restrict__ A, int ld, long long stride, int32_t*
             P[c * ldp + r] = (c < kb) ? a[(size_t)(k0 + r) * ld + k0 + c] : T(0);
         }
         __syncthreads();
-        // ---- unblocked factorization of the panel
+        // ---- unblocked factorization of the panel. Thread t owns panel rows t, t + nt, ...
+        // (at most LU_ROWS of them), so the pivot search reads only its own rows and each
+        // column costs two barriers: after the warp candidates, after the row interchange.
         for (int j = 0; j < kb; ++j) {
             T best = T(-1);
-            int bi = j;
-            for (int r = j + tid; r < mrows; r += nt) {
-                T v = tabs(P[j * ldp + r]);
-                if (v > best) { best = v; bi = r; }
+            int bi = mrows;  // sentinel: larger than any row
+#pragma unroll
+            for (int k = 0; k < LU_ROWS; ++k) {
+                int r = tid + k * nt;
+                if (r >= j && r < mrows) {
+                    T v = tabs(P[j * ldp + r]);
+                    if (v > best || (v == best && r < bi)) { best = v; bi = r; }
+                }
             }
             for (int o = 16; o > 0; o >>= 1) {
                 T ov = __shfl_xor_sync(0xffffffffu, best, o);
@@ -85,35 +96,36 @@ k_lu_factor(int N, int NC, T* __restrict__ A, int ld, long long stride, int32_t*
             }
             if ((tid & 31) == 0) { redv[tid >> 5] = best; redi[tid >> 5] = bi; }
             __syncthreads();
-            if (tid == 0) {
-                T b = redv[0];
-                int i0 = redi[0];
-                for (int w = 1; w < nt / 32; ++w)
-                    if (redv[w] > b || (redv[w] == b && redi[w] < i0)) { b = redv[w]; i0 = redi[w]; }
-                s_piv = i0;
-                pv[k0 + j] = k0 + i0;
-                if (!(P[j * ldp + i0] != T(0)) && inf == 0) inf = k0 + j + 1;
-            }
-            __syncthreads();
-            const int pr = s_piv;
-            if (pr != j)
-                for (int c = tid; c < kb; c += nt) {
-                    T t0 = P[c * ldp + j];
-                    P[c * ldp + j] = P[c * ldp + pr];
-                    P[c * ldp + pr] = t0;
+            T b = redv[0];
+            int pr = redi[0];
+            for (int w = 1; w < nt / 32; ++w)
+                if (redv[w] > b || (redv[w] == b && redi[w] < pr)) { b = redv[w]; pr = redi[w]; }
+            if (pr >= mrows) pr = j;  // all candidates NaN: keep the diagonal
+            if (tid < 32) {
+                if (pr != j && tid < kb) {
+                    T t0 = P[tid * ldp + j];
+                    P[tid * ldp + j] = P[tid * ldp + pr];
+                    P[tid * ldp + pr] = t0;
                 }
+                if (tid == 0) {
+                    pv[k0 + j] = k0 + pr;
+                    if (!(b != T(0)) && inf == 0) inf = k0 + j + 1;
+                }
+            }
             __syncthreads();
             const T d = P[j * ldp + j];
             const T inv = (d != T(0)) ? T(1) / d : T(0);
-            for (int r = j + 1 + tid; r < mrows; r += nt) P[j * ldp + r] *= inv;
-            __syncthreads();
-            const int rem_r = mrows - j - 1, rem_c = kb - j - 1;
-            for (int e = tid; e < rem_r * rem_c; e += nt) {
-                int r = j + 1 + e % rem_r, c = j + 1 + e / rem_r;
-                P[c * ldp + r] -= P[j * ldp + r] * P[c * ldp + j];
+#pragma unroll
+            for (int k = 0; k < LU_ROWS; ++k) {
+                int r = tid + k * nt;
+                if (r > j && r < mrows) {
+                    T l = P[j * ldp + r] * inv;
+                    P[j * ldp + r] = l;
+                    for (int c = j + 1; c < kb; ++c) P[c * ldp + r] -= l * P[c * ldp + j];
+                }
             }
-            __syncthreads();
         }
+        __syncthreads();
         // ---- write the panel back
         for (int e = tid; e < mrows * kb; e += nt) {
             int r = e / kb, c = e % kb;
@@ -273,14 +285,22 @@ k_lu_solve(int N, const T* __restrict__ A, int ld, long long stride, const int32
     for (int i = tid; i < N; i += nt) bb[i] = x[i];
 }
 
+template <typename T, int NB, int ROWS>
+cudaError_t launch_factor_r(int P, int N, int NC, T* A, int ld, long long stride, int32_t* piv, int32_t* info,
+                            cudaStream_t s) {
+    size_t sm = lu_smem_elems(N, NC, NB) * sizeof(T);
+    cudaError_t e = cudaFuncSetAttribute(k_lu_factor<T, NB, ROWS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    k_lu_factor<T, NB, ROWS><<<P, LU_THREADS, sm, s>>>(N, NC, A, ld, stride, piv, info);
+    return cudaGetLastError();
+}
+
 template <typename T, int NB>
 cudaError_t launch_factor(int P, int N, int NC, T* A, int ld, long long stride, int32_t* piv, int32_t* info,
                           cudaStream_t s) {
-    size_t sm = lu_smem_elems(N, NC, NB) * sizeof(T);
-    cudaError_t e = cudaFuncSetAttribute(k_lu_factor<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
-    k_lu_factor<T, NB><<<P, LU_THREADS, sm, s>>>(N, NC, A, ld, stride, piv, info);
-    return cudaGetLastError();
+    if (N <= 2 * LU_THREADS) return launch_factor_r<T, NB, 2>(P, N, NC, A, ld, stride, piv, info, s);
+    if (N <= 4 * LU_THREADS) return launch_factor_r<T, NB, 4>(P, N, NC, A, ld, stride, piv, info, s);
+    return launch_factor_r<T, NB, 8>(P, N, NC, A, ld, stride, piv, info, s);
 }
 
 }  // namespace
@@ -300,6 +320,7 @@ template <typename T>
 cudaError_t bte_lu_factor_t(int P, int N, int NC, T* A, int ld, long long stride, int32_t* piv, int32_t* info,
                             cudaStream_t s) {
     if (P <= 0) return cudaSuccess;
+    if (N > LU_MAX_N) return cudaErrorInvalidValue;  // panel rows per thread are bounded
     int nb = pick_nb<T>(N, NC);
     if (nb == 32) return launch_factor<T, 32>(P, N, NC, A, ld, stride, piv, info, s);
     if (nb == 16) return launch_factor<T, 16>(P, N, NC, A, ld, stride, piv, info, s);

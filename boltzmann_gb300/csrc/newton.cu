@@ -8,7 +8,8 @@
 // with the raw (un-scaled, banded) operators F_raw = M F, the exact Jacobian
 // (including -(M h) w^T and the Coulomb-logarithm derivative), an LU of the
 // (n+1) x (n+1) bordered matrix, per-point Armijo backtracking on the reference's
-// merit 1/2 ||Q^T M^-1 F||^2 (:939-952) and per-point convergence.
+// merit (a lumped-mass scaling of the reference's 1/2 ||Q^T M^-1 F||^2, :939-952) and
+// per-point convergence.
 //
 //   residual   FP64 always (one CTA per point)
 //   Jacobian   FP64 (plain) or FP32 (mixed) straight into the factorization buffer
@@ -33,6 +34,7 @@ struct GridView {
     double vth, mw0, c_adv, gam_c, k1ev;
     const double *Mr, *Minv, *mm1, *mm2, *q0, *q1, *cgT, *adv_coef;
     const double *mass, *temp, *u, *p, *Mp, *W;
+    const double *invMd, *vD;  // 1 / diag(M) and the unit vector D M p of the merit
     const double *HL, *GL, *CA, *CB;
     const int* tri;
     const float *fq0, *fq1, *fcgT, *fmm1, *fmm2, *fMr, *fHL, *fGL, *fCA, *fCB;
@@ -54,7 +56,8 @@ enum { SC_GAMMA = 0, SC_MU, SC_T0, SC_M0, SC_NE, SC_COUNT = 8 };
 __global__ void __launch_bounds__(256)
 k_residual(GridView g, PointParams pp, int ee, const int* __restrict__ act, int nact,
            const double* __restrict__ h, const double* __restrict__ dh, int ldd, const double* __restrict__ alpha,
-           const int* __restrict__ need, double* hout, double* F, double* aux, double* scal, double* rnorm) {
+           const int* __restrict__ need, double* hout, double* F, double* aux, double* scal, double* rnorm,
+           double* srel) {
     extern __shared__ double sm[];
     const int slot = blockIdx.x;
     if (slot >= nact) return;
@@ -70,13 +73,24 @@ k_residual(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
 
     const double* hp = h + (size_t)pt * n;
     const double a = alpha ? alpha[pt] : 0.0;
+    double sd = 0.0, shn = 0.0;
     for (int i = tid; i < n; i += nt) {
         double v = hp[i];
-        if (dh) v += a * dh[(size_t)pt * ldd + i];
+        if (dh) {
+            double d = dh[(size_t)pt * ldd + i];
+            sd += d * d;
+            shn += v * v;
+            v += a * d;
+        }
         sh[i] = v;
         if (hout) hout[(size_t)pt * n + i] = v;
     }
     __syncthreads();
+    if (srel) {
+        sd = block_sum(sd, red);
+        shn = block_sum(shn, red);
+        if (tid == 0) srel[pt] = sqrt(sd / fmax(shn, 1e-300));
+    }
     const double n0 = pp.n0[pt], Tg = pp.Tg[pt], E = pp.E[pt], ne = pp.ne[pt];
     double m0 = 0, t0 = 0, mu = 0;
     for (int i = tid; i < n; i += nt) {
@@ -182,7 +196,37 @@ k_residual(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
         sc[SC_GAMMA] = gam; sc[SC_MU] = mu; sc[SC_T0] = t0; sc[SC_M0] = m0; sc[SC_NE] = ne;
     }
     __syncthreads();
-    // r = M^-1 F (block diagonal in l), projected on p-perp
+    // merit ||P_v D F||, D = diag(M)^-1, v = D M p / |D M p|: zero exactly at the reference's
+    // roots (Q^T M^-1 F = 0 <=> F || M p) without the round-off amplification of a dense M^-1
+    double pr = 0.0;
+    for (int r = tid; r < n; r += nt) {
+        double d = sF[r] * g.invMd[r];
+        sR[r] = d;
+        pr += g.vD[r] * d;
+    }
+    pr = block_sum(pr, red);
+    double nn = 0.0;
+    for (int r = tid; r < n; r += nt) {
+        double v = sR[r] - g.vD[r] * pr;
+        nn += v * v;
+    }
+    nn = block_sum(nn, red);
+    if (tid == 0) rnorm[pt] = sqrt(nn);
+}
+
+// The reference's merit ||(I - p p^T) M^-1 F|| = ||Q^T M^-1 F|| (bte_0d3v_batched.py:920-926)
+// of stored raw residuals, for reporting (one CTA per point).
+__global__ void __launch_bounds__(256)
+k_ref_merit(GridView g, int P, const double* __restrict__ F, double* out) {
+    extern __shared__ double sm[];
+    __shared__ double red[32];
+    const int pt = blockIdx.x;
+    if (pt >= P) return;
+    const int n = g.n, nsh = g.nsh, nsp = g.nsp, tid = threadIdx.x, nt = blockDim.x;
+    double* sF = sm;
+    double* sR = sm + n;
+    for (int i = tid; i < n; i += nt) sF[i] = F[(size_t)pt * n + i];
+    __syncthreads();
     double pr = 0.0;
     for (int r = tid; r < n; r += nt) {
         int p = r / nsh, l = r % nsh;
@@ -199,7 +243,185 @@ k_residual(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
         nn += v * v;
     }
     nn = block_sum(nn, red);
-    if (tid == 0) rnorm[pt] = sqrt(nn);
+    if (tid == 0) out[pt] = sqrt(nn);
+}
+
+// ---------------------------------------------------------------------------------
+// FP64 iterative refinement of the mixed-precision Newton step: r = b - J x with the
+// bordered Jacobian applied matrix-free in FP64 (the same terms k_jacobian writes):
+//   (J x)[a] = static(x)[a] - mu (M x)[a] - (M h)[a] (w . x) + ne gamma [C(x; HL h, GL h)
+//              + C(h; HL x, GL x)][a] + ne U[a] (dgamma . x) - beta Mp[a] x[n]
+//   (J x)[n] = beta u . x,   b = (-F, beta (1 - u . h)).
+// The residual is scaled by its max-norm sigma and stored in FP32 (slot-major) for the
+// FP32 substitution; sigma[slot] is kept to undo the scaling.
+// ---------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+k_refine_residual(GridView g, PointParams pp, int ee, const int* __restrict__ act, int nact,
+                  const double* __restrict__ h, const double* __restrict__ F, const double* __restrict__ aux,
+                  const double* __restrict__ scal, const double* __restrict__ x, int ldd, double beta_scale,
+                  const double* __restrict__ rowscale, float* __restrict__ rs, double* __restrict__ sigma) {
+    extern __shared__ double sm[];
+    const int slot = blockIdx.x;
+    if (slot >= nact) return;
+    const int pt = act[slot];
+    const int n = g.n, nsh = g.nsh, nsp = g.nsp, N = n + 1, tid = threadIdx.x, nt = blockDim.x;
+    double* sx = sm;            // x (n + 1)
+    double* sh = sm + N;        // h
+    double* sxh = sh + n;       // HL x
+    double* sxg = sxh + n;      // GL x
+    double* sr = sxg + n;       // r
+    __shared__ double red[32];
+    const double* hp = h + (size_t)pt * n;
+    const double* ax = aux + (size_t)pt * 4 * n;
+    const double* sc = scal + (size_t)pt * SC_COUNT;
+    for (int i = tid; i < N; i += nt) sx[i] = x[(size_t)pt * ldd + i];
+    for (int i = tid; i < n; i += nt) sh[i] = hp[i];
+    __syncthreads();
+    const double n0 = pp.n0[pt], Tg = pp.Tg[pt], E = pp.E[pt], ne = sc[SC_NE];
+    const double gam = sc[SC_GAMMA], mu = sc[SC_MU], t0 = sc[SC_T0], m0 = sc[SC_M0];
+    const double beta = beta_scale * n0;
+    double wx = 0, dgx = 0, ux = 0, uh = 0;
+    for (int i = tid; i < n; i += nt) {
+        double ws = 0;
+        for (int s = 0; s < g.nspecies; ++s) ws += n0 * pp.ns[(size_t)s * pp.P + pt] * g.W[(size_t)s * n + i];
+        wx += ws * sx[i];
+        dgx += (g.temp[i] / t0 - g.mass[i] / m0) * sx[i];
+        ux += g.u[i] * sx[i];
+        uh += g.u[i] * sh[i];
+    }
+    wx = block_sum(wx, red);
+    dgx = block_sum(dgx, red) * g.gam_c * 1.5;
+    ux = block_sum(ux, red);
+    uh = block_sum(uh, red);
+    if (ee) {
+        for (int r = tid; r < n; r += nt) {
+            int p = r / nsh, l = r % nsh;
+            const double* HLr = g.HL + ((size_t)l * nsp + p) * nsp;
+            const double* GLr = g.GL + ((size_t)l * nsp + p) * nsp;
+            double s1 = 0, s2 = 0;
+            for (int c = 0; c < nsp; ++c) {
+                double v = sx[c * nsh + l];
+                s1 += HLr[c] * v;
+                s2 += GLr[c] * v;
+            }
+            sxh[r] = s1;
+            sxg[r] = s2;
+        }
+        __syncthreads();
+    }
+    const double cadv = E * g.c_adv;
+    double amax = 0.0;
+    for (int r = tid; r < n; r += nt) {
+        const int p = r / nsh, q = r % nsh;
+        double y = 0.0;
+        for (int s = 0; s < g.nspecies; ++s) {
+            double ns = n0 * pp.ns[(size_t)s * pp.P + pt];
+            double acc = 0.0;
+            if (q == 0) {
+                const double* row = g.q0 + ((size_t)s * nsp + p) * nsp;
+                for (int k = 0; k < nsp; ++k) acc += row[k] * sx[k * nsh];
+            } else {
+                const double* row = g.q1 + ((size_t)s * nsp + p) * BTE_NB;
+                for (int dk = -BTE_BAND; dk <= BTE_BAND; ++dk) {
+                    int k = p + dk;
+                    if (k >= 0 && k < nsp) acc += row[dk + BTE_BAND] * sx[k * nsh + q];
+                }
+            }
+            y += ns * acc;
+        }
+        double gt = 0.0, adv = 0.0, mx = 0.0;
+        for (int dk = -BTE_BAND; dk <= BTE_BAND; ++dk) {
+            int k = p + dk;
+            if (k < 0 || k >= nsp) continue;
+            int bi = p * BTE_NB + dk + BTE_BAND;
+            if (q == 0) gt += g.cgT[bi] * sx[k * nsh];
+            if (q + 1 <= g.lmax)
+                adv += (g.mm1[bi] * g.adv_coef[q * 4 + 0] + g.adv_coef[q * 4 + 1] * g.mm2[bi]) * sx[k * nsh + q + 1];
+            if (q >= 1)
+                adv += (g.mm1[bi] * g.adv_coef[q * 4 + 2] + g.adv_coef[q * 4 + 3] * g.mm2[bi]) * sx[k * nsh + q - 1];
+            mx += g.Mr[bi] * sx[k * nsh + q];
+        }
+        y += n0 * Tg * gt + cadv * adv - mu * mx - ax[3 * n + r] * wx;
+        if (ee) {
+            double c1 = 0.0;
+            for (int t = 0; t < g.ntri; ++t) {
+                if (g.tri[3 * t] != q) continue;
+                const int l = g.tri[3 * t + 1], s = g.tri[3 * t + 2];
+                const double* ca = g.CA + ((size_t)t * nsp + p) * BTE_NB * BTE_NB;
+                const double* cb = g.CB + ((size_t)t * nsp + p) * BTE_NB * BTE_NB;
+                for (int dk = -BTE_BAND; dk <= BTE_BAND; ++dk) {
+                    int k = p + dk;
+                    if (k < 0 || k >= nsp) continue;
+                    double in_h = 0.0, in_x = 0.0;
+                    for (int dr = -BTE_BAND; dr <= BTE_BAND; ++dr) {
+                        int rr = p + dr;
+                        if (rr < 0 || rr >= nsp) continue;
+                        int o = (dk + BTE_BAND) * BTE_NB + dr + BTE_BAND;
+                        in_h += ca[o] * ax[rr * nsh + s] + cb[o] * ax[n + rr * nsh + s];
+                        in_x += ca[o] * sxh[rr * nsh + s] + cb[o] * sxg[rr * nsh + s];
+                    }
+                    c1 += in_h * sx[k * nsh + l] + in_x * sh[k * nsh + l];
+                }
+            }
+            y += ne * gam * c1 + ne * ax[2 * n + r] * dgx;
+        }
+        y += -beta * g.Mp[r] * sx[n];
+        double rv = (-F[(size_t)pt * n + r] - y) * rowscale[(size_t)slot * N + r];
+        sr[r] = rv;
+        amax = fmax(amax, fabs(rv));
+    }
+    if (tid == 0) {
+        double rv = (beta * (1.0 - uh) - beta * ux) * rowscale[(size_t)slot * N + n];
+        sr[n] = rv;
+        amax = fmax(amax, fabs(rv));
+    }
+    // max-norm for the FP32 scaling
+    for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    __syncthreads();
+    if ((tid & 31) == 0) red[tid >> 5] = amax;
+    __syncthreads();
+    if (tid == 0) {
+        double m = 0.0;
+        for (int w = 0; w < (nt + 31) / 32; ++w) m = fmax(m, red[w]);
+        red[0] = (m > 0.0) ? m : 1.0;
+        sigma[slot] = red[0];
+    }
+    __syncthreads();
+    const double inv = 1.0 / red[0];
+    for (int i = tid; i < N; i += nt) rs[(size_t)slot * N + i] = (float)(sr[i] * inv);
+}
+
+// x[pt] += sigma * y[slot]; corr[pt] = ||sigma * y|| / ||x|| of this pass
+__global__ void k_refine_update(int nact, const int* __restrict__ act, int N, const float* __restrict__ y,
+                                const double* __restrict__ sigma, double* x, int ldd, double* corr) {
+    __shared__ double red[32];
+    int slot = blockIdx.x;
+    if (slot >= nact) return;
+    int pt = act[slot];
+    double sg = sigma[slot];
+    double cc = 0.0, xx = 0.0;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        double d = sg * (double)y[(size_t)slot * N + i];
+        double v = x[(size_t)pt * ldd + i] + d;
+        x[(size_t)pt * ldd + i] = v;
+        cc += d * d;
+        xx += v * v;
+    }
+    cc = block_sum(cc, red);
+    xx = block_sum(xx, red);
+    if (threadIdx.x == 0) corr[pt] = sqrt(cc / fmax(xx, 1e-300));
+}
+
+// after the refinement passes: a correction that did not shrink by 4x from the first
+// to the last pass (and is not already at round-off) means the FP32 factors cannot
+// resolve this point's Jacobian: hand the point to the FP64 path
+__global__ void k_refine_check(int nact, const int* __restrict__ act, const double* __restrict__ c_first,
+                               const double* __restrict__ c_last, int* status) {
+    int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= nact) return;
+    int pt = act[slot];
+    double a = c_first[pt], b = c_last[pt];
+    if (!(b <= 0.25 * a || b <= 1e-13) && status[pt] < 0) status[pt] = BTE_ST_NEED_FP64;
 }
 
 // ---------------------------------------------------------------------------------
@@ -240,11 +462,25 @@ struct OpsT<float> {
 
 constexpr int JAC_WARPS = 8;
 
+// Row equilibration of one bordered row (matrix part [0, N) and the RHS column N): the
+// row is divided by its largest |entry| so that the factorization sees rows of unit
+// size (the l = 0 energy-exchange rows are ~m/M smaller than the l >= 1 rows). The
+// applied factor is returned for the FP64 refinement.
+template <typename T>
+__device__ inline void equilibrate_row(T* Jr, int N, int lane, double* scale_out) {
+    T m = T(0);
+    for (int j = lane; j < N; j += 32) m = fmax(m, fabs(Jr[j]));
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    const T sc = (m > T(0)) ? T(1) / m : T(1);
+    for (int j = lane; j < N + 1; j += 32) Jr[j] *= sc;
+    if (lane == 0 && scale_out) *scale_out = (double)sc;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(JAC_WARPS * 32)
 k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int nact, const double* __restrict__ h,
            const double* __restrict__ F, const double* __restrict__ aux, const double* __restrict__ scal,
-           T* __restrict__ J, int ld, long long stride, double beta_scale) {
+           T* __restrict__ J, int ld, long long stride, double beta_scale, double* __restrict__ rowscale) {
     const int slot = blockIdx.y;
     if (slot >= nact) return;
     const int pt = act[slot];
@@ -269,6 +505,8 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
             Jr[n] = T(0);
             Jr[n + 1] = (T)(beta * (1.0 - uh));
         }
+        __syncwarp();
+        equilibrate_row(Jr, N, lane, rowscale ? rowscale + (size_t)slot * N + a : nullptr);
         return;
     }
     const int p = a / nsh, q = a % nsh;
@@ -279,26 +517,24 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
     // dgamma/dh = gam_c * 1.5 * (Top / (Top.h) - Mop / (Mop.h)), Top = temp * K_1eV
     const double dg_t = ee ? ne * Ua * g.gam_c * 1.5 / t0 : 0.0;
     const double dg_m = ee ? ne * Ua * g.gam_c * 1.5 / m0 : 0.0;
-    // K2a[dr][s], K2b[dr][s] for this row: sum over triples (q, l, s) and dk of C[t][p][dk][dr] h[(p+dk, l)]
-    const T* CA = OpsT<T>::CA(g);
-    const T* CB = OpsT<T>::CB(g);
-    T k2a[BTE_NB * 5], k2b[BTE_NB * 5];  // l_max <= 4
+    // K2a[dr][s], K2b[dr][s] for this row: sum over triples (q, l, s) and dk of C[t][p][dk][dr] h[(p+dk, l)],
+    // accumulated in FP64; only the dense products with HL / GL run in T.
+    double k2a[BTE_NB * 5], k2b[BTE_NB * 5];  // l_max <= 4
     if (ee) {
 #pragma unroll
-        for (int i = 0; i < BTE_NB * 5; ++i) { k2a[i] = T(0); k2b[i] = T(0); }
+        for (int i = 0; i < BTE_NB * 5; ++i) { k2a[i] = 0.0; k2b[i] = 0.0; }
         for (int t = 0; t < g.ntri; ++t) {
             if (g.tri[3 * t] != q) continue;
             const int l = g.tri[3 * t + 1], s = g.tri[3 * t + 2];
-            const T* ca = CA + ((size_t)t * nsp + p) * BTE_NB * BTE_NB;
-            const T* cb = CB + ((size_t)t * nsp + p) * BTE_NB * BTE_NB;
+            const double* ca = g.CA + ((size_t)t * nsp + p) * BTE_NB * BTE_NB;
+            const double* cb = g.CB + ((size_t)t * nsp + p) * BTE_NB * BTE_NB;
             for (int dk = -BTE_BAND; dk <= BTE_BAND; ++dk) {
                 int k = p + dk;
                 if (k < 0 || k >= nsp) continue;
-                T hv = (T)hp[k * nsh + l];
+                double hv = hp[k * nsh + l];
 #pragma unroll
                 for (int dr = 0; dr < BTE_NB; ++dr) {
                     int o = (dk + BTE_BAND) * BTE_NB + dr;
-                    // s is bounded by l_max <= 4, index computed at run time
                     k2a[s * BTE_NB + dr] += ca[o] * hv;
                     k2b[s * BTE_NB + dr] += cb[o] * hv;
                 }
@@ -307,23 +543,17 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
     }
     const T* HL = OpsT<T>::HL(g);
     const T* GL = OpsT<T>::GL(g);
-    const T* q0 = OpsT<T>::q0(g);
-    const T* q1 = OpsT<T>::q1(g);
-    const T* cgT = OpsT<T>::cgT(g);
-    const T* mm1 = OpsT<T>::mm1(g);
-    const T* mm2 = OpsT<T>::mm2(g);
-    const T* Mr = OpsT<T>::Mr(g);
     const double cadv = E * g.c_adv;
     for (int j = lane; j < N + 1; j += 32) {
         if (j == n) { Jr[j] = (T)(-beta * g.Mp[a]); continue; }
         if (j == n + 1) { Jr[j] = (T)(-F[(size_t)pt * n + a]); continue; }
         const int c = j / nsh, s = j % nsh;
-        T v = T(0);
+        // every term but the dense Coulomb product is summed in FP64 and rounded once:
+        // the l = 0 rows cancel nearly equal terms at low E/N
         double wj = 0.0;
         if (s == 0)
             for (int sp = 0; sp < g.nspecies; ++sp) wj += n0 * pp.ns[(size_t)sp * pp.P + pt] * g.W[(size_t)sp * n + j];
-        double dgj = ee ? (dg_t * g.temp[j] * g.k1ev - dg_m * g.mass[j]) : 0.0;
-        v += (T)(-mh * wj + dgj);
+        double v = -mh * wj + (ee ? (dg_t * g.temp[j] - dg_m * g.mass[j]) : 0.0);
         if (ee) {
             const T* hl = HL + (size_t)s * nsp * nsp + c;
             const T* gl = GL + (size_t)s * nsp * nsp + c;
@@ -332,47 +562,47 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
             for (int dr = 0; dr < BTE_NB; ++dr) {
                 int r = p + dr - BTE_BAND;
                 if (r < 0 || r >= nsp) continue;
-                acc += k2a[s * BTE_NB + dr] * hl[(size_t)r * nsp] + k2b[s * BTE_NB + dr] * gl[(size_t)r * nsp];
+                acc += (T)k2a[s * BTE_NB + dr] * hl[(size_t)r * nsp] + (T)k2b[s * BTE_NB + dr] * gl[(size_t)r * nsp];
             }
-            v += (T)negam * acc;
+            v += negam * (double)acc;
         }
         // l = 0 collision block (not banded: v_post shifts the support)
         if (q == 0 && s == 0)
             for (int sp = 0; sp < g.nspecies; ++sp)
-                v += (T)(n0 * pp.ns[(size_t)sp * pp.P + pt]) * q0[((size_t)sp * nsp + p) * nsp + c];
+                v += (n0 * pp.ns[(size_t)sp * pp.P + pt]) * g.q0[((size_t)sp * nsp + p) * nsp + c];
         const int dk = c - p;
         if (dk >= -BTE_BAND && dk <= BTE_BAND) {
             const int bi = p * BTE_NB + dk + BTE_BAND;
             if (s == q) {
-                if (q == 0) v += (T)(n0 * Tg) * cgT[bi];
+                if (q == 0) v += (n0 * Tg) * g.cgT[bi];
                 else
                     for (int sp = 0; sp < g.nspecies; ++sp)
-                        v += (T)(n0 * pp.ns[(size_t)sp * pp.P + pt]) * q1[((size_t)sp * nsp + p) * BTE_NB + dk + BTE_BAND];
-                v -= (T)mu * Mr[bi];
+                        v += (n0 * pp.ns[(size_t)sp * pp.P + pt]) * g.q1[((size_t)sp * nsp + p) * BTE_NB + dk + BTE_BAND];
+                v -= mu * g.Mr[bi];
             }
-            if (s == q + 1)
-                v += (T)cadv * (mm1[bi] * (T)g.adv_coef[q * 4 + 0] + (T)g.adv_coef[q * 4 + 1] * mm2[bi]);
-            if (s == q - 1)
-                v += (T)cadv * (mm1[bi] * (T)g.adv_coef[q * 4 + 2] + (T)g.adv_coef[q * 4 + 3] * mm2[bi]);
+            if (s == q + 1) v += cadv * (g.mm1[bi] * g.adv_coef[q * 4 + 0] + g.adv_coef[q * 4 + 1] * g.mm2[bi]);
+            if (s == q - 1) v += cadv * (g.mm1[bi] * g.adv_coef[q * 4 + 2] + g.adv_coef[q * 4 + 3] * g.mm2[bi]);
             if (ee) {
                 // K1[(p,q)][(c,s)] = sum_{t=(q,s,s')} sum_dr C[t][p][dk][dr] pot[(p+dr, s')]
-                T k1 = T(0);
+                double k1 = 0.0;
                 for (int t = 0; t < g.ntri; ++t) {
                     if (g.tri[3 * t] != q || g.tri[3 * t + 1] != s) continue;
                     const int s2 = g.tri[3 * t + 2];
-                    const T* ca = CA + ((size_t)t * nsp + p) * BTE_NB * BTE_NB + (dk + BTE_BAND) * BTE_NB;
-                    const T* cb = CB + ((size_t)t * nsp + p) * BTE_NB * BTE_NB + (dk + BTE_BAND) * BTE_NB;
+                    const double* ca = g.CA + ((size_t)t * nsp + p) * BTE_NB * BTE_NB + (dk + BTE_BAND) * BTE_NB;
+                    const double* cb = g.CB + ((size_t)t * nsp + p) * BTE_NB * BTE_NB + (dk + BTE_BAND) * BTE_NB;
                     for (int dr = -BTE_BAND; dr <= BTE_BAND; ++dr) {
                         int rr = p + dr;
                         if (rr < 0 || rr >= nsp) continue;
-                        k1 += ca[dr + BTE_BAND] * (T)ax[rr * nsh + s2] + cb[dr + BTE_BAND] * (T)ax[n + rr * nsh + s2];
+                        k1 += ca[dr + BTE_BAND] * ax[rr * nsh + s2] + cb[dr + BTE_BAND] * ax[n + rr * nsh + s2];
                     }
                 }
-                v += (T)negam * k1;
+                v += negam * k1;
             }
         }
-        Jr[j] = v;
+        Jr[j] = (T)v;
     }
+    __syncwarp();
+    equilibrate_row(Jr, N, lane, rowscale ? rowscale + (size_t)slot * N + a : nullptr);
 }
 
 // h <- f / (u . f) (bte_0d3v_batched.py:903-911)
@@ -417,25 +647,31 @@ __global__ void k_store_solution(int P_act, const T* __restrict__ xs, int N, con
     for (int i = threadIdx.x; i < N; i += blockDim.x) dh[(size_t)pt * ldd + i] = (double)xs[(size_t)slot * N + i];
 }
 
-// Armijo test (bte_0d3v_batched.py:942-952) for every point still searching
+// Armijo test (bte_0d3v_batched.py:942-952) for every point still searching. Round-off
+// stop: a full Newton step smaller than step_rtol * ||h|| that does not decrease the merit
+// (or a residual already below stagnate_rtol * ||r0|| that the full step cannot reduce)
+// means the state is converged to the arithmetic's floor.
 __global__ void k_armijo(int nact, const int* __restrict__ act, int* searching, double* alpha,
                          const double* __restrict__ r, const double* __restrict__ rt, double c, double rho,
                          double amin, int* status, int* nsearch, int* accepted, const double* __restrict__ r0,
-                         double stagnate_rtol) {
+                         double stagnate_rtol, const double* __restrict__ srel, double step_rtol) {
     int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= nact) return;
     int pt = act[slot];
     if (!searching[pt]) return;
+    if (status[pt] == BTE_ST_NEED_FP64) { searching[pt] = 0; accepted[pt] = 0; return; }
     double rr = r[pt], rn = rt[pt], al = alpha[pt];
     bool ok = (0.5 * rn * rn <= 0.5 * rr * rr - c * al * rr * rr);
     if (!isfinite(rn)) ok = false;
+    const bool tiny = srel[pt] <= step_rtol;
     if (ok) {
         searching[pt] = 0;
         accepted[pt] = 1;
+        // a step that barely contracts the merit at round-off level ends the solve after it is taken
+        if (rn > 0.5 * rr && (rn <= stagnate_rtol * r0[pt] || tiny)) status[pt] = BTE_ST_ROUNDOFF;
         return;
     }
-    // at round-off level a full step that does not decrease the merit ends the solve
-    if (al == 1.0 && rr <= stagnate_rtol * r0[pt]) {
+    if (al == 1.0 && (rr <= stagnate_rtol * r0[pt] || tiny)) {
         searching[pt] = 0;
         accepted[pt] = 0;
         status[pt] = BTE_ST_ROUNDOFF;
@@ -523,13 +759,19 @@ struct BteWork {
     double *h = nullptr, *ht = nullptr, *F = nullptr, *Ft = nullptr, *aux = nullptr, *auxt = nullptr;
     double *scal = nullptr, *scalt = nullptr, *dh = nullptr, *r = nullptr, *rt = nullptr, *r0 = nullptr, *alpha = nullptr;
     double* xs = nullptr;  // LU solutions by slot, P x (n + 1)
+    double* sigma = nullptr;  // refinement scaling by slot, P
+    double* srel = nullptr;   // ||dh|| / ||h|| of the current Newton step, P
+    double* rowscale = nullptr;  // row equilibration factors of the Jacobians, P x (n + 1)
+    double* h0 = nullptr;     // initial state (restart of points that fall back to FP64), P x n
+    double *ref_r = nullptr, *ref_r0 = nullptr;  // the reference's merit at the end / start, P
+    double *corr0 = nullptr, *corr1 = nullptr;   // relative refinement corrections, first / last pass
     void* J = nullptr;
     int32_t *piv = nullptr, *info = nullptr, *act = nullptr, *act2 = nullptr, *cnt = nullptr;
     int32_t *searching = nullptr, *accepted = nullptr;
 };
 
 static void free_work(BteWork* w) {
-    void* ptrs[] = {w->xs, w->h, w->ht, w->F, w->Ft, w->aux, w->auxt, w->scal, w->scalt, w->dh, w->r, w->rt, w->r0,
+    void* ptrs[] = {w->corr0, w->corr1, w->ref_r, w->ref_r0, w->rowscale, w->h0, w->srel, w->sigma, w->xs, w->h, w->ht, w->F, w->Ft, w->aux, w->auxt, w->scal, w->scalt, w->dh, w->r, w->rt, w->r0,
                     w->alpha, w->J, w->piv, w->info, w->act, w->act2, w->cnt, w->searching, w->accepted};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -544,7 +786,7 @@ static GridView view_of(const BteGrid* g) {
     v.k1ev = BTE_QE / BTE_KB;
     v.Mr = g->d_Mr; v.Minv = g->d_Minv; v.mm1 = g->d_mm1; v.mm2 = g->d_mm2; v.q0 = g->d_q0; v.q1 = g->d_q1;
     v.cgT = g->d_cgT; v.adv_coef = g->d_adv_coef; v.mass = g->d_mass; v.temp = g->d_temp; v.u = g->d_u; v.p = g->d_p;
-    v.Mp = g->d_Mp; v.W = g->d_W; v.HL = g->d_HL; v.GL = g->d_GL; v.CA = g->d_CA; v.CB = g->d_CB; v.tri = g->d_tri;
+    v.Mp = g->d_Mp; v.W = g->d_W; v.invMd = g->d_invMd; v.vD = g->d_vD; v.HL = g->d_HL; v.GL = g->d_GL; v.CA = g->d_CA; v.CB = g->d_CB; v.tri = g->d_tri;
     v.fq0 = g->f_q0; v.fq1 = g->f_q1; v.fcgT = g->f_cgT; v.fmm1 = g->f_mm1; v.fmm2 = g->f_mm2; v.fMr = g->f_Mr;
     v.fHL = g->f_HL; v.fGL = g->f_GL; v.fCA = g->f_CA; v.fCB = g->f_CB;
     return v;
@@ -565,7 +807,11 @@ static int ensure_work(BteWork* w, const BteGrid* g, int P, int prec) {
               A((void**)&w->scal, (size_t)P * SC_COUNT * sizeof(double)) &&
               A((void**)&w->scalt, (size_t)P * SC_COUNT * sizeof(double)) &&
               A((void**)&w->dh, (size_t)P * (N + 1) * sizeof(double)) &&
-              A((void**)&w->xs, (size_t)P * (N + 1) * sizeof(double)) && A((void**)&w->r, P * sizeof(double)) &&
+              A((void**)&w->xs, (size_t)P * (N + 1) * sizeof(double)) &&
+              A((void**)&w->sigma, (size_t)P * sizeof(double)) && A((void**)&w->srel, (size_t)P * sizeof(double)) &&
+              A((void**)&w->rowscale, (size_t)P * (N + 1) * sizeof(double)) && A((void**)&w->h0, pn) &&
+              A((void**)&w->ref_r, (size_t)P * sizeof(double)) && A((void**)&w->ref_r0, (size_t)P * sizeof(double)) &&
+              A((void**)&w->corr0, (size_t)P * sizeof(double)) && A((void**)&w->corr1, (size_t)P * sizeof(double)) && A((void**)&w->r, P * sizeof(double)) &&
               A((void**)&w->rt, P * sizeof(double)) && A((void**)&w->r0, P * sizeof(double)) &&
               A((void**)&w->alpha, P * sizeof(double)) && A(&w->J, jb) &&
               A((void**)&w->piv, (size_t)P * N * sizeof(int32_t)) && A((void**)&w->info, P * sizeof(int32_t)) &&
@@ -587,6 +833,253 @@ void bte_work_release(BteWork* w) {
     if (w) { free_work(w); delete w; }
 }
 
+// ---------------------------------------------------------------------------------
+// Library-wide launch counter and per-family CUDA-event timing (off unless enabled).
+// ---------------------------------------------------------------------------------
+enum { PF_RESIDUAL = 0, PF_JACOBIAN, PF_LU, PF_LUSOLVE, PF_REFINE, PF_OTHER, PF_COUNT };
+struct Profiler {
+    bool on = false;
+    long long launches = 0;
+    long long fallback = 0;  // points of the mixed form re-solved in FP64
+    long long fam_launches[PF_COUNT] = {0};
+    double fam_ms[PF_COUNT] = {0}, fam_flops[PF_COUNT] = {0}, fam_bytes[PF_COUNT] = {0};
+    struct Rec { int fam; cudaEvent_t a, b; double flops, bytes; };
+    std::vector<Rec> pending;
+    std::vector<cudaEvent_t> pool;
+    cudaEvent_t ev() {
+        if (pool.empty()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            return e;
+        }
+        cudaEvent_t e = pool.back();
+        pool.pop_back();
+        return e;
+    }
+    // time one launch (or launch group) of family `fam` with algorithmic flops / bytes
+    template <typename F>
+    cudaError_t run(int fam, cudaStream_t s, double flops, double bytes, int nlaunch, F&& f) {
+        launches += nlaunch;
+        fam_launches[fam] += nlaunch;
+        fam_flops[fam] += flops;
+        fam_bytes[fam] += bytes;
+        if (!on) { f(); return cudaGetLastError(); }
+        Rec r{fam, ev(), ev(), flops, bytes};
+        cudaEventRecord(r.a, s);
+        f();
+        cudaError_t e = cudaGetLastError();
+        cudaEventRecord(r.b, s);
+        pending.push_back(r);
+        return e;
+    }
+    void drain() {  // call after a stream synchronize
+        for (auto& r : pending) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, r.a, r.b);
+            fam_ms[r.fam] += ms;
+            pool.push_back(r.a);
+            pool.push_back(r.b);
+        }
+        pending.clear();
+    }
+    void reset(bool enable) {
+        drain();
+        on = enable;
+        launches = 0;
+        fallback = 0;
+        for (int i = 0; i < PF_COUNT; ++i) { fam_launches[i] = 0; fam_ms[i] = 0; fam_flops[i] = 0; fam_bytes[i] = 0; }
+    }
+};
+static Profiler g_prof;
+
+extern "C" int bte_stats_reset(int enable_timing) {
+    cudaDeviceSynchronize();
+    g_prof.reset(enable_timing != 0);
+    return BTE_OK;
+}
+
+// out[0] = kernel launches since the last reset; then for each family f in
+// {residual, jacobian, lu_factor, lu_solve, refine, other}: launches, total ms (CUDA
+// events, 0 when timing is off), algorithmic flops, algorithmic bytes; last: points of the
+// mixed form re-solved in FP64 -> 2 + 4 * 6 doubles.
+extern "C" int bte_stats(double* out, int count) {
+    if (!out || count < 2 + 4 * PF_COUNT) return BTE_ERR_ARG;
+    cudaDeviceSynchronize();
+    g_prof.drain();
+    out[0] = (double)g_prof.launches;
+    for (int f = 0; f < PF_COUNT; ++f) {
+        out[1 + 4 * f] = (double)g_prof.fam_launches[f];
+        out[2 + 4 * f] = g_prof.fam_ms[f];
+        out[3 + 4 * f] = g_prof.fam_flops[f];
+        out[4 + 4 * f] = g_prof.fam_bytes[f];
+    }
+    out[1 + 4 * PF_COUNT] = (double)g_prof.fallback;
+    return BTE_OK;
+}
+
+// algorithmic work per point (see DESIGN: per-unit figures of each kernel)
+static double res_flops_pt(const BteGrid* g, int ee) {
+    double n = g->n, nsp = g->nsp, tri = g->ntri;
+    double f = 2.0 * (nsp * nsp * g->nspecies + n * 7 * 4 + n * nsp);  // collisions, bands, M^-1 F
+    if (ee) f += 2.0 * (2 * n * nsp) + 2.0 * 2.0 * nsp * tri * 49.0;   // potentials, trilinear form
+    return f;
+}
+static double res_bytes_pt(const BteGrid* g, bool trial) {
+    double n = g->n;
+    return 8.0 * n * (1 + 1 + 4) + (trial ? 8.0 * (n + 1) + 8.0 * n : 0.0);  // h, F, aux (+ dh, h_trial)
+}
+static double jac_flops_pt(const BteGrid* g, int ee) {
+    double n = g->n, N = n + 1;
+    return ee ? 2.0 * (14.0 * n * n) + 4.0 * N * N : 4.0 * N * N;
+}
+static double lu_flops(int N) { return (2.0 / 3.0) * (double)N * N * N + (double)N * N; }
+
+// points with status >= 2 (not converged) -> act list; their status reset to running
+__global__ void k_collect_failed(int P, int* status, int* act_out, int* nout) {
+    int pt = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pt >= P) return;
+    if (status[pt] >= BTE_ST_MAXITER) {
+        status[pt] = -1;
+        act_out[atomicAdd(nout, 1)] = pt;
+    }
+}
+
+__global__ void k_restore(int n, int nact, const int* __restrict__ act, const double* __restrict__ h0, double* h) {
+    int slot = blockIdx.x;
+    if (slot >= nact) return;
+    int pt = act[slot];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) h[(size_t)pt * n + i] = h0[(size_t)pt * n + i];
+}
+
+struct SolveCtx {
+    BteGrid* g;
+    BteWork* w;
+    GridView gv;
+    PointParams pp;
+    int P, n, N, ld, ldd, ee;
+    long long jstride;
+    double beta_scale;
+    size_t res_smem, ref_smem;
+    const bte_solve_opts* o;
+    int32_t* status;
+    int32_t* iters;
+    cudaStream_t s;
+};
+
+// Newton iterations on the active list w->act[0..nact) whose F, aux, scal and r are current.
+static int newton_loop(SolveCtx& c, int nact, int prec, int max_iter) {
+    BteGrid* g = c.g;
+    BteWork* w = c.w;
+    const int n = c.n, N = c.N, ld = c.ld, ldd = c.ldd, ee = c.ee, P = c.P;
+    const long long jstride = c.jstride;
+    const double beta_scale = c.beta_scale;
+    const size_t res_smem = c.res_smem, ref_smem = c.ref_smem;
+    const bte_solve_opts* o = c.o;
+    GridView& gv = c.gv;
+    PointParams& pp = c.pp;
+    cudaStream_t s = c.s;
+    int32_t* status = c.status;
+    int32_t* iters = c.iters;
+    const double wsz = (prec == BTE_PREC_MIXED) ? 4.0 : 8.0;
+    const int nrefine = (prec == BTE_PREC_MIXED) ? std::min(std::max(o->refine, 0), 8) : 0;
+    // a mixed-form point that needs more than 13 halvings goes to the FP64 path instead
+    const double amin = (prec == BTE_PREC_MIXED) ? std::max(o->alpha_min, 1.0 / 8192.0) : o->alpha_min;
+    Profiler& pf = g_prof;
+    auto other = [&](auto&& fn) { return pf.run(PF_OTHER, s, 0, 0, 1, fn); };
+    for (int it = 0; it < max_iter && nact > 0; ++it) {
+        // Jacobian straight into the factorization buffer, then LU of [J | -F] and back substitution
+        dim3 gj(nblk(N, JAC_WARPS), nact);
+        const double jb = (double)nact * N * (N + 1) * wsz;
+        const double lub = 2.0 * (double)nact * N * (N + 1) * wsz;
+        const double lsb = (double)nact * (0.5 * N * (N + 1) * wsz + N * wsz);
+        cudaError_t le = cudaSuccess;
+        if (prec == BTE_PREC_MIXED) {
+            float* xs = reinterpret_cast<float*>(w->xs);
+            CKR(pf.run(PF_JACOBIAN, s, nact * jac_flops_pt(g, ee), jb, 1, [&] {
+                k_jacobian<float><<<gj, JAC_WARPS * 32, 0, s>>>(gv, pp, ee, w->act, nact, w->h, w->F, w->aux, w->scal,
+                                                                  (float*)w->J, ld, jstride, beta_scale, w->rowscale);
+            }));
+            CKR(pf.run(PF_LU, s, nact * lu_flops(N), lub, 1, [&] {
+                le = bte_lu_factor_t<float>(nact, N, N + 1, (float*)w->J, ld, jstride, w->piv, w->info, s);
+            }));
+            CKR(le);
+            CKR(pf.run(PF_LUSOLVE, s, nact * (double)N * N, lsb, 1, [&] {
+                le = bte_lu_solve_t<float>(nact, N, (const float*)w->J, ld, jstride, w->piv, xs, 1, s);
+            }));
+            CKR(le);
+            CKR(other([&] { k_store_solution<float><<<nact, 128, 0, s>>>(nact, xs, N, w->act, w->dh, ldd); }));
+            // FP64 iterative refinement of the step against the matrix-free FP64 Jacobian
+            for (int rf = 0; rf < nrefine; ++rf) {
+                CKR(pf.run(PF_REFINE, s, nact * (res_flops_pt(g, ee) + 2.0 * (double)N * N),
+                           nact * (res_bytes_pt(g, true) + 0.5 * N * (N + 1) * wsz), 3, [&] {
+                    k_refine_residual<<<nact, 256, ref_smem, s>>>(gv, pp, ee, w->act, nact, w->h, w->F, w->aux,
+                                                                  w->scal, w->dh, ldd, beta_scale, w->rowscale, xs,
+                                                                  w->sigma);
+                    le = bte_lu_solve_t<float>(nact, N, (const float*)w->J, ld, jstride, w->piv, xs, 0, s);
+                    k_refine_update<<<nact, 128, 0, s>>>(nact, w->act, N, xs, w->sigma, w->dh, ldd,
+                                                         rf == 0 ? w->corr0 : w->corr1);
+                }));
+                CKR(le);
+            }
+            if (nrefine >= 2)
+                CKR(other([&] { k_refine_check<<<nblk(nact, 256), 256, 0, s>>>(nact, w->act, w->corr0, w->corr1, status); }));
+        } else {
+            double* xs = w->xs;
+            CKR(pf.run(PF_JACOBIAN, s, nact * jac_flops_pt(g, ee), jb, 1, [&] {
+                k_jacobian<double><<<gj, JAC_WARPS * 32, 0, s>>>(gv, pp, ee, w->act, nact, w->h, w->F, w->aux, w->scal,
+                                                                   (double*)w->J, ld, jstride, beta_scale, w->rowscale);
+            }));
+            CKR(pf.run(PF_LU, s, nact * lu_flops(N), lub, 1, [&] {
+                le = bte_lu_factor_t<double>(nact, N, N + 1, (double*)w->J, ld, jstride, w->piv, w->info, s);
+            }));
+            CKR(le);
+            CKR(pf.run(PF_LUSOLVE, s, nact * (double)N * N, lsb, 1, [&] {
+                le = bte_lu_solve_t<double>(nact, N, (const double*)w->J, ld, jstride, w->piv, xs, 1, s);
+            }));
+            CKR(le);
+            CKR(other([&] { k_store_solution<double><<<nact, 128, 0, s>>>(nact, xs, N, w->act, w->dh, ldd); }));
+        }
+        // per-point Armijo backtracking
+        CKR(other([&] { k_fill_int<<<nblk(P, 256), 256, 0, s>>>(w->searching, 0, P); }));
+        CKR(other([&] { k_fill_int<<<nblk(P, 256), 256, 0, s>>>(w->accepted, 0, P); }));
+        CKR(other([&] { k_set_active<<<nblk(nact, 256), 256, 0, s>>>(nact, w->act, w->searching, w->alpha); }));
+        int nsearch = nact;
+        for (int ls = 0; ls < 200; ++ls) {
+            CKR(pf.run(PF_RESIDUAL, s, nsearch * res_flops_pt(g, ee), nsearch * res_bytes_pt(g, true), 1, [&] {
+                k_residual<<<nact, 256, res_smem, s>>>(gv, pp, ee, w->act, nact, w->h, w->dh, ldd, w->alpha,
+                                                       w->searching, w->ht, w->Ft, w->auxt, w->scalt, w->rt, w->srel);
+            }));
+            CKR(cudaMemsetAsync(w->cnt, 0, sizeof(int32_t), s));
+            CKR(other([&] {
+                k_armijo<<<nblk(nact, 256), 256, 0, s>>>(nact, w->act, w->searching, w->alpha, w->r, w->rt,
+                                                        o->line_search_c, o->alpha_rho, amin, status, w->cnt,
+                                                        w->accepted, w->r0, 1e-9, w->srel, 1e-10);
+            }));
+            int hc = 0;
+            CKR(cudaMemcpyAsync(&hc, w->cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+            CKR(cudaStreamSynchronize(s));
+            nsearch = hc;
+            if (hc == 0) break;
+        }
+        CKR(other([&] {
+            k_accept<<<nact, 256, 0, s>>>(n, nact, w->act, w->accepted, w->h, w->ht, w->F, w->Ft, w->aux, w->auxt,
+                                         w->scal, w->scalt, w->r, w->rt, iters);
+        }));
+        CKR(cudaMemsetAsync(w->cnt, 0, sizeof(int32_t), s));
+        CKR(other([&] {
+            k_converge<<<nblk(nact, 256), 256, 0, s>>>(nact, w->act, w->r, w->r0, o->atol, o->rtol,
+                                                      it + 1 == max_iter, status, w->act2, w->cnt, w->info, 0);
+        }));
+        int hn = 0;
+        CKR(cudaMemcpyAsync(&hn, w->cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        CKR(cudaStreamSynchronize(s));
+        pf.drain();
+        std::swap(w->act, w->act2);
+        nact = hn;
+    }
+    return BTE_OK;
+}
+
 int bte_solve_impl(BteGrid* g, int P, const double* n0, const double* ne, const double* ns_by_n0, const double* Tg,
                    const double* E, double* f, int32_t* status, int32_t* iters, const bte_solve_opts* o,
                    cudaStream_t s) {
@@ -595,85 +1088,75 @@ int bte_solve_impl(BteGrid* g, int P, const double* n0, const double* ne, const 
     const int prec = o->precision;
     int rc = ensure_work(w, g, P, prec);
     if (rc) return rc;
-    const int n = g->n, N = n + 1;
-    const int ld = (N + 1 + 3) & ~3;
-    const long long jstride = (long long)N * ld;
-    const int ee = (o->ee && g->ee) ? 1 : 0;
-    GridView gv = view_of(g);
-    PointParams pp{n0, ne, Tg, E, ns_by_n0, P};
+    SolveCtx c{};
+    c.g = g; c.w = w; c.gv = view_of(g); c.pp = PointParams{n0, ne, Tg, E, ns_by_n0, P};
+    c.P = P; c.n = g->n; c.N = g->n + 1; c.ld = (c.N + 1 + 3) & ~3; c.ldd = c.N + 1;
+    c.ee = (o->ee && g->ee) ? 1 : 0;
+    c.jstride = (long long)c.N * c.ld;
     // border scale: typical magnitude of the raw collision operator per unit n0
-    const double beta_scale = g->q0max / (g->umax > 0 ? g->umax : 1.0);
-    const size_t res_smem = (size_t)5 * n * sizeof(double);
-    if (res_smem > 48 * 1024) CKR(cudaFuncSetAttribute(k_residual, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)res_smem));
+    c.beta_scale = g->q0max / (g->umax > 0 ? g->umax : 1.0);
+    c.res_smem = (size_t)5 * c.n * sizeof(double);
+    c.ref_smem = (size_t)(5 * c.n + 1) * sizeof(double);
+    c.o = o; c.status = status; c.iters = iters; c.s = s;
+    const int n = c.n;
+    if (c.res_smem > 48 * 1024) CKR(cudaFuncSetAttribute(k_residual, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.res_smem));
+    if (c.ref_smem > 48 * 1024) CKR(cudaFuncSetAttribute(k_refine_residual, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.ref_smem));
+    Profiler& pf = g_prof;
+    auto other = [&](auto&& fn) { return pf.run(PF_OTHER, s, 0, 0, 1, fn); };
+    auto residual_all = [&](int nact) {
+        return pf.run(PF_RESIDUAL, s, nact * res_flops_pt(g, c.ee), nact * res_bytes_pt(g, false), 1, [&] {
+            k_residual<<<nact, 256, c.res_smem, s>>>(c.gv, c.pp, c.ee, w->act, nact, w->h, nullptr, 0, nullptr,
+                                                     nullptr, nullptr, w->F, w->aux, w->scal, w->r, nullptr);
+        });
+    };
 
-    k_mass_normalize<<<P, 256, 0, s>>>(n, g->d_u, f, w->h, P);
-    k_fill_int<<<nblk(P, 256), 256, 0, s>>>(status, -1, P);
-    k_fill_int<<<nblk(P, 256), 256, 0, s>>>(iters, 0, P);
-    k_iota<<<nblk(P, 256), 256, 0, s>>>(w->act, P);
-    CKR(cudaGetLastError());
-    k_residual<<<P, 256, res_smem, s>>>(gv, pp, ee, w->act, P, w->h, nullptr, 0, nullptr, nullptr, nullptr, w->F,
-                                        w->aux, w->scal, w->r);
-    CKR(cudaGetLastError());
+    CKR(other([&] { k_mass_normalize<<<P, 256, 0, s>>>(n, g->d_u, f, w->h, P); }));
+    CKR(cudaMemcpyAsync(w->h0, w->h, (size_t)P * n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CKR(other([&] { k_fill_int<<<nblk(P, 256), 256, 0, s>>>(status, -1, P); }));
+    CKR(other([&] { k_fill_int<<<nblk(P, 256), 256, 0, s>>>(iters, 0, P); }));
+    CKR(other([&] { k_iota<<<nblk(P, 256), 256, 0, s>>>(w->act, P); }));
+    CKR(residual_all(P));
     CKR(cudaMemcpyAsync(w->r0, w->r, P * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    int nact = P;
-    const int ldd = N + 1;
-    for (int it = 0; it < o->max_iter && nact > 0; ++it) {
-        // Jacobian straight into the factorization buffer, then LU of [J | -F]
-        dim3 gj(nblk(N, JAC_WARPS), nact);
-        if (prec == BTE_PREC_MIXED) {
-            k_jacobian<float><<<gj, JAC_WARPS * 32, 0, s>>>(gv, pp, ee, w->act, nact, w->h, w->F, w->aux, w->scal,
-                                                              (float*)w->J, ld, jstride, beta_scale);
-            CKR(cudaGetLastError());
-            CKR(bte_lu_factor_t<float>(nact, N, N + 1, (float*)w->J, ld, jstride, w->piv, w->info, s));
-        } else {
-            k_jacobian<double><<<gj, JAC_WARPS * 32, 0, s>>>(gv, pp, ee, w->act, nact, w->h, w->F, w->aux, w->scal,
-                                                               (double*)w->J, ld, jstride, beta_scale);
-            CKR(cudaGetLastError());
-            CKR(bte_lu_factor_t<double>(nact, N, N + 1, (double*)w->J, ld, jstride, w->piv, w->info, s));
-        }
-        // back substitution into dh (FP64 buffer indexed by point)
-        if (prec == BTE_PREC_MIXED) {
-            float* xs = reinterpret_cast<float*>(w->xs);
-            CKR(bte_lu_solve_t<float>(nact, N, (const float*)w->J, ld, jstride, w->piv, xs, 1, s));
-            k_store_solution<float><<<nact, 128, 0, s>>>(nact, xs, N, w->act, w->dh, ldd);
-        } else {
-            double* xs = w->xs;
-            CKR(bte_lu_solve_t<double>(nact, N, (const double*)w->J, ld, jstride, w->piv, xs, 1, s));
-            k_store_solution<double><<<nact, 128, 0, s>>>(nact, xs, N, w->act, w->dh, ldd);
-        }
-        CKR(cudaGetLastError());
-        // line search
-        k_fill_int<<<nblk(P, 256), 256, 0, s>>>(w->searching, 0, P);
-        k_fill_int<<<nblk(P, 256), 256, 0, s>>>(w->accepted, 0, P);
-        k_set_active<<<nblk(nact, 256), 256, 0, s>>>(nact, w->act, w->searching, w->alpha);
-        for (int ls = 0; ls < 200; ++ls) {
-            k_residual<<<nact, 256, res_smem, s>>>(gv, pp, ee, w->act, nact, w->h, w->dh, ldd, w->alpha, w->searching,
-                                                   w->ht, w->Ft, w->auxt, w->scalt, w->rt);
-            CKR(cudaMemsetAsync(w->cnt, 0, sizeof(int32_t), s));
-            k_armijo<<<nblk(nact, 256), 256, 0, s>>>(nact, w->act, w->searching, w->alpha, w->r, w->rt, o->line_search_c,
-                                                    o->alpha_rho, o->alpha_min, status, w->cnt, w->accepted, w->r0, 1e-9);
-            CKR(cudaGetLastError());
-            int hc = 0;
-            CKR(cudaMemcpyAsync(&hc, w->cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-            CKR(cudaStreamSynchronize(s));
-            if (hc == 0) break;
-        }
-        k_accept<<<nact, 256, 0, s>>>(n, nact, w->act, w->accepted, w->h, w->ht, w->F, w->Ft, w->aux, w->auxt, w->scal,
-                                     w->scalt, w->r, w->rt, iters);
+    const size_t rm_smem = (size_t)2 * n * sizeof(double);
+    if (rm_smem > 48 * 1024) CKR(cudaFuncSetAttribute(k_ref_merit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rm_smem));
+    CKR(other([&] { k_ref_merit<<<P, 256, rm_smem, s>>>(c.gv, P, w->F, w->ref_r0); }));
+    rc = newton_loop(c, P, prec, o->max_iter);
+    if (rc) return rc;
+    if (prec == BTE_PREC_MIXED) {
+        // points the mixed form did not converge restart from the initial state in FP64
         CKR(cudaMemsetAsync(w->cnt, 0, sizeof(int32_t), s));
-        k_converge<<<nblk(nact, 256), 256, 0, s>>>(nact, w->act, w->r, w->r0, o->atol, o->rtol,
-                                                  it + 1 == o->max_iter, status, w->act2, w->cnt, w->info, 0);
-        CKR(cudaGetLastError());
-        int hn = 0;
-        CKR(cudaMemcpyAsync(&hn, w->cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        CKR(other([&] { k_collect_failed<<<nblk(P, 256), 256, 0, s>>>(P, status, w->act2, w->cnt); }));
+        int nf = 0;
+        CKR(cudaMemcpyAsync(&nf, w->cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         CKR(cudaStreamSynchronize(s));
-        std::swap(w->act, w->act2);
-        nact = hn;
+        pf.fallback += nf;
+        // the J buffer holds FP32 matrices for P points: FP64 chunks of at most P / 2
+        const int chunk = std::max(1, P / 2);
+        std::vector<int32_t> failed(nf);
+        if (nf) CKR(cudaMemcpyAsync(failed.data(), w->act2, nf * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        CKR(cudaStreamSynchronize(s));
+        for (int c0 = 0; c0 < nf; c0 += chunk) {
+            int m = std::min(chunk, nf - c0);
+            CKR(cudaMemcpyAsync(w->act, failed.data() + c0, m * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+            CKR(other([&] { k_restore<<<m, 256, 0, s>>>(n, m, w->act, w->h0, w->h); }));
+            CKR(residual_all(m));
+            rc = newton_loop(c, m, BTE_PREC_FP64, o->max_iter);
+            if (rc) return rc;
+        }
     }
     const double c_gamma = std::sqrt(2.0 * (BTE_QE / BTE_ME));
     const double mm_fac = std::sqrt(1.0 / (4.0 * M_PI)) * 4.0 * M_PI;
     const double sc3 = 2.0 * std::pow(g->vth / c_gamma, 3);
-    k_normalized_distribution<<<P, 256, 0, s>>>(n, g->d_mass, mm_fac, sc3, w->h, f, P);
-    CKR(cudaGetLastError());
+    CKR(other([&] { k_normalized_distribution<<<P, 256, 0, s>>>(n, g->d_mass, mm_fac, sc3, w->h, f, P); }));
+    CKR(other([&] { k_ref_merit<<<P, 256, rm_smem, s>>>(c.gv, P, w->F, w->ref_r); }));
+    return BTE_OK;
+}
+
+// per-point residual norms of the last steady solve on this grid: r_final, r_initial
+int bte_solve_info_impl(BteGrid* g, int P, double* r_final, double* r_initial, cudaStream_t s) {
+    BteWork* w = g->work;
+    if (!w || w->cap < P) return BTE_ERR_STATE;
+    if (cudaMemcpyAsync(r_final, w->ref_r, P * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess) return BTE_ERR_CUDA;
+    if (cudaMemcpyAsync(r_initial, w->ref_r0, P * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess) return BTE_ERR_CUDA;
     return BTE_OK;
 }

@@ -63,7 +63,8 @@ typedef struct {
     double alpha_min, alpha_rho, line_search_c;  /* Armijo backtracking                       */
     int ee;                       /* include the e-e Coulomb term                              */
     int precision;                /* BTE_PREC_FP64 or BTE_PREC_MIXED                           */
-    int reserved[6];
+    int refine;                   /* mixed form: FP64 iterative-refinement passes per step (0-8) */
+    int reserved[5];
 } bte_solve_opts;
 
 /* Build a grid and assemble every operator on the device (FP64).
@@ -112,6 +113,11 @@ int bte_solve_steady(bte_grid* g, int P, const double* n0, const double* ne, con
                      const double* Tg, const double* E, double* f, int32_t* status, int32_t* iters,
                      const bte_solve_opts* opts, void* stream);
 
+/* Per-point merit norms ||Q^T M^-1 F|| of the last bte_solve_steady on this grid (device
+ * buffers [P]): at the returned state and at the initial state. Replaces the residual
+ * printout of steady_state_solve (bte_0d3v_batched.py:960-963, 970-971). */
+int bte_solve_info(bte_grid* g, int P, double* r_final, double* r_initial, void* stream);
+
 /* Quantities of interest of P normalized distributions (device f [P x n]); outputs
  * [P] each and rates [n_proc x P]. effective_mobility as in the reference.
  * Replaces bte_0d3v_batched.compute_QoIs (bte_0d3v_batched.py:1163-1202). */
@@ -138,6 +144,18 @@ int bte_lu_solve(int dtype, int P, int N, const void* A, int ld, long long strid
  * Replaces bte_0d3v_batched.compute_radial_components (bte_0d3v_batched.py:1219-1239). */
 int bte_radial_components(const bte_grid* g, int P, const double* f, int n_ev, const double* ev, double* out,
                           void* stream);
+
+/* Reset the library's kernel-launch counter and per-family statistics; enable_timing = 1
+ * also brackets every solver launch with CUDA events (small overhead).
+ * Replaces bte_0d3v_batched.profile_reset (bte_0d3v_batched.py:1241-1246). */
+int bte_stats_reset(int enable_timing);
+
+/* Statistics since the last reset: out[0] = kernel launches; then per family
+ * {residual, jacobian, lu_factor, lu_solve, refine, other}: launches, device ms,
+ * algorithmic flops, algorithmic bytes; out[25] = points of the mixed form that did not
+ * converge and were re-solved from their initial state in FP64 (count >= 26 doubles).
+ * Replaces bte_0d3v_batched.profile_stats (bte_0d3v_batched.py:1248-1315). */
+int bte_stats(double* out, int count);
 
 /* Last CUDA error string seen by the library on this thread (never NULL). */
 const char* bte_last_error(void);
