@@ -253,7 +253,7 @@ def run_gb300(a, rank, ws):
 
 
 def roofline(st, peaks):
-    fams = {k: v for k, v in st.items() if isinstance(v, dict)}
+    fams = {k: v for k, v in st.items() if isinstance(v, dict) and "ms" in v}
     dom = max(fams, key=lambda k: fams[k]["ms"])
     v = fams[dom]
     hbm = peaks.get("hbm_gbs")
@@ -345,6 +345,7 @@ def main():
                        "unit": "batch solve of %d points" % a.n_pts},
         "e2e": r["e2e"], "gpu_launches": st["launches"],
         "fp64_fallback_points_per_step": st["fp64_fallback_points"] / a.steps,
+        "fp64_fallback_reasons": st["fp64_fallback_reasons"],
         "roofline": roofline(st, peaks), "cpu_baseline": cpu, "clocks": r["clocks"],
         "plain_fp64": r["plain"], "setup_s": r["setup_s"],
         "newton_iters": {"mean": float(np.mean(r["iters"])), "max": int(np.max(r["iters"]))},

@@ -22,7 +22,7 @@ STATUS = {0: "converged", 1: "roundoff", 2: "max_iter", 3: "line_search", 4: "no
 
 EXPORTED = ["bte_grid_create", "bte_grid_destroy", "bte_grid_info", "bte_grid_export", "bte_initialize",
             "bte_solve_steady", "bte_qoi", "bte_lu_factor", "bte_lu_solve", "bte_last_error",
-            "bte_radial_components", "bte_stats_reset", "bte_stats", "bte_solve_info"]
+            "bte_radial_components", "bte_stats_reset", "bte_stats", "bte_solve_info", "bte_lu_factor_ex"]
 
 STAT_FAMILIES = ["residual", "jacobian", "lu_factor", "lu_solve", "refine", "other"]
 
@@ -76,6 +76,7 @@ def load() -> C.CDLL:
     lib.bte_qoi.argtypes = [vp, C.c_int, vp, vp, vp, C.c_int, vp, vp, vp, vp, vp]
     lib.bte_lu_factor.argtypes = [C.c_int, C.c_int, C.c_int, vp, C.c_int, C.c_longlong, vp, vp, vp]
     lib.bte_lu_solve.argtypes = [C.c_int, C.c_int, C.c_int, vp, C.c_int, C.c_longlong, vp, vp, vp]
+    lib.bte_lu_factor_ex.argtypes = [C.c_int, C.c_int, C.c_int, vp, C.c_int, C.c_longlong, vp, vp, C.c_int, vp]
     lib.bte_last_error.restype = C.c_char_p
     lib.bte_stats_reset.argtypes = [C.c_int]
     lib.bte_solve_info.argtypes = [vp, C.c_int, vp, vp, vp]
@@ -104,11 +105,13 @@ def stats_reset(timing: bool) -> None:
 
 def stats() -> dict:
     """Kernel launches and per-family (launches, device ms, algorithmic flops, bytes)."""
-    nb = 2 + 4 * len(STAT_FAMILIES)
+    nb = 2 + 4 * len(STAT_FAMILIES) + 5
     buf = (C.c_double * nb)()
     check(load().bte_stats(buf, nb), "bte_stats")
     out = {"launches": int(buf[0])}
     for i, f in enumerate(STAT_FAMILIES):
         out[f] = dict(launches=int(buf[1 + 4 * i]), ms=buf[2 + 4 * i], flops=buf[3 + 4 * i], bytes=buf[4 + 4 * i])
     out["fp64_fallback_points"] = int(buf[1 + 4 * len(STAT_FAMILIES)])
+    out["fp64_fallback_reasons"] = {k: int(buf[2 + 4 * len(STAT_FAMILIES) + i]) for i, k in
+                                    enumerate(["max_iter", "line_search", "non_finite", "singular", "refinement"])}
     return out

@@ -300,7 +300,7 @@ class bte_0d3v_batched:
         opts = _lib.SolveOpts(atol=float(atol), rtol=float(rtol), max_iter=int(max_iter), alpha_min=float(alpha_min),
                               alpha_rho=float(alpha_rho), line_search_c=float(line_search_c),
                               ee=int(getattr(self._args, "ee_collisions", 0)), precision=self._precision(),
-                              refine=int(getattr(self._args, "refine", 2)))
+                              refine=int(getattr(self._args, "refine", 4)))
         stream = torch.cuda.current_stream().cuda_stream
         _lib.check(_lib.load().bte_solve_steady(self._grid[grid_idx], n_pts, _ptr(n0), _ptr(ne), _ptr(ns), _ptr(Tg),
                                                 _ptr(E), _ptr(f), _ptr(status), _ptr(iters), C.byref(opts),

@@ -10,7 +10,7 @@
 
 template <typename T>
 cudaError_t bte_lu_factor_t(int P, int N, int NC, T* A, int ld, long long stride, int32_t* piv, int32_t* info,
-                            cudaStream_t s);
+                            cudaStream_t s, int kernel);
 template <typename T>
 cudaError_t bte_lu_solve_t(int P, int N, const T* A, int ld, long long stride, const int32_t* piv, T* b, int mode,
                            cudaStream_t s);
@@ -424,11 +424,17 @@ int bte_qoi(const bte_grid* g, int P, const double* f, const double* n0, const d
 
 int bte_lu_factor(int dtype, int P, int N, void* A, int ld, long long stride, int32_t* piv, int32_t* info,
                   void* stream) {
-    if (P < 0 || N < 1 || ld < N || stride < (long long)ld * N || !A || !piv || !info)
+    return bte_lu_factor_ex(dtype, P, N, A, ld, stride, piv, info, 0, stream);
+}
+
+int bte_lu_factor_ex(int dtype, int P, int N, void* A, int ld, long long stride, int32_t* piv, int32_t* info,
+                     int kernel, void* stream) {
+    if (P < 0 || N < 1 || N > 2048 || ld < N || stride < (long long)ld * N || !A || !piv || !info || kernel < 0 ||
+        kernel > 1)
         return fail(BTE_ERR_ARG, "bad LU arguments");
     cudaError_t e = (dtype == 0)
-                        ? bte_lu_factor_t<double>(P, N, N, (double*)A, ld, stride, piv, info, (cudaStream_t)stream)
-                        : bte_lu_factor_t<float>(P, N, N, (float*)A, ld, stride, piv, info, (cudaStream_t)stream);
+                        ? bte_lu_factor_t<double>(P, N, N, (double*)A, ld, stride, piv, info, (cudaStream_t)stream, kernel)
+                        : bte_lu_factor_t<float>(P, N, N, (float*)A, ld, stride, piv, info, (cudaStream_t)stream, kernel);
     CUDA_OR_FAIL(e, "bte_lu_factor");
     return BTE_OK;
 }

@@ -23,7 +23,7 @@
 
 template <typename T>
 cudaError_t bte_lu_factor_t(int P, int N, int NC, T* A, int ld, long long stride, int32_t* piv, int32_t* info,
-                            cudaStream_t s);
+                            cudaStream_t s, int kernel);
 template <typename T>
 cudaError_t bte_lu_solve_t(int P, int N, const T* A, int ld, long long stride, const int32_t* piv, T* b, int mode,
                            cudaStream_t s);
@@ -259,12 +259,18 @@ __global__ void __launch_bounds__(256)
 k_refine_residual(GridView g, PointParams pp, int ee, const int* __restrict__ act, int nact,
                   const double* __restrict__ h, const double* __restrict__ F, const double* __restrict__ aux,
                   const double* __restrict__ scal, const double* __restrict__ x, int ldd, double beta_scale,
-                  const double* __restrict__ rowscale, float* __restrict__ rs, double* __restrict__ sigma) {
+                  const double* __restrict__ rowscale, float* __restrict__ rs, double* __restrict__ sigma,
+                  const int* __restrict__ done) {
     extern __shared__ double sm[];
     const int slot = blockIdx.x;
     if (slot >= nact) return;
     const int pt = act[slot];
     const int n = g.n, nsh = g.nsh, nsp = g.nsp, N = n + 1, tid = threadIdx.x, nt = blockDim.x;
+    if (done[pt]) {  // refinement finished for this point: a zero correction
+        for (int i = tid; i < N; i += nt) rs[(size_t)slot * N + i] = 0.0f;
+        if (tid == 0) sigma[slot] = 0.0;
+        return;
+    }
     double* sx = sm;            // x (n + 1)
     double* sh = sm + N;        // h
     double* sxh = sh + n;       // HL x
@@ -393,11 +399,13 @@ k_refine_residual(GridView g, PointParams pp, int ee, const int* __restrict__ ac
 
 // x[pt] += sigma * y[slot]; corr[pt] = ||sigma * y|| / ||x|| of this pass
 __global__ void k_refine_update(int nact, const int* __restrict__ act, int N, const float* __restrict__ y,
-                                const double* __restrict__ sigma, double* x, int ldd, double* corr) {
+                                const double* __restrict__ sigma, double* x, int ldd, double* corr,
+                                const int* __restrict__ done) {
     __shared__ double red[32];
     int slot = blockIdx.x;
     if (slot >= nact) return;
     int pt = act[slot];
+    if (done[pt]) return;
     double sg = sigma[slot];
     double cc = 0.0, xx = 0.0;
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
@@ -412,16 +420,24 @@ __global__ void k_refine_update(int nact, const int* __restrict__ act, int N, co
     if (threadIdx.x == 0) corr[pt] = sqrt(cc / fmax(xx, 1e-300));
 }
 
-// after the refinement passes: a correction that did not shrink by 4x from the first
-// to the last pass (and is not already at round-off) means the FP32 factors cannot
-// resolve this point's Jacobian: hand the point to the FP64 path
-__global__ void k_refine_check(int nact, const int* __restrict__ act, const double* __restrict__ c_first,
-                               const double* __restrict__ c_last, int* status) {
+// After refinement pass p >= 1 (0-based), per point: a correction at round-off or 4x
+// smaller than the previous one ends the refinement; one that did not shrink (ratio
+// above 0.9) means the FP32 factors cannot resolve this point's Jacobian: the point goes
+// to the FP64 path. Otherwise keep refining (up to the pass limit).
+__global__ void k_refine_check(int nact, const int* __restrict__ act, const double* __restrict__ c_prev,
+                               const double* __restrict__ c_cur, int* status, int* done, int last) {
     int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= nact) return;
     int pt = act[slot];
-    double a = c_first[pt], b = c_last[pt];
-    if (!(b <= 0.25 * a || b <= 1e-13) && status[pt] < 0) status[pt] = BTE_ST_NEED_FP64;
+    if (done[pt]) return;
+    double a = c_prev[pt], b = c_cur[pt];
+    if (b <= 1e-13 || b <= 0.25 * a) { done[pt] = 1; return; }
+    if (!(b <= 0.9 * a)) {
+        if (status[pt] < 0) status[pt] = BTE_ST_NEED_FP64;
+        done[pt] = 1;
+        return;
+    }
+    if (last) done[pt] = 1;
 }
 
 // ---------------------------------------------------------------------------------
@@ -785,13 +801,15 @@ struct BteWork {
     double* h0 = nullptr;     // initial state (restart of points that fall back to FP64), P x n
     double *ref_r = nullptr, *ref_r0 = nullptr;  // the reference's merit at the end / start, P
     double *corr0 = nullptr, *corr1 = nullptr;   // relative refinement corrections, first / last pass
+    int32_t* reason = nullptr;                   // mixed-form status of each point before the FP64 pass
+    int32_t* refdone = nullptr;                  // refinement finished for the point in this Newton step
     void* J = nullptr;
     int32_t *piv = nullptr, *info = nullptr, *act = nullptr, *act2 = nullptr, *cnt = nullptr;
     int32_t *searching = nullptr, *accepted = nullptr;
 };
 
 static void free_work(BteWork* w) {
-    void* ptrs[] = {w->corr0, w->corr1, w->ref_r, w->ref_r0, w->rowscale, w->h0, w->srel, w->sigma, w->xs, w->h, w->ht, w->F, w->Ft, w->aux, w->auxt, w->scal, w->scalt, w->dh, w->r, w->rt, w->r0,
+    void* ptrs[] = {w->refdone, w->reason, w->corr0, w->corr1, w->ref_r, w->ref_r0, w->rowscale, w->h0, w->srel, w->sigma, w->xs, w->h, w->ht, w->F, w->Ft, w->aux, w->auxt, w->scal, w->scalt, w->dh, w->r, w->rt, w->r0,
                     w->alpha, w->J, w->piv, w->info, w->act, w->act2, w->cnt, w->searching, w->accepted};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -831,7 +849,8 @@ static int ensure_work(BteWork* w, const BteGrid* g, int P, int prec) {
               A((void**)&w->sigma, (size_t)P * sizeof(double)) && A((void**)&w->srel, (size_t)P * sizeof(double)) &&
               A((void**)&w->rowscale, (size_t)P * (N + 1) * sizeof(double)) && A((void**)&w->h0, pn) &&
               A((void**)&w->ref_r, (size_t)P * sizeof(double)) && A((void**)&w->ref_r0, (size_t)P * sizeof(double)) &&
-              A((void**)&w->corr0, (size_t)P * sizeof(double)) && A((void**)&w->corr1, (size_t)P * sizeof(double)) && A((void**)&w->r, P * sizeof(double)) &&
+              A((void**)&w->corr0, (size_t)P * sizeof(double)) && A((void**)&w->corr1, (size_t)P * sizeof(double)) &&
+              A((void**)&w->reason, (size_t)P * sizeof(int32_t)) && A((void**)&w->refdone, (size_t)P * sizeof(int32_t)) && A((void**)&w->r, P * sizeof(double)) &&
               A((void**)&w->rt, P * sizeof(double)) && A((void**)&w->r0, P * sizeof(double)) &&
               A((void**)&w->alpha, P * sizeof(double)) && A(&w->J, jb) &&
               A((void**)&w->piv, (size_t)P * N * sizeof(int32_t)) && A((void**)&w->info, P * sizeof(int32_t)) &&
@@ -861,6 +880,7 @@ struct Profiler {
     bool on = false;
     long long launches = 0;
     long long fallback = 0;  // points of the mixed form re-solved in FP64
+    long long fb_reason[8] = {0};  // ... by the status that sent them (2 max_iter .. 6 refinement)
     long long fam_launches[PF_COUNT] = {0};
     double fam_ms[PF_COUNT] = {0}, fam_flops[PF_COUNT] = {0}, fam_bytes[PF_COUNT] = {0};
     struct Rec { int fam; cudaEvent_t a, b; double flops, bytes; };
@@ -907,6 +927,7 @@ struct Profiler {
         on = enable;
         launches = 0;
         fallback = 0;
+        for (int i = 0; i < 8; ++i) fb_reason[i] = 0;
         for (int i = 0; i < PF_COUNT; ++i) { fam_launches[i] = 0; fam_ms[i] = 0; fam_flops[i] = 0; fam_bytes[i] = 0; }
     }
 };
@@ -934,6 +955,8 @@ extern "C" int bte_stats(double* out, int count) {
         out[4 + 4 * f] = g_prof.fam_bytes[f];
     }
     out[1 + 4 * PF_COUNT] = (double)g_prof.fallback;
+    if (count >= 2 + 4 * PF_COUNT + 5)
+        for (int i = 0; i < 5; ++i) out[2 + 4 * PF_COUNT + i] = (double)g_prof.fb_reason[2 + i];
     return BTE_OK;
 }
 
@@ -955,9 +978,10 @@ static double jac_flops_pt(const BteGrid* g, int ee) {
 static double lu_flops(int N) { return (2.0 / 3.0) * (double)N * N * N + (double)N * N; }
 
 // points with status >= 2 (not converged) -> act list; their status reset to running
-__global__ void k_collect_failed(int P, int* status, int* act_out, int* nout) {
+__global__ void k_collect_failed(int P, int* status, int* act_out, int* nout, int* reason) {
     int pt = blockIdx.x * blockDim.x + threadIdx.x;
     if (pt >= P) return;
+    reason[pt] = status[pt];
     if (status[pt] >= BTE_ST_MAXITER) {
         status[pt] = -1;
         act_out[atomicAdd(nout, 1)] = pt;
@@ -1020,7 +1044,7 @@ static int newton_loop(SolveCtx& c, int nact, int prec, int max_iter) {
                                                                   (float*)w->J, ld, jstride, beta_scale, w->rowscale);
             }));
             CKR(pf.run(PF_LU, s, nact * lu_flops(N), lub, 1, [&] {
-                le = bte_lu_factor_t<float>(nact, N, N + 1, (float*)w->J, ld, jstride, w->piv, w->info, s);
+                le = bte_lu_factor_t<float>(nact, N, N + 1, (float*)w->J, ld, jstride, w->piv, w->info, s, 0);
             }));
             CKR(le);
             CKR(pf.run(PF_LUSOLVE, s, nact * (double)N * N, lsb, 1, [&] {
@@ -1028,21 +1052,28 @@ static int newton_loop(SolveCtx& c, int nact, int prec, int max_iter) {
             }));
             CKR(le);
             CKR(other([&] { k_store_solution<float><<<nact, 128, 0, s>>>(nact, xs, N, w->act, w->dh, ldd); }));
-            // FP64 iterative refinement of the step against the matrix-free FP64 Jacobian
+            // FP64 iterative refinement of the step against the matrix-free FP64 Jacobian,
+            // per point until its correction contracts (or it is handed to FP64)
+            if (nrefine > 0) CKR(other([&] { k_fill_int<<<nblk(P, 256), 256, 0, s>>>(w->refdone, 0, P); }));
             for (int rf = 0; rf < nrefine; ++rf) {
+                double* cprev = (rf & 1) ? w->corr0 : w->corr1;
+                double* ccur = (rf & 1) ? w->corr1 : w->corr0;
                 CKR(pf.run(PF_REFINE, s, nact * (res_flops_pt(g, ee) + 2.0 * (double)N * N),
                            nact * (res_bytes_pt(g, true) + 0.5 * N * (N + 1) * wsz), 3, [&] {
                     k_refine_residual<<<nact, 256, ref_smem, s>>>(gv, pp, ee, w->act, nact, w->h, w->F, w->aux,
                                                                   w->scal, w->dh, ldd, beta_scale, w->rowscale, xs,
-                                                                  w->sigma);
+                                                                  w->sigma, w->refdone);
                     le = bte_lu_solve_t<float>(nact, N, (const float*)w->J, ld, jstride, w->piv, xs, 0, s);
-                    k_refine_update<<<nact, 128, 0, s>>>(nact, w->act, N, xs, w->sigma, w->dh, ldd,
-                                                         rf == 0 ? w->corr0 : w->corr1);
+                    k_refine_update<<<nact, 128, 0, s>>>(nact, w->act, N, xs, w->sigma, w->dh, ldd, ccur,
+                                                         w->refdone);
                 }));
                 CKR(le);
+                if (rf >= 1)
+                    CKR(other([&] {
+                        k_refine_check<<<nblk(nact, 256), 256, 0, s>>>(nact, w->act, cprev, ccur, status, w->refdone,
+                                                                       rf + 1 == nrefine);
+                    }));
             }
-            if (nrefine >= 2)
-                CKR(other([&] { k_refine_check<<<nblk(nact, 256), 256, 0, s>>>(nact, w->act, w->corr0, w->corr1, status); }));
         } else {
             double* xs = w->xs;
             CKR(pf.run(PF_JACOBIAN, s, nact * jac_flops_pt(g, ee), jb, 1, [&] {
@@ -1050,7 +1081,7 @@ static int newton_loop(SolveCtx& c, int nact, int prec, int max_iter) {
                                                                    (double*)w->J, ld, jstride, beta_scale, w->rowscale);
             }));
             CKR(pf.run(PF_LU, s, nact * lu_flops(N), lub, 1, [&] {
-                le = bte_lu_factor_t<double>(nact, N, N + 1, (double*)w->J, ld, jstride, w->piv, w->info, s);
+                le = bte_lu_factor_t<double>(nact, N, N + 1, (double*)w->J, ld, jstride, w->piv, w->info, s, 0);
             }));
             CKR(le);
             CKR(pf.run(PF_LUSOLVE, s, nact * (double)N * N, lsb, 1, [&] {
@@ -1145,7 +1176,7 @@ int bte_solve_impl(BteGrid* g, int P, const double* n0, const double* ne, const 
     if (prec == BTE_PREC_MIXED) {
         // points the mixed form did not converge restart from the initial state in FP64
         CKR(cudaMemsetAsync(w->cnt, 0, sizeof(int32_t), s));
-        CKR(other([&] { k_collect_failed<<<nblk(P, 256), 256, 0, s>>>(P, status, w->act2, w->cnt); }));
+        CKR(other([&] { k_collect_failed<<<nblk(P, 256), 256, 0, s>>>(P, status, w->act2, w->cnt, w->reason); }));
         int nf = 0;
         CKR(cudaMemcpyAsync(&nf, w->cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         CKR(cudaStreamSynchronize(s));
@@ -1155,6 +1186,14 @@ int bte_solve_impl(BteGrid* g, int P, const double* n0, const double* ne, const 
         std::vector<int32_t> failed(nf);
         if (nf) CKR(cudaMemcpyAsync(failed.data(), w->act2, nf * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         CKR(cudaStreamSynchronize(s));
+        if (nf && pf.on) {  // why they failed (statuses were reset to running by k_collect_failed)
+            std::vector<int32_t> st(P);
+            CKR(cudaMemcpy(st.data(), w->reason, P * sizeof(int32_t), cudaMemcpyDeviceToHost));
+            for (int i = 0; i < nf; ++i) {
+                int r = st[failed[i]];
+                if (r >= 0 && r < 8) pf.fb_reason[r]++;
+            }
+        }
         for (int c0 = 0; c0 < nf; c0 += chunk) {
             int m = std::min(chunk, nf - c0);
             CKR(cudaMemcpyAsync(w->act, failed.data() + c0, m * sizeof(int32_t), cudaMemcpyHostToDevice, s));

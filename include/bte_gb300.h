@@ -63,7 +63,10 @@ typedef struct {
     double alpha_min, alpha_rho, line_search_c;  /* Armijo backtracking                       */
     int ee;                       /* include the e-e Coulomb term                              */
     int precision;                /* BTE_PREC_FP64 or BTE_PREC_MIXED                           */
-    int refine;                   /* mixed form: FP64 iterative-refinement passes per step (0-8) */
+    int refine;                   /* mixed form: at most this many FP64 refinement passes per
+                                     Newton step (0-8); a point stops once its correction
+                                     contracts 4x, and goes to the FP64 path if it does not
+                                     contract at all                                          */
     int reserved[5];
 } bte_solve_opts;
 
@@ -126,13 +129,20 @@ int bte_qoi(const bte_grid* g, int P, const double* f, const double* n0, const d
             double* rates, void* stream);
 
 /* Batched dense LU with partial pivoting, in place, on P ROW-major N x N matrices
- * (A[r * ld + c]) with matrix stride `stride` (elements). dtype 0 = FP64, 1 = FP32.
- * piv [P x N] int32 receives the 0-based row interchanges in LAPACK order (row k was
- * swapped with piv[k], applied to every column); info [P] = 0 or the 1-based index of
- * the first zero pivot.
+ * (A[r * ld + c], N <= 2048) with matrix stride `stride` (elements). dtype 0 = FP64, 1 = FP32.
+ * Rows are not exchanged in memory: piv [P x N] int32 receives the permutation, and row
+ * perm[r] of the output holds row r of L\U (L unit lower). info [P] = 0 or the 1-based
+ * pivot position of the first zero pivot.
  * Replaces the xp.linalg.inv call of bte_0d3v_batched.batched_inv (bte_0d3v_batched.py:856-880). */
-int bte_lu_factor(int dtype, int P, int N, void* A, int ld, long long stride, int32_t* piv,
-                  int32_t* info, void* stream);
+int bte_lu_factor(int dtype, int P, int N, void* A, int ld, long long stride, int32_t* piv, int32_t* info,
+                  void* stream);
+
+/* As bte_lu_factor with an explicit kernel: 0 = automatic (FP32: left-looking with blocks
+ * resident in registers for N <= 512, right-looking above; FP64: right-looking),
+ * 1 = right-looking for every N.
+ * No counterpart in the reference; used to cross-check the two factorizations. */
+int bte_lu_factor_ex(int dtype, int P, int N, void* A, int ld, long long stride, int32_t* piv, int32_t* info,
+                     int kernel, void* stream);
 
 /* Solve A x = b for one right-hand side per matrix using bte_lu_factor's output;
  * b [P x N] (contiguous per point) is overwritten by x. Same dtype as the factors. */

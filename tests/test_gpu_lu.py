@@ -9,7 +9,8 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("N", [1, 7, 31, 64, 129, 385, 600, 1281])
 @pytest.mark.parametrize("dtype", ["f64", "f32"])
-def test_lu_factor_solve(N, dtype):
+@pytest.mark.parametrize("kernel", [0, 1], ids=["auto", "right"])
+def test_lu_factor_solve(N, dtype, kernel):
     import torch
     from boltzmann_gb300 import _lib
     lib = _lib.load()
@@ -24,8 +25,8 @@ def test_lu_factor_solve(N, dtype):
     info = torch.empty(P, dtype=torch.int32, device="cuda")
     dt = 0 if dtype == "f64" else 1
     st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
-    _lib.check(lib.bte_lu_factor(dt, P, N, C.c_void_p(dA.data_ptr()), N, N * N, C.c_void_p(piv.data_ptr()),
-                                 C.c_void_p(info.data_ptr()), st), "lu_factor")
+    _lib.check(lib.bte_lu_factor_ex(dt, P, N, C.c_void_p(dA.data_ptr()), N, N * N, C.c_void_p(piv.data_ptr()),
+                                    C.c_void_p(info.data_ptr()), kernel, st), "lu_factor")
     _lib.check(lib.bte_lu_solve(dt, P, N, C.c_void_p(dA.data_ptr()), N, N * N, C.c_void_p(piv.data_ptr()),
                                 C.c_void_p(db.data_ptr()), st), "lu_solve")
     torch.cuda.synchronize()
@@ -42,3 +43,21 @@ def test_lu_factor_solve(N, dtype):
     if dtype == "f64":
         ref = np.linalg.solve(A, b[..., None])[..., 0]
         assert np.max(np.linalg.norm(x - ref, axis=1) / np.linalg.norm(ref, axis=1)) < 1e-9
+
+
+def test_lu_zero_pivot_reported():
+    """A singular matrix reports the first zero pivot instead of faulting or returning NaN silently."""
+    import torch
+    from boltzmann_gb300 import _lib
+    lib = _lib.load()
+    N = 40
+    A = np.eye(N)
+    A[17, 17] = 0.0
+    dA = torch.as_tensor(A[None], device="cuda").contiguous()
+    piv = torch.empty((1, N), dtype=torch.int32, device="cuda")
+    info = torch.empty(1, dtype=torch.int32, device="cuda")
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.check(lib.bte_lu_factor(0, 1, N, C.c_void_p(dA.data_ptr()), N, N * N, C.c_void_p(piv.data_ptr()),
+                                 C.c_void_p(info.data_ptr()), st), "lu_factor")
+    torch.cuda.synchronize()
+    assert int(info.item()) == 18
