@@ -242,9 +242,14 @@ def run_gb300(a, rank, ws):
         err = np.linalg.norm(ff_mixed - ffp, axis=0) / np.linalg.norm(ffp, axis=0)
         qerr = {k: float(np.max(np.abs(q[k].cpu().numpy() - qp[k].cpu().numpy()) / np.abs(qp[k].cpu().numpy())))
                 for k in ("energy", "mobility", "diffusion")}
+        worst = np.argsort(err)[-5:][::-1]
         plain = {"value": a.n_pts * ws / (pms / 1e3), "ms_per_step": pms,
                  "mixed_speedup": (a.n_pts * ws / (ms / 1e3)) / (a.n_pts * ws / (pms / 1e3)),
                  "edf_max_rel_err_mixed_vs_fp64": float(np.max(err)), "qoi_max_rel_err_mixed_vs_fp64": qerr,
+                 "edf_rel_err_percentiles": {p: float(np.percentile(err, float(p))) for p in ("50", "90", "99", "99.9")},
+                 "points_above_1e-8": int(np.sum(err > 1e-8)),
+                 "worst_points": [{"EbyN_Td": float(prm["EbyN"][i]), "ion_deg": float(prm["ne"][i] / prm["n0"][i]),
+                                   "err": float(err[i])} for i in worst],
                  "status_counts": {str(k): int(v) for k, v in zip(*np.unique(qp["status"].cpu().numpy(), return_counts=True))}}
         del sp
     os.unlink(xs)

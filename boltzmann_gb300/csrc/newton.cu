@@ -496,13 +496,33 @@ template <typename T>
 __global__ void __launch_bounds__(JAC_WARPS * 32)
 k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int nact, const double* __restrict__ h,
            const double* __restrict__ F, const double* __restrict__ aux, const double* __restrict__ scal,
-           T* __restrict__ J, int ld, long long stride, double beta_scale, double* __restrict__ rowscale) {
+           T* __restrict__ J, int ld, long long stride, double beta_scale, double* __restrict__ rowscale,
+           int stage_hl) {
+    extern __shared__ __align__(16) unsigned char jsm[];
     const int slot = blockIdx.y;
     if (slot >= nact) return;
     const int pt = act[slot];
     const int n = g.n, nsh = g.nsh, nsp = g.nsp, N = n + 1;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int a = blockIdx.x * JAC_WARPS + wid;  // row
+    // rows of HL / GL this CTA's rows touch (p - 3 .. p + 3), staged in shared memory
+    const int a0 = blockIdx.x * JAC_WARPS;
+    const int prow0 = max(0, min(a0, n - 1) / nsh - BTE_BAND);
+    const int prow1 = min(nsp - 1, min(a0 + JAC_WARPS - 1, n - 1) / nsh + BTE_BAND);
+    const int nr = prow1 - prow0 + 1;
+    T* sHL = reinterpret_cast<T*>(jsm);
+    T* sGL = sHL + (size_t)nr * nsh * nsp;
+    if (stage_hl && ee) {
+        const T* HLg = OpsT<T>::HL(g);
+        const T* GLg = OpsT<T>::GL(g);
+        for (int e = threadIdx.x; e < nr * nsh * nsp; e += blockDim.x) {
+            const int sidx = e / (nr * nsp), rem = e % (nr * nsp);
+            const size_t src = ((size_t)sidx * nsp + prow0 + rem / nsp) * nsp + rem % nsp;
+            sHL[e] = HLg[src];
+            sGL[e] = GLg[src];
+        }
+        __syncthreads();
+    }
     if (a > n) return;
     T* Jr = J + (size_t)slot * stride + (size_t)a * ld;
     const double* hp = h + (size_t)pt * n;
@@ -573,8 +593,8 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
         // dense Coulomb product in T
         T acc = T(0);
         if (ee) {
-            const T* hl = HL + (size_t)s * nsp * nsp + c;
-            const T* gl = GL + (size_t)s * nsp * nsp + c;
+            const T* hl = stage_hl ? sHL + ((ptrdiff_t)s * nr - prow0) * nsp + c : HL + (size_t)s * nsp * nsp + c;
+            const T* gl = stage_hl ? sGL + ((ptrdiff_t)s * nr - prow0) * nsp + c : GL + (size_t)s * nsp * nsp + c;
 #pragma unroll
             for (int dr = 0; dr < BTE_NB; ++dr) {
                 int r = p + dr - BTE_BAND;
@@ -864,6 +884,21 @@ static int ensure_work(BteWork* w, const BteGrid* g, int P, int prec) {
 
 static inline unsigned nblk(int n, int b) { return (unsigned)((n + b - 1) / b); }
 
+// shared memory of a Jacobian CTA when its HL / GL rows are staged (0: read from global)
+template <typename T>
+static size_t jac_smem(const BteGrid* g, int ee) {
+    if (!ee) return 0;
+    const int rows = (JAC_WARPS + g->nsh - 1) / g->nsh + 1 + 2 * BTE_BAND;
+    size_t b = (size_t)2 * rows * g->nsh * g->nsp * sizeof(T);
+    if (b > 96 * 1024) return 0;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_jacobian<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+        attr_set = true;
+    }
+    return b;
+}
+
 BteWork* bte_work_get(BteGrid* g) {
     if (!g->work) g->work = new BteWork();
     return g->work;
@@ -1040,8 +1075,9 @@ static int newton_loop(SolveCtx& c, int nact, int prec, int max_iter) {
         if (prec == BTE_PREC_MIXED) {
             float* xs = reinterpret_cast<float*>(w->xs);
             CKR(pf.run(PF_JACOBIAN, s, nact * jac_flops_pt(g, ee), jb, 1, [&] {
-                k_jacobian<float><<<gj, JAC_WARPS * 32, 0, s>>>(gv, pp, ee, w->act, nact, w->h, w->F, w->aux, w->scal,
-                                                                  (float*)w->J, ld, jstride, beta_scale, w->rowscale);
+                k_jacobian<float><<<gj, JAC_WARPS * 32, jac_smem<float>(g, ee), s>>>(gv, pp, ee, w->act, nact, w->h, w->F, w->aux, w->scal,
+                                                                  (float*)w->J, ld, jstride, beta_scale, w->rowscale,
+                                                                  jac_smem<float>(g, ee) > 0);
             }));
             CKR(pf.run(PF_LU, s, nact * lu_flops(N), lub, 1, [&] {
                 le = bte_lu_factor_t<float>(nact, N, N + 1, (float*)w->J, ld, jstride, w->piv, w->info, s, 0);
@@ -1077,8 +1113,9 @@ static int newton_loop(SolveCtx& c, int nact, int prec, int max_iter) {
         } else {
             double* xs = w->xs;
             CKR(pf.run(PF_JACOBIAN, s, nact * jac_flops_pt(g, ee), jb, 1, [&] {
-                k_jacobian<double><<<gj, JAC_WARPS * 32, 0, s>>>(gv, pp, ee, w->act, nact, w->h, w->F, w->aux, w->scal,
-                                                                   (double*)w->J, ld, jstride, beta_scale, w->rowscale);
+                k_jacobian<double><<<gj, JAC_WARPS * 32, jac_smem<double>(g, ee), s>>>(gv, pp, ee, w->act, nact, w->h, w->F, w->aux, w->scal,
+                                                                   (double*)w->J, ld, jstride, beta_scale, w->rowscale,
+                                                                  jac_smem<double>(g, ee) > 0);
             }));
             CKR(pf.run(PF_LU, s, nact * lu_flops(N), lub, 1, [&] {
                 le = bte_lu_factor_t<double>(nact, N, N + 1, (double*)w->J, ld, jstride, w->piv, w->info, s, 0);
