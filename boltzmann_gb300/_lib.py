@@ -84,6 +84,8 @@ def load() -> C.CDLL:
     for name in EXPORTED:
         if not hasattr(lib, name):
             raise RuntimeError("libbte_gb300.so does not export %s" % name)
+    if hasattr(lib, "bte_initialize_noalloc"):
+        lib.bte_initialize_noalloc.argtypes = [vp, C.c_int, vp, vp]
     if hasattr(lib, "bte_radial_components"):
         lib.bte_radial_components.argtypes = [vp, C.c_int, vp, C.c_int, vp, vp, vp]
     if hasattr(lib, "bte_solve_transient"):

@@ -5,6 +5,7 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <mutex>
 #include "bte_common.cuh"
 #include "bte_grid.h"
 
@@ -379,6 +380,76 @@ int bte_initialize(const bte_grid* g, int P, double* f, void* stream) {
     CUDA_OR_FAIL(cudaGetLastError(), "k_maxwell");
     cudaFreeAsync(radial, s);
     cudaFreeAsync(dang, s);
+    CUDA_OR_FAIL(cudaStreamSynchronize(s), "initialize");
+    return BTE_OK;
+}
+
+} // extern "C"
+
+// Scratch of bte_initialize_noalloc: the radial projection of the Maxwellian (n_sp doubles,
+// from offset 0) and the angular factors (num_sh doubles, from offset
+// BTE_INIT_NOALLOC_MAX_NSP). Static device memory of this module, so every GPU that loads
+// the library holds these 4,160 bytes until the process exits. Host code must not pass
+// `g_init_scratch` itself to a kernel (on the host it names a stand-in, not device memory):
+// it passes the address that init_scratch_address looked up.
+static __device__ __align__(256) double g_init_scratch[BTE_INIT_NOALLOC_MAX_NSP + BTE_INIT_NOALLOC_MAX_SH];
+static_assert(BTE_INIT_NOALLOC_MAX_NSP == 512 && BTE_INIT_NOALLOC_MAX_SH == 8, "limits quoted in messages");
+#define BTE_NOALLOC_MAX_DEVICES 64
+static double* g_init_scratch_ptr[BTE_NOALLOC_MAX_DEVICES];
+static std::mutex g_init_scratch_mu;
+
+// Device address of g_init_scratch on `device` (which must be current); looked up once per
+// device on its first use, and cached.
+static int init_scratch_address(int device, double** out) {
+    if (device < 0 || device >= BTE_NOALLOC_MAX_DEVICES)
+        return fail(BTE_ERR_ARG, "bte_initialize_noalloc: device index beyond the library's table of 64 devices");
+    std::lock_guard<std::mutex> lock(g_init_scratch_mu);
+    if (!g_init_scratch_ptr[device]) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_init_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "bte_initialize_noalloc: cudaGetSymbolAddress of the scratch");
+        g_init_scratch_ptr[device] = (double*)ptr;
+    }
+    *out = g_init_scratch_ptr[device];
+    return BTE_OK;
+}
+
+extern "C" {
+
+int bte_initialize_noalloc(const bte_grid* g, int P, double* f, void* stream) {
+    if (!g || !f || P < 0) return fail(BTE_ERR_ARG, "bad argument");
+    if (g->nsp > BTE_INIT_NOALLOC_MAX_NSP || g->nsh > BTE_INIT_NOALLOC_MAX_SH)
+        return fail(BTE_ERR_ARG, "bte_initialize_noalloc: grid too large for the static scratch "
+                                 "(needs n_sp <= 512 and num_sh <= 8); use bte_initialize");
+    if (P == 0) return BTE_OK;
+    CUDA_OR_FAIL(cudaSetDevice(g->device), "cudaSetDevice");
+    double* scratch = nullptr;
+    int rc = init_scratch_address(g->device, &scratch);
+    if (rc != BTE_OK) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    // angular factors on the host stack: the 2-point Gauss-Legendre rule in cos(theta)
+    // (nodes -+1/sqrt(3), weights 1) times the 2-point periodic trapezoid in phi
+    double ang[BTE_INIT_NOALLOC_MAX_SH];
+    const double node = 1.0 / std::sqrt(3.0);
+    for (int l = 0; l < g->nsh; ++l) {
+        double acc = 0.0;
+        for (int i = 0; i < 2; ++i) {
+            const double mu = (i == 0) ? -node : node;
+            double p0 = 1.0, p1 = mu, Pl = (l == 0) ? 1.0 : mu;
+            for (int k = 2; k <= l; ++k) { Pl = ((2.0 * k - 1.0) * mu * p1 - (k - 1.0) * p0) / k; p0 = p1; p1 = Pl; }
+            acc += std::sqrt((2.0 * l + 1) / (4.0 * M_PI)) * Pl;
+        }
+        ang[l] = acc * (2.0 * M_PI / 2.0) * 2.0;
+    }
+    // both scratch regions are written in full (radial by k_maxwell_rhs, ang by the copy)
+    // before they are read, so nothing left by an earlier call needs clearing
+    double* radial = scratch;
+    double* dang = scratch + BTE_INIT_NOALLOC_MAX_NSP;
+    CUDA_OR_FAIL(cudaMemcpyAsync(dang, ang, g->nsh * sizeof(double), cudaMemcpyHostToDevice, s), "copy");
+    k_maxwell_rhs<<<(g->nsp + 127) / 128, 128, 0, s>>>(g->nsp, g->d_span_iv, g->q5.q, g->q5.x, g->q5.w, g->q5.span,
+                                                      g->q5.B, radial);
+    k_maxwell_fill<<<(g->n + 127) / 128, 128, 0, s>>>(g->nsp, g->nsh, g->d_Minv, radial, dang, f, P);
+    CUDA_OR_FAIL(cudaGetLastError(), "k_maxwell");
     CUDA_OR_FAIL(cudaStreamSynchronize(s), "initialize");
     return BTE_OK;
 }

@@ -107,6 +107,27 @@ int bte_grid_export(const bte_grid* g, int which, double* out, size_t count, voi
  * Replaces bte_0d3v_batched.initialize(grid, n_pts, "maxwellian") (bte_0d3v_batched.py:481-520). */
 int bte_initialize(const bte_grid* g, int P, double* f, void* stream);
 
+/* The Maxwellian initial state of bte_initialize (equal to round-off), from a call that
+ * allocates no device memory. It is meant for callers that cannot allocate at the point where
+ * they initialize points: a serving process whose device memory is all reserved by another
+ * allocator (a caching allocator that holds the whole pool, or a job at its memory cap),
+ * where a stream-ordered allocation can fail with out-of-memory or stall while the pool
+ * grows. The call's scratch (the radial projection, n_sp doubles, and the angular factors,
+ * num_sh doubles) lives in one static device array of the library, 4,160 bytes, which every
+ * GPU that loads the library holds until the process exits; grids with
+ * n_sp > BTE_INIT_NOALLOC_MAX_NSP or num_sh > BTE_INIT_NOALLOC_MAX_SH are rejected with
+ * BTE_ERR_ARG and a message naming the limit. The caller passes f as for bte_initialize.
+ * The first call on each device looks up the scratch's device address (this can load the
+ * library's device code), so make that first call during set-up, before any stream capture.
+ * All calls on a device share the one scratch array: calls that overlap on the GPU (other
+ * streams, other host threads) race on it, so the caller serialises them. Every element
+ * read is written earlier in the same call, so nothing in the scratch needs to start at
+ * zero. Synchronizes `stream` before returning, as bte_initialize does.
+ * No counterpart in the reference: an addition of this library. */
+#define BTE_INIT_NOALLOC_MAX_NSP 512
+#define BTE_INIT_NOALLOC_MAX_SH 8
+int bte_initialize_noalloc(const bte_grid* g, int P, double* f, void* stream);
+
 /* Steady-state solve of P independent points. Device inputs n0, ne, Tg, E [P],
  * ns_by_n0 [n_species x P]; f [P x n] in: initial state (any positive multiple),
  * out: the normalized distribution (normalized_distribution). status/iters [P] int32.
