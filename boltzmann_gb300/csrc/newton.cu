@@ -15,6 +15,8 @@
 //   Jacobian   FP64 (plain) or FP32 (mixed) straight into the factorization buffer
 //   LU         FP64 or FP32, right-hand side appended as column n+1
 #include <cstdio>
+#include <mutex>
+#include <deque>
 #include <vector>
 #include <algorithm>
 #include <cmath>
@@ -43,6 +45,7 @@ struct GridView {
 struct PointParams {
     const double *n0, *ne, *Tg, *E, *ns;  // ns: n_species x P (species-major)
     int P;
+    const int8_t* eept;  // per-point e-e switch (a serving engine's warm-start phase); null: the launch's `ee`
 };
 
 // per-point scalar slots
@@ -62,6 +65,7 @@ k_residual(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
     const int slot = blockIdx.x;
     if (slot >= nact) return;
     const int pt = act[slot];
+    if (pp.eept) ee = pp.eept[pt];
     if (need && !need[pt]) return;
     const int n = g.n, nsh = g.nsh, nsp = g.nsp, tid = threadIdx.x, nt = blockDim.x;
     double* sh = sm;           // h
@@ -217,11 +221,11 @@ k_residual(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
 // The reference's merit ||(I - p p^T) M^-1 F|| = ||Q^T M^-1 F|| (bte_0d3v_batched.py:920-926)
 // of stored raw residuals, for reporting (one CTA per point).
 __global__ void __launch_bounds__(256)
-k_ref_merit(GridView g, int P, const double* __restrict__ F, double* out) {
+k_ref_merit(GridView g, int P, const int* __restrict__ list, const double* __restrict__ F, double* out) {
     extern __shared__ double sm[];
     __shared__ double red[32];
-    const int pt = blockIdx.x;
-    if (pt >= P) return;
+    if ((int)blockIdx.x >= P) return;
+    const int pt = list ? list[blockIdx.x] : (int)blockIdx.x;
     const int n = g.n, nsh = g.nsh, nsp = g.nsp, tid = threadIdx.x, nt = blockDim.x;
     double* sF = sm;
     double* sR = sm + n;
@@ -265,6 +269,7 @@ k_refine_residual(GridView g, PointParams pp, int ee, const int* __restrict__ ac
     const int slot = blockIdx.x;
     if (slot >= nact) return;
     const int pt = act[slot];
+    if (pp.eept) ee = pp.eept[pt];
     const int n = g.n, nsh = g.nsh, nsp = g.nsp, N = n + 1, tid = threadIdx.x, nt = blockDim.x;
     if (done[pt]) {  // refinement finished for this point: a zero correction
         for (int i = tid; i < N; i += nt) rs[(size_t)slot * N + i] = 0.0f;
@@ -502,6 +507,7 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
     const int slot = blockIdx.y;
     if (slot >= nact) return;
     const int pt = act[slot];
+    if (pp.eept) ee = pp.eept[pt];
     const int n = g.n, nsh = g.nsh, nsp = g.nsp, N = n + 1;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int a = blockIdx.x * JAC_WARPS + wid;  // row
@@ -767,17 +773,18 @@ __global__ void k_accept(int n, int nact, const int* __restrict__ act, const int
 
 // convergence test and compaction of the active list
 __global__ void k_converge(int nact, const int* __restrict__ act, const double* __restrict__ r,
-                           const double* __restrict__ r0, double atol, double rtol, int last, int* status,
-                           int* act_out, int* nout, const int32_t* __restrict__ info, int check_info) {
+                           const double* __restrict__ r0, double atol, double rtol, int* nit, int max_iter,
+                           int* status, int* act_out, int* nout, const int32_t* __restrict__ info, int check_info) {
     int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= nact) return;
     int pt = act[slot];
     int st = status[pt];
+    const int it = ++nit[pt];  // Newton iterations of this point in its current solve
     if (st < 0) {
         if (!isfinite(r[pt])) st = BTE_ST_NONFINITE;
         else if (r[pt] <= atol + rtol * r0[pt]) st = BTE_ST_CONVERGED;
         else if (check_info && info[slot] != 0) st = BTE_ST_SINGULAR;
-        else if (last) st = BTE_ST_MAXITER;
+        else if (it >= max_iter) st = BTE_ST_MAXITER;
         status[pt] = st;
     }
     if (st < 0) {
@@ -823,13 +830,14 @@ struct BteWork {
     double *corr0 = nullptr, *corr1 = nullptr;   // relative refinement corrections, first / last pass
     int32_t* reason = nullptr;                   // mixed-form status of each point before the FP64 pass
     int32_t* refdone = nullptr;                  // refinement finished for the point in this Newton step
+    int32_t* nit = nullptr;                      // Newton iterations of each point in its current solve
     void* J = nullptr;
     int32_t *piv = nullptr, *info = nullptr, *act = nullptr, *act2 = nullptr, *cnt = nullptr;
     int32_t *searching = nullptr, *accepted = nullptr;
 };
 
 static void free_work(BteWork* w) {
-    void* ptrs[] = {w->refdone, w->reason, w->corr0, w->corr1, w->ref_r, w->ref_r0, w->rowscale, w->h0, w->srel, w->sigma, w->xs, w->h, w->ht, w->F, w->Ft, w->aux, w->auxt, w->scal, w->scalt, w->dh, w->r, w->rt, w->r0,
+    void* ptrs[] = {w->nit, w->refdone, w->reason, w->corr0, w->corr1, w->ref_r, w->ref_r0, w->rowscale, w->h0, w->srel, w->sigma, w->xs, w->h, w->ht, w->F, w->Ft, w->aux, w->auxt, w->scal, w->scalt, w->dh, w->r, w->rt, w->r0,
                     w->alpha, w->J, w->piv, w->info, w->act, w->act2, w->cnt, w->searching, w->accepted};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -870,7 +878,8 @@ static int ensure_work(BteWork* w, const BteGrid* g, int P, int prec) {
               A((void**)&w->rowscale, (size_t)P * (N + 1) * sizeof(double)) && A((void**)&w->h0, pn) &&
               A((void**)&w->ref_r, (size_t)P * sizeof(double)) && A((void**)&w->ref_r0, (size_t)P * sizeof(double)) &&
               A((void**)&w->corr0, (size_t)P * sizeof(double)) && A((void**)&w->corr1, (size_t)P * sizeof(double)) &&
-              A((void**)&w->reason, (size_t)P * sizeof(int32_t)) && A((void**)&w->refdone, (size_t)P * sizeof(int32_t)) && A((void**)&w->r, P * sizeof(double)) &&
+              A((void**)&w->reason, (size_t)P * sizeof(int32_t)) && A((void**)&w->refdone, (size_t)P * sizeof(int32_t)) &&
+              A((void**)&w->nit, (size_t)P * sizeof(int32_t)) && A((void**)&w->r, P * sizeof(double)) &&
               A((void**)&w->rt, P * sizeof(double)) && A((void**)&w->r0, P * sizeof(double)) &&
               A((void**)&w->alpha, P * sizeof(double)) && A(&w->J, jb) &&
               A((void**)&w->piv, (size_t)P * N * sizeof(int32_t)) && A((void**)&w->info, P * sizeof(int32_t)) &&
@@ -912,13 +921,16 @@ void bte_work_release(BteWork* w) {
 // ---------------------------------------------------------------------------------
 enum { PF_RESIDUAL = 0, PF_JACOBIAN, PF_LU, PF_LUSOLVE, PF_REFINE, PF_OTHER, PF_COUNT };
 struct Profiler {
+    // shared by every solve and serving engine of the process; engines driven from several
+    // host threads record into it concurrently, so every member is guarded by `mu`
+    std::mutex mu;
     bool on = false;
     long long launches = 0;
     long long fallback = 0;  // points of the mixed form re-solved in FP64
     long long fb_reason[8] = {0};  // ... by the status that sent them (2 max_iter .. 6 refinement)
     long long fam_launches[PF_COUNT] = {0};
     double fam_ms[PF_COUNT] = {0}, fam_flops[PF_COUNT] = {0}, fam_bytes[PF_COUNT] = {0};
-    struct Rec { int fam; cudaEvent_t a, b; double flops, bytes; };
+    struct Rec { int fam; cudaStream_t s; cudaEvent_t a, b; double flops, bytes; };
     std::vector<Rec> pending;
     std::vector<cudaEvent_t> pool;
     cudaEvent_t ev() {
@@ -934,12 +946,13 @@ struct Profiler {
     // time one launch (or launch group) of family `fam` with algorithmic flops / bytes
     template <typename F>
     cudaError_t run(int fam, cudaStream_t s, double flops, double bytes, int nlaunch, F&& f) {
+        std::lock_guard<std::mutex> lock(mu);
         launches += nlaunch;
         fam_launches[fam] += nlaunch;
         fam_flops[fam] += flops;
         fam_bytes[fam] += bytes;
         if (!on) { f(); return cudaGetLastError(); }
-        Rec r{fam, ev(), ev(), flops, bytes};
+        Rec r{fam, s, ev(), ev(), flops, bytes};
         cudaEventRecord(r.a, s);
         f();
         cudaError_t e = cudaGetLastError();
@@ -947,18 +960,32 @@ struct Profiler {
         pending.push_back(r);
         return e;
     }
-    void drain() {  // call after a stream synchronize
-        for (auto& r : pending) {
+    void count_fallback(long long n, const long long* reasons) {
+        std::lock_guard<std::mutex> lock(mu);
+        fallback += n;
+        if (reasons)
+            for (int i = 0; i < 8; ++i) fb_reason[i] += reasons[i];
+    }
+    void drain_locked(cudaStream_t s, bool all) {
+        size_t keep = 0;
+        for (size_t i = 0; i < pending.size(); ++i) {
+            Rec& r = pending[i];
+            if (!all && r.s != s) { pending[keep++] = r; continue; }
             float ms = 0.f;
             cudaEventElapsedTime(&ms, r.a, r.b);
             fam_ms[r.fam] += ms;
             pool.push_back(r.a);
             pool.push_back(r.b);
         }
-        pending.clear();
+        pending.resize(keep);
     }
-    void reset(bool enable) {
-        drain();
+    void drain(cudaStream_t s) {  // after stream `s` was synchronized: its records are complete
+        std::lock_guard<std::mutex> lock(mu);
+        drain_locked(s, false);
+    }
+    void reset(bool enable) {  // after a device synchronize
+        std::lock_guard<std::mutex> lock(mu);
+        drain_locked(nullptr, true);
         on = enable;
         launches = 0;
         fallback = 0;
@@ -981,7 +1008,8 @@ extern "C" int bte_stats_reset(int enable_timing) {
 extern "C" int bte_stats(double* out, int count) {
     if (!out || count < 2 + 4 * PF_COUNT) return BTE_ERR_ARG;
     cudaDeviceSynchronize();
-    g_prof.drain();
+    std::lock_guard<std::mutex> lock(g_prof.mu);
+    g_prof.drain_locked(nullptr, true);
     out[0] = (double)g_prof.launches;
     for (int f = 0; f < PF_COUNT; ++f) {
         out[1 + 4 * f] = (double)g_prof.fam_launches[f];
@@ -995,7 +1023,7 @@ extern "C" int bte_stats(double* out, int count) {
     return BTE_OK;
 }
 
-// algorithmic work per point (see DESIGN: per-unit figures of each kernel)
+// algorithmic work per point of each kernel family (flops; bytes moved to and from HBM)
 static double res_flops_pt(const BteGrid* g, int ee) {
     double n = g->n, nsp = g->nsp, tri = g->ntri;
     double f = 2.0 * (nsp * nsp * g->nspecies + n * 7 * 4 + n * nsp);  // collisions, bands, M^-1 F
@@ -1023,10 +1051,15 @@ __global__ void k_collect_failed(int P, int* status, int* act_out, int* nout, in
     }
 }
 
-__global__ void k_restore(int n, int nact, const int* __restrict__ act, const double* __restrict__ h0, double* h) {
+// a point handed over because its refinement stalled keeps its last accepted iterate (every
+// iterate the mixed form accepted decreased the FP64 merit); the others restart from h0
+__global__ void k_restore(int n, int nact, const int* __restrict__ act, const int* __restrict__ reason,
+                          const double* __restrict__ h0, double* h, int* nit) {
     int slot = blockIdx.x;
     if (slot >= nact) return;
     int pt = act[slot];
+    if (threadIdx.x == 0) nit[pt] = 0;
+    if (reason[pt] == BTE_ST_NEED_FP64) return;
     for (int i = threadIdx.x; i < n; i += blockDim.x) h[(size_t)pt * n + i] = h0[(size_t)pt * n + i];
 }
 
@@ -1045,8 +1078,21 @@ struct SolveCtx {
     cudaStream_t s;
 };
 
-// Newton iterations on the active list w->act[0..nact) whose F, aux, scal and r are current.
-static int newton_loop(SolveCtx& c, int nact, int prec, int max_iter) {
+// One active list of points and the buffers indexed by position in it (Jacobians, pivots,
+// LU solutions, row scales, refinement scalings). A standalone solve runs one lane at a time;
+// a serving engine keeps a mixed-precision lane and an FP64 lane.
+struct Lane {
+    int32_t *act, *act2;
+    void* J;
+    int32_t *piv, *info;
+    double *xs, *rowscale, *sigma;
+};
+
+// One Newton iteration (Jacobian, factorization, step, refinement, line search, acceptance,
+// convergence test) for the `nact` points of lane L whose F, aux, scal and r are current;
+// returns the points still running, whose list is then L.act (the list before the
+// iteration is left in L.act2), or a negative code.
+static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
     BteGrid* g = c.g;
     BteWork* w = c.w;
     const int n = c.n, N = c.N, ld = c.ld, ldd = c.ldd, ee = c.ee, P = c.P;
@@ -1065,7 +1111,7 @@ static int newton_loop(SolveCtx& c, int nact, int prec, int max_iter) {
     const double amin = (prec == BTE_PREC_MIXED) ? std::max(o->alpha_min, 1.0 / 8192.0) : o->alpha_min;
     Profiler& pf = g_prof;
     auto other = [&](auto&& fn) { return pf.run(PF_OTHER, s, 0, 0, 1, fn); };
-    for (int it = 0; it < max_iter && nact > 0; ++it) {
+    {
         // Jacobian straight into the factorization buffer, then LU of [J | -F] and back substitution
         dim3 gj(nblk(N, JAC_WARPS), nact);
         const double jb = (double)nact * N * (N + 1) * wsz;
@@ -1073,21 +1119,21 @@ static int newton_loop(SolveCtx& c, int nact, int prec, int max_iter) {
         const double lsb = (double)nact * (0.5 * N * (N + 1) * wsz + N * wsz);
         cudaError_t le = cudaSuccess;
         if (prec == BTE_PREC_MIXED) {
-            float* xs = reinterpret_cast<float*>(w->xs);
+            float* xs = reinterpret_cast<float*>(L.xs);
             CKR(pf.run(PF_JACOBIAN, s, nact * jac_flops_pt(g, ee), jb, 1, [&] {
-                k_jacobian<float><<<gj, JAC_WARPS * 32, jac_smem<float>(g, ee), s>>>(gv, pp, ee, w->act, nact, w->h, w->F, w->aux, w->scal,
-                                                                  (float*)w->J, ld, jstride, beta_scale, w->rowscale,
+                k_jacobian<float><<<gj, JAC_WARPS * 32, jac_smem<float>(g, ee), s>>>(gv, pp, ee, L.act, nact, w->h, w->F, w->aux, w->scal,
+                                                                  (float*)L.J, ld, jstride, beta_scale, L.rowscale,
                                                                   jac_smem<float>(g, ee) > 0);
             }));
             CKR(pf.run(PF_LU, s, nact * lu_flops(N), lub, 1, [&] {
-                le = bte_lu_factor_t<float>(nact, N, N + 1, (float*)w->J, ld, jstride, w->piv, w->info, s, 0);
+                le = bte_lu_factor_t<float>(nact, N, N + 1, (float*)L.J, ld, jstride, L.piv, L.info, s, 0);
             }));
             CKR(le);
             CKR(pf.run(PF_LUSOLVE, s, nact * (double)N * N, lsb, 1, [&] {
-                le = bte_lu_solve_t<float>(nact, N, (const float*)w->J, ld, jstride, w->piv, xs, 1, s);
+                le = bte_lu_solve_t<float>(nact, N, (const float*)L.J, ld, jstride, L.piv, xs, 1, s);
             }));
             CKR(le);
-            CKR(other([&] { k_store_solution<float><<<nact, 128, 0, s>>>(nact, xs, N, w->act, w->dh, ldd); }));
+            CKR(other([&] { k_store_solution<float><<<nact, 128, 0, s>>>(nact, xs, N, L.act, w->dh, ldd); }));
             // FP64 iterative refinement of the step against the matrix-free FP64 Jacobian,
             // per point until its correction contracts (or it is handed to FP64)
             if (nrefine > 0) CKR(other([&] { k_fill_int<<<nblk(P, 256), 256, 0, s>>>(w->refdone, 0, P); }));
@@ -1096,50 +1142,50 @@ static int newton_loop(SolveCtx& c, int nact, int prec, int max_iter) {
                 double* ccur = (rf & 1) ? w->corr1 : w->corr0;
                 CKR(pf.run(PF_REFINE, s, nact * (res_flops_pt(g, ee) + 2.0 * (double)N * N),
                            nact * (res_bytes_pt(g, true) + 0.5 * N * (N + 1) * wsz), 3, [&] {
-                    k_refine_residual<<<nact, 256, ref_smem, s>>>(gv, pp, ee, w->act, nact, w->h, w->F, w->aux,
-                                                                  w->scal, w->dh, ldd, beta_scale, w->rowscale, xs,
-                                                                  w->sigma, w->refdone);
-                    le = bte_lu_solve_t<float>(nact, N, (const float*)w->J, ld, jstride, w->piv, xs, 0, s);
-                    k_refine_update<<<nact, 128, 0, s>>>(nact, w->act, N, xs, w->sigma, w->dh, ldd, ccur,
+                    k_refine_residual<<<nact, 256, ref_smem, s>>>(gv, pp, ee, L.act, nact, w->h, w->F, w->aux,
+                                                                  w->scal, w->dh, ldd, beta_scale, L.rowscale, xs,
+                                                                  L.sigma, w->refdone);
+                    le = bte_lu_solve_t<float>(nact, N, (const float*)L.J, ld, jstride, L.piv, xs, 0, s);
+                    k_refine_update<<<nact, 128, 0, s>>>(nact, L.act, N, xs, L.sigma, w->dh, ldd, ccur,
                                                          w->refdone);
                 }));
                 CKR(le);
                 if (rf >= 1)
                     CKR(other([&] {
-                        k_refine_check<<<nblk(nact, 256), 256, 0, s>>>(nact, w->act, cprev, ccur, status, w->refdone,
+                        k_refine_check<<<nblk(nact, 256), 256, 0, s>>>(nact, L.act, cprev, ccur, status, w->refdone,
                                                                        rf + 1 == nrefine);
                     }));
             }
         } else {
-            double* xs = w->xs;
+            double* xs = L.xs;
             CKR(pf.run(PF_JACOBIAN, s, nact * jac_flops_pt(g, ee), jb, 1, [&] {
-                k_jacobian<double><<<gj, JAC_WARPS * 32, jac_smem<double>(g, ee), s>>>(gv, pp, ee, w->act, nact, w->h, w->F, w->aux, w->scal,
-                                                                   (double*)w->J, ld, jstride, beta_scale, w->rowscale,
+                k_jacobian<double><<<gj, JAC_WARPS * 32, jac_smem<double>(g, ee), s>>>(gv, pp, ee, L.act, nact, w->h, w->F, w->aux, w->scal,
+                                                                   (double*)L.J, ld, jstride, beta_scale, L.rowscale,
                                                                   jac_smem<double>(g, ee) > 0);
             }));
             CKR(pf.run(PF_LU, s, nact * lu_flops(N), lub, 1, [&] {
-                le = bte_lu_factor_t<double>(nact, N, N + 1, (double*)w->J, ld, jstride, w->piv, w->info, s, 0);
+                le = bte_lu_factor_t<double>(nact, N, N + 1, (double*)L.J, ld, jstride, L.piv, L.info, s, 0);
             }));
             CKR(le);
             CKR(pf.run(PF_LUSOLVE, s, nact * (double)N * N, lsb, 1, [&] {
-                le = bte_lu_solve_t<double>(nact, N, (const double*)w->J, ld, jstride, w->piv, xs, 1, s);
+                le = bte_lu_solve_t<double>(nact, N, (const double*)L.J, ld, jstride, L.piv, xs, 1, s);
             }));
             CKR(le);
-            CKR(other([&] { k_store_solution<double><<<nact, 128, 0, s>>>(nact, xs, N, w->act, w->dh, ldd); }));
+            CKR(other([&] { k_store_solution<double><<<nact, 128, 0, s>>>(nact, xs, N, L.act, w->dh, ldd); }));
         }
         // per-point Armijo backtracking
         CKR(other([&] { k_fill_int<<<nblk(P, 256), 256, 0, s>>>(w->searching, 0, P); }));
         CKR(other([&] { k_fill_int<<<nblk(P, 256), 256, 0, s>>>(w->accepted, 0, P); }));
-        CKR(other([&] { k_set_active<<<nblk(nact, 256), 256, 0, s>>>(nact, w->act, w->searching, w->alpha); }));
+        CKR(other([&] { k_set_active<<<nblk(nact, 256), 256, 0, s>>>(nact, L.act, w->searching, w->alpha); }));
         int nsearch = nact;
         for (int ls = 0; ls < 200; ++ls) {
             CKR(pf.run(PF_RESIDUAL, s, nsearch * res_flops_pt(g, ee), nsearch * res_bytes_pt(g, true), 1, [&] {
-                k_residual<<<nact, 256, res_smem, s>>>(gv, pp, ee, w->act, nact, w->h, w->dh, ldd, w->alpha,
+                k_residual<<<nact, 256, res_smem, s>>>(gv, pp, ee, L.act, nact, w->h, w->dh, ldd, w->alpha,
                                                        w->searching, w->ht, w->Ft, w->auxt, w->scalt, w->rt, w->srel);
             }));
             CKR(cudaMemsetAsync(w->cnt, 0, sizeof(int32_t), s));
             CKR(other([&] {
-                k_armijo<<<nblk(nact, 256), 256, 0, s>>>(nact, w->act, w->searching, w->alpha, w->r, w->rt,
+                k_armijo<<<nblk(nact, 256), 256, 0, s>>>(nact, L.act, w->searching, w->alpha, w->r, w->rt,
                                                         o->line_search_c, o->alpha_rho, amin, status, w->cnt,
                                                         w->accepted, w->r0, 1e-9, w->srel, 1e-8);
             }));
@@ -1150,22 +1196,22 @@ static int newton_loop(SolveCtx& c, int nact, int prec, int max_iter) {
             if (hc == 0) break;
         }
         CKR(other([&] {
-            k_accept<<<nact, 256, 0, s>>>(n, nact, w->act, w->accepted, w->h, w->ht, w->F, w->Ft, w->aux, w->auxt,
+            k_accept<<<nact, 256, 0, s>>>(n, nact, L.act, w->accepted, w->h, w->ht, w->F, w->Ft, w->aux, w->auxt,
                                          w->scal, w->scalt, w->r, w->rt, iters);
         }));
         CKR(cudaMemsetAsync(w->cnt, 0, sizeof(int32_t), s));
         CKR(other([&] {
-            k_converge<<<nblk(nact, 256), 256, 0, s>>>(nact, w->act, w->r, w->r0, o->atol, o->rtol,
-                                                      it + 1 == max_iter, status, w->act2, w->cnt, w->info, 0);
+            k_converge<<<nblk(nact, 256), 256, 0, s>>>(nact, L.act, w->r, w->r0, o->atol, o->rtol,
+                                                      w->nit, o->max_iter, status, L.act2, w->cnt, L.info, 0);
         }));
         int hn = 0;
         CKR(cudaMemcpyAsync(&hn, w->cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         CKR(cudaStreamSynchronize(s));
-        pf.drain();
-        std::swap(w->act, w->act2);
+        pf.drain(s);
+        std::swap(L.act, L.act2);
         nact = hn;
     }
-    return BTE_OK;
+    return nact;
 }
 
 int bte_solve_impl(BteGrid* g, int P, const double* n0, const double* ne, const double* ns_by_n0, const double* Tg,
@@ -1190,10 +1236,11 @@ int bte_solve_impl(BteGrid* g, int P, const double* n0, const double* ne, const 
     if (c.res_smem > 48 * 1024) CKR(cudaFuncSetAttribute(k_residual, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.res_smem));
     if (c.ref_smem > 48 * 1024) CKR(cudaFuncSetAttribute(k_refine_residual, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.ref_smem));
     Profiler& pf = g_prof;
+    Lane L{w->act, w->act2, w->J, w->piv, w->info, w->xs, w->rowscale, w->sigma};
     auto other = [&](auto&& fn) { return pf.run(PF_OTHER, s, 0, 0, 1, fn); };
     auto residual_all = [&](int nact) {
         return pf.run(PF_RESIDUAL, s, nact * res_flops_pt(g, c.ee), nact * res_bytes_pt(g, false), 1, [&] {
-            k_residual<<<nact, 256, c.res_smem, s>>>(c.gv, c.pp, c.ee, w->act, nact, w->h, nullptr, 0, nullptr,
+            k_residual<<<nact, 256, c.res_smem, s>>>(c.gv, c.pp, c.ee, L.act, nact, w->h, nullptr, 0, nullptr,
                                                      nullptr, nullptr, w->F, w->aux, w->scal, w->r, nullptr);
         });
     };
@@ -1202,49 +1249,55 @@ int bte_solve_impl(BteGrid* g, int P, const double* n0, const double* ne, const 
     CKR(cudaMemcpyAsync(w->h0, w->h, (size_t)P * n * sizeof(double), cudaMemcpyDeviceToDevice, s));
     CKR(other([&] { k_fill_int<<<nblk(P, 256), 256, 0, s>>>(status, -1, P); }));
     CKR(other([&] { k_fill_int<<<nblk(P, 256), 256, 0, s>>>(iters, 0, P); }));
-    CKR(other([&] { k_iota<<<nblk(P, 256), 256, 0, s>>>(w->act, P); }));
+    CKR(other([&] { k_fill_int<<<nblk(P, 256), 256, 0, s>>>(w->nit, 0, P); }));
+    CKR(other([&] { k_iota<<<nblk(P, 256), 256, 0, s>>>(L.act, P); }));
     CKR(residual_all(P));
     CKR(cudaMemcpyAsync(w->r0, w->r, P * sizeof(double), cudaMemcpyDeviceToDevice, s));
     const size_t rm_smem = (size_t)2 * n * sizeof(double);
     if (rm_smem > 48 * 1024) CKR(cudaFuncSetAttribute(k_ref_merit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rm_smem));
-    CKR(other([&] { k_ref_merit<<<P, 256, rm_smem, s>>>(c.gv, P, w->F, w->ref_r0); }));
-    rc = newton_loop(c, P, prec, o->max_iter);
-    if (rc) return rc;
+    CKR(other([&] { k_ref_merit<<<P, 256, rm_smem, s>>>(c.gv, P, nullptr, w->F, w->ref_r0); }));
+    for (int it = 0, nact = P; it < o->max_iter && nact > 0; ++it) {
+        nact = newton_iteration(c, L, nact, prec);
+        if (nact < 0) return nact;
+    }
     if (prec == BTE_PREC_MIXED) {
-        // points the mixed form did not converge restart from the initial state in FP64
+        // points the mixed form did not converge go to the FP64 form (k_restore: from where)
         CKR(cudaMemsetAsync(w->cnt, 0, sizeof(int32_t), s));
-        CKR(other([&] { k_collect_failed<<<nblk(P, 256), 256, 0, s>>>(P, status, w->act2, w->cnt, w->reason); }));
+        CKR(other([&] { k_collect_failed<<<nblk(P, 256), 256, 0, s>>>(P, status, L.act2, w->cnt, w->reason); }));
         int nf = 0;
         CKR(cudaMemcpyAsync(&nf, w->cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         CKR(cudaStreamSynchronize(s));
-        pf.fallback += nf;
         // the J buffer holds FP32 matrices for P points: FP64 chunks of at most P / 2
         const int chunk = std::max(1, P / 2);
         std::vector<int32_t> failed(nf);
-        if (nf) CKR(cudaMemcpyAsync(failed.data(), w->act2, nf * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        if (nf) CKR(cudaMemcpyAsync(failed.data(), L.act2, nf * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         CKR(cudaStreamSynchronize(s));
+        long long why[8] = {0};
         if (nf && pf.on) {  // why they failed (statuses were reset to running by k_collect_failed)
             std::vector<int32_t> st(P);
             CKR(cudaMemcpy(st.data(), w->reason, P * sizeof(int32_t), cudaMemcpyDeviceToHost));
             for (int i = 0; i < nf; ++i) {
                 int r = st[failed[i]];
-                if (r >= 0 && r < 8) pf.fb_reason[r]++;
+                if (r >= 0 && r < 8) why[r]++;
             }
         }
+        pf.count_fallback(nf, why);
         for (int c0 = 0; c0 < nf; c0 += chunk) {
             int m = std::min(chunk, nf - c0);
-            CKR(cudaMemcpyAsync(w->act, failed.data() + c0, m * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-            CKR(other([&] { k_restore<<<m, 256, 0, s>>>(n, m, w->act, w->h0, w->h); }));
+            CKR(cudaMemcpyAsync(L.act, failed.data() + c0, m * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+            CKR(other([&] { k_restore<<<m, 256, 0, s>>>(n, m, L.act, w->reason, w->h0, w->h, w->nit); }));
             CKR(residual_all(m));
-            rc = newton_loop(c, m, BTE_PREC_FP64, o->max_iter);
-            if (rc) return rc;
+            for (int it = 0, nact = m; it < o->max_iter && nact > 0; ++it) {
+                nact = newton_iteration(c, L, nact, BTE_PREC_FP64);
+                if (nact < 0) return nact;
+            }
         }
     }
     const double c_gamma = std::sqrt(2.0 * (BTE_QE / BTE_ME));
     const double mm_fac = std::sqrt(1.0 / (4.0 * M_PI)) * 4.0 * M_PI;
     const double sc3 = 2.0 * std::pow(g->vth / c_gamma, 3);
     CKR(other([&] { k_normalized_distribution<<<P, 256, 0, s>>>(n, g->d_mass, mm_fac, sc3, w->h, f, P); }));
-    CKR(other([&] { k_ref_merit<<<P, 256, rm_smem, s>>>(c.gv, P, w->F, w->ref_r); }));
+    CKR(other([&] { k_ref_merit<<<P, 256, rm_smem, s>>>(c.gv, P, nullptr, w->F, w->ref_r); }));
     return BTE_OK;
 }
 
