@@ -22,7 +22,9 @@ STATUS = {0: "converged", 1: "roundoff", 2: "max_iter", 3: "line_search", 4: "no
 
 EXPORTED = ["bte_grid_create", "bte_grid_destroy", "bte_grid_info", "bte_grid_export", "bte_initialize",
             "bte_solve_steady", "bte_qoi", "bte_lu_factor", "bte_lu_solve", "bte_last_error",
-            "bte_radial_components", "bte_stats_reset", "bte_stats", "bte_solve_info", "bte_lu_factor_ex"]
+            "bte_radial_components", "bte_stats_reset", "bte_stats", "bte_solve_info", "bte_lu_factor_ex",
+            "bte_engine_create", "bte_engine_destroy", "bte_engine_admit", "bte_engine_step", "bte_engine_collect",
+            "bte_engine_info"]
 
 STAT_FAMILIES = ["residual", "jacobian", "lu_factor", "lu_solve", "refine", "other"]
 
@@ -84,6 +86,12 @@ def load() -> C.CDLL:
     for name in EXPORTED:
         if not hasattr(lib, name):
             raise RuntimeError("libbte_gb300.so does not export %s" % name)
+    lib.bte_engine_create.argtypes = [vp, C.c_int, C.c_int, C.POINTER(SolveOpts), C.POINTER(C.c_void_p)]
+    lib.bte_engine_destroy.argtypes = [vp]
+    lib.bte_engine_admit.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp, vp, C.c_int, i32p, vp]
+    lib.bte_engine_step.argtypes = [vp, C.POINTER(C.c_int), i32p, vp]
+    lib.bte_engine_collect.argtypes = [vp, C.c_int, i32p, vp, vp, vp, vp]
+    lib.bte_engine_info.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_size_t)]
     if hasattr(lib, "bte_initialize_noalloc"):
         lib.bte_initialize_noalloc.argtypes = [vp, C.c_int, vp, vp]
     if hasattr(lib, "bte_radial_components"):
@@ -117,3 +125,8 @@ def stats() -> dict:
     out["fp64_fallback_reasons"] = {k: int(buf[2 + 4 * len(STAT_FAMILIES) + i]) for i, k in
                                     enumerate(["max_iter", "line_search", "non_finite", "singular", "refinement"])}
     return out
+
+
+def ptr(t) -> C.c_void_p:
+    """Device pointer of a CUDA tensor (null for None)."""
+    return C.c_void_p(0 if t is None else t.data_ptr())

@@ -89,6 +89,21 @@ int bte_assemble(BteGrid* g, cudaStream_t s);
 struct BteWork;
 BteWork* bte_work_get(BteGrid* g);
 void bte_work_release(BteWork* w);
+struct BteEngine;
+int bte_engine_create_impl(BteGrid* g, int cap, int fcap, const bte_solve_opts* o, BteEngine** out);
+void bte_engine_destroy_impl(BteEngine* e);
+int bte_engine_admit_impl(BteEngine* e, int m, const double* n0, const double* ne, const double* ns_by_n0,
+                          const double* Tg, const double* E, const double* f0, int want_ee, int32_t* slots_out,
+                          cudaStream_t s);
+int bte_engine_step_impl(BteEngine* e, int* n_done, int32_t* done_out, cudaStream_t s);
+int bte_engine_collect_impl(BteEngine* e, int m, const int32_t* slots, double* f, int32_t* status, int32_t* iters,
+                            cudaStream_t s);
+int bte_engine_free_slots(const BteEngine* e);
+int bte_engine_active(const BteEngine* e);
+size_t bte_engine_bytes(const BteEngine* e);
+int bte_engine_fp64_capacity(const BteEngine* e);
+int bte_engine_capacity(const BteEngine* e);
+BteGrid* bte_engine_grid(const BteEngine* e);
 int bte_solve_impl(BteGrid* g, int P, const double* n0, const double* ne, const double* ns_by_n0,
                    const double* Tg, const double* E, double* f, int32_t* status, int32_t* iters,
                    const bte_solve_opts* opts, cudaStream_t s);

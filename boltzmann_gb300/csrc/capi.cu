@@ -454,6 +454,71 @@ int bte_initialize_noalloc(const bte_grid* g, int P, double* f, void* stream) {
     return BTE_OK;
 }
 
+int bte_engine_create(bte_grid* g, int capacity, int fp64_capacity, const bte_solve_opts* opts, bte_engine** out) {
+    if (!g || !opts || !out) return fail(BTE_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (capacity < 1 || capacity > (1 << 20)) return fail(BTE_ERR_ARG, "capacity out of range [1, 2^20]");
+    if (opts->precision != BTE_PREC_FP64 && opts->precision != BTE_PREC_MIXED) return fail(BTE_ERR_ARG, "bad precision");
+    if (opts->max_iter < 1 || !(opts->alpha_rho > 0 && opts->alpha_rho < 1)) return fail(BTE_ERR_ARG, "bad solver options");
+    if (opts->precision == BTE_PREC_MIXED && fp64_capacity < 1) return fail(BTE_ERR_ARG, "the mixed form needs fp64_capacity >= 1");
+    CUDA_OR_FAIL(cudaSetDevice(g->device), "cudaSetDevice");
+    int rc = bte_engine_create_impl(g, capacity, fp64_capacity, opts, out);
+    if (rc != BTE_OK) return fail(rc, rc == BTE_ERR_ALLOC ? "engine: device allocation failed" : "engine: create failed");
+    return BTE_OK;
+}
+
+int bte_engine_destroy(bte_engine* e) {
+    if (!e) return BTE_OK;
+    cudaSetDevice(bte_engine_grid(e)->device);
+    cudaDeviceSynchronize();
+    bte_engine_destroy_impl(e);
+    return BTE_OK;
+}
+
+int bte_engine_admit(bte_engine* e, int P, const double* n0, const double* ne, const double* ns_by_n0,
+                     const double* Tg, const double* E, const double* f0, int ee, int32_t* slots, void* stream) {
+    if (!e || P < 0) return fail(BTE_ERR_ARG, "bad argument");
+    if (P == 0) return BTE_OK;
+    if (!n0 || !ne || !ns_by_n0 || !Tg || !E || !f0 || !slots) return fail(BTE_ERR_ARG, "null buffer");
+    BteGrid* g = bte_engine_grid(e);
+    if (ee && !g->ee) return fail(BTE_ERR_STATE, "e-e requested but the grid was built without Coulomb operators");
+    if (P > bte_engine_free_slots(e)) return fail(BTE_ERR_STATE, "not enough free slots");
+    cudaSetDevice(g->device);
+    int rc = bte_engine_admit_impl(e, P, n0, ne, ns_by_n0, Tg, E, f0, ee, slots, (cudaStream_t)stream);
+    if (rc != BTE_OK) return fail(rc, std::string("engine admit failed: ") + cudaGetErrorString(cudaGetLastError()));
+    return BTE_OK;
+}
+
+int bte_engine_step(bte_engine* e, int* n_done, int32_t* done_slots, void* stream) {
+    if (!e || !n_done || !done_slots) return fail(BTE_ERR_ARG, "null argument");
+    cudaSetDevice(bte_engine_grid(e)->device);
+    int rc = bte_engine_step_impl(e, n_done, done_slots, (cudaStream_t)stream);
+    if (rc != BTE_OK) return fail(rc, std::string("engine step failed: ") + cudaGetErrorString(cudaGetLastError()));
+    return BTE_OK;
+}
+
+int bte_engine_collect(bte_engine* e, int P, const int32_t* slots, double* f, int32_t* status, int32_t* iters,
+                       void* stream) {
+    if (!e || P < 0) return fail(BTE_ERR_ARG, "bad argument");
+    if (P == 0) return BTE_OK;
+    if (!slots || !f) return fail(BTE_ERR_ARG, "null buffer");
+    cudaSetDevice(bte_engine_grid(e)->device);
+    int rc = bte_engine_collect_impl(e, P, slots, f, status, iters, (cudaStream_t)stream);
+    if (rc == BTE_ERR_ARG) return fail(rc, "slot index out of range");
+    if (rc != BTE_OK) return fail(rc, std::string("engine collect failed: ") + cudaGetErrorString(cudaGetLastError()));
+    return BTE_OK;
+}
+
+int bte_engine_info(const bte_engine* e, int* ints4, size_t* bytes) {
+    if (!e || !ints4) return fail(BTE_ERR_ARG, "null argument");
+    ints4[0] = bte_engine_capacity(e);
+    ints4[1] = bte_engine_free_slots(e);
+    ints4[2] = bte_engine_active(e);
+    ints4[3] = bte_engine_fp64_capacity(e);
+    if (bytes) *bytes = bte_engine_bytes(e);
+    return BTE_OK;
+}
+
 int bte_solve_steady(bte_grid* g, int P, const double* n0, const double* ne, const double* ns_by_n0, const double* Tg,
                      const double* E, double* f, int32_t* status, int32_t* iters, const bte_solve_opts* opts,
                      void* stream) {

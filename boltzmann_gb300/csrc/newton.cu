@@ -1309,3 +1309,355 @@ int bte_solve_info_impl(BteGrid* g, int P, double* r_final, double* r_initial, c
     if (cudaMemcpyAsync(r_initial, w->ref_r0, P * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess) return BTE_ERR_CUDA;
     return BTE_OK;
 }
+
+// ---------------------------------------------------------------------------------
+// Serving engine: a fixed set of point slots on one grid, resident on the device. Points
+// enter free slots between Newton iterations and leave as soon as their own solve ends, so
+// requests that arrive while others run join the same launches (continuous batching at the
+// granularity of one Newton iteration). Each slot runs the reference driver's two solves
+// (bte_0d3v_batched_driver.py:192-204): phase 0 without e-e collisions from the admitted
+// state, then, if the request asks for e-e, phase 1 with them from phase 0's normalized
+// result. Per point the arithmetic is that of bte_solve_steady: in the mixed form a point
+// whose FP32 solve fails moves to an FP64 lane (its own Jacobian buffers, fcap slots) for
+// the rest of that phase, from the same state bte_solve_steady would use.
+// ---------------------------------------------------------------------------------
+struct BteEngine {
+    BteGrid* g = nullptr;
+    int cap = 0, fcap = 0, prec = 0;
+    bte_solve_opts opts{};
+    BteWork w;          // per-slot state; its position-indexed buffers serve the main lane
+    Lane main{}, f64{}; // f64: mixed form only
+    void* J64 = nullptr;
+    int32_t *piv64 = nullptr, *info64 = nullptr, *act64a = nullptr, *act64b = nullptr;
+    double *xs64 = nullptr, *rs64 = nullptr, *sg64 = nullptr;
+    double *n0 = nullptr, *ne = nullptr, *Tg = nullptr, *E = nullptr, *ns = nullptr;  // per slot, ns species-major
+    int8_t *phase = nullptr, *want_ee = nullptr;   // per slot
+    int32_t *status = nullptr, *iters = nullptr;   // per slot
+    int32_t *l_done = nullptr, *l_fb = nullptr, *l_sw = nullptr, *l_in = nullptr, *cnt = nullptr;
+    int nmain = 0, nf64 = 0;
+    std::vector<int> free_slots;
+    std::deque<int> f64_wait;   // slots waiting for room in the FP64 lane
+    std::vector<void*> allocs;
+    size_t bytes = 0;           // device memory held
+};
+
+__global__ void k_engine_admit(int m, const int* __restrict__ slots, int n, const double* __restrict__ u,
+                               const double* __restrict__ f0, double* h, double* h0, const double* __restrict__ n0_in,
+                               const double* __restrict__ ne_in, const double* __restrict__ Tg_in,
+                               const double* __restrict__ E_in, const double* __restrict__ ns_in, int nspecies,
+                               double* n0, double* ne, double* Tg, double* E, double* ns, int cap, int8_t* phase,
+                               int8_t* want_ee, int want, int* status, int* iters, int* nit) {
+    __shared__ double red[32];
+    const int i = blockIdx.x;
+    if (i >= m) return;
+    const int pt = slots[i];
+    // the state enters as bte_solve_steady takes it: h = f0 / (u . f0)
+    double sacc = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) sacc += u[k] * f0[(size_t)i * n + k];
+    sacc = block_sum(sacc, red);
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const double v = f0[(size_t)i * n + k] / sacc;
+        h[(size_t)pt * n + k] = v;
+        h0[(size_t)pt * n + k] = v;
+    }
+    if (threadIdx.x == 0) {
+        n0[pt] = n0_in[i]; ne[pt] = ne_in[i]; Tg[pt] = Tg_in[i]; E[pt] = E_in[i];
+        for (int sp = 0; sp < nspecies; ++sp) ns[(size_t)sp * cap + pt] = ns_in[(size_t)sp * m + i];
+        phase[pt] = 0; want_ee[pt] = (int8_t)want; status[pt] = -1; iters[pt] = 0; nit[pt] = 0;
+    }
+}
+
+__global__ void k_copy_list(int m, const int* __restrict__ list, const double* __restrict__ src, double* dst) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m) dst[list[i]] = src[list[i]];
+}
+
+// sort the points that left a lane in its last iteration: finished (done), handed to the FP64
+// lane (fb, mixed main lane only), or switching to the e-e phase (sw)
+__global__ void k_engine_sort(int nold, const int* __restrict__ old, const int* __restrict__ status,
+                              const int8_t* __restrict__ phase, const int8_t* __restrict__ want_ee, int can_fb,
+                              int* done, int* fb, int* sw, int* cnt) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nold) return;
+    const int pt = old[i];
+    const int st = status[pt];
+    if (st < 0) return;  // still running
+    if (can_fb && st >= BTE_ST_MAXITER) { fb[atomicAdd(&cnt[1], 1)] = pt; return; }
+    if (st <= BTE_ST_ROUNDOFF && phase[pt] == 0 && want_ee[pt]) { sw[atomicAdd(&cnt[2], 1)] = pt; return; }
+    done[atomicAdd(&cnt[0], 1)] = pt;
+}
+
+// a point entering the FP64 lane: as k_collect_failed + k_restore do in bte_solve_steady
+__global__ void k_engine_to_fp64(int m, const int* __restrict__ list, int n, int* status, int* reason, int* nit,
+                                 const double* __restrict__ h0, double* h) {
+    const int i = blockIdx.x;
+    if (i >= m) return;
+    const int pt = list[i];
+    const int st = status[pt];
+    __syncthreads();
+    if (threadIdx.x == 0) { reason[pt] = st; status[pt] = -1; nit[pt] = 0; }
+    if (st == BTE_ST_NEED_FP64) return;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) h[(size_t)pt * n + k] = h0[(size_t)pt * n + k];
+}
+
+// phase 0 -> phase 1: the state bte_solve_steady's second call starts from, i.e. the
+// normalized distribution of the first call, mass-normalized again
+__global__ void k_engine_phase1(int m, const int* __restrict__ list, int n, const double* __restrict__ mass,
+                                double mm_fac, double scale3, const double* __restrict__ u, double* h, double* h0,
+                                int8_t* phase, int* status, int* nit) {
+    __shared__ double red[32];
+    const int i = blockIdx.x;
+    if (i >= m) return;
+    const int pt = list[i];
+    double* hp = h + (size_t)pt * n;
+    double sacc = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) sacc += (mass[k] / mm_fac) * hp[k];
+    sacc = block_sum(sacc, red) * scale3;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) hp[k] = hp[k] / sacc;
+    double s2 = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) s2 += u[k] * hp[k];
+    s2 = block_sum(s2, red);
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const double v = hp[k] / s2;
+        hp[k] = v;
+        h0[(size_t)pt * n + k] = v;
+    }
+    if (threadIdx.x == 0) { phase[pt] = 1; status[pt] = -1; nit[pt] = 0; }
+}
+
+__global__ void k_engine_collect(int m, const int* __restrict__ list, int n, const double* __restrict__ mass,
+                                 double mm_fac, double scale3, const double* __restrict__ h,
+                                 const int* __restrict__ status, const int* __restrict__ iters, double* f,
+                                 int32_t* st_out, int32_t* it_out) {
+    __shared__ double red[32];
+    const int i = blockIdx.x;
+    if (i >= m) return;
+    const int pt = list[i];
+    const double* hp = h + (size_t)pt * n;
+    double sacc = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) sacc += (mass[k] / mm_fac) * hp[k];
+    sacc = block_sum(sacc, red) * scale3;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) f[(size_t)i * n + k] = hp[k] / sacc;
+    if (threadIdx.x == 0) {
+        if (st_out) st_out[i] = status[pt];
+        if (it_out) it_out[i] = iters[pt];
+    }
+}
+
+static void engine_free(BteEngine* e) {
+    for (void* p : e->allocs) cudaFree(p);
+    e->allocs.clear();
+    free_work(&e->w);
+}
+
+static SolveCtx engine_ctx(BteEngine* e, cudaStream_t s) {
+    BteGrid* g = e->g;
+    SolveCtx c{};
+    c.g = g; c.w = &e->w; c.gv = view_of(g);
+    c.pp = PointParams{e->n0, e->ne, e->Tg, e->E, e->ns, e->cap, e->phase};
+    c.P = e->cap; c.n = g->n; c.N = g->n + 1; c.ld = (c.N + 1 + 3) & ~3; c.ldd = c.N + 1;
+    c.ee = g->ee ? 1 : 0;  // per point: the slot's phase
+    c.jstride = (long long)c.N * c.ld;
+    c.beta_scale = g->q0max / (g->umax > 0 ? g->umax : 1.0);
+    c.res_smem = (size_t)5 * c.n * sizeof(double);
+    c.ref_smem = (size_t)(5 * c.n + 1) * sizeof(double);
+    c.o = &e->opts; c.status = e->status; c.iters = e->iters; c.s = s;
+    return c;
+}
+
+int bte_engine_create_impl(BteGrid* g, int cap, int fcap, const bte_solve_opts* o, BteEngine** out) {
+    BteEngine* e = new BteEngine();
+    e->g = g; e->cap = cap; e->prec = o->precision; e->opts = *o;
+    e->fcap = (o->precision == BTE_PREC_MIXED) ? std::max(1, std::min(fcap, cap)) : 0;
+    const int n = g->n, N = n + 1, ld = (N + 1 + 3) & ~3;
+    int rc = ensure_work(&e->w, g, cap, e->prec);
+    if (rc) { delete e; return rc; }
+    e->bytes = e->w.jbytes + (size_t)cap * (size_t)(n * 12 + (N + 1) * 3 + 24) * sizeof(double);  // J + per-slot vectors
+    bool ok = true;
+    auto A = [&](void** p, size_t bytes) {
+        if (!ok) return;
+        if (cudaMalloc(p, std::max<size_t>(bytes, 8)) != cudaSuccess) { ok = false; *p = nullptr; return; }
+        e->allocs.push_back(*p);
+        e->bytes += bytes;
+    };
+    const size_t dc = (size_t)cap * sizeof(double), ic = (size_t)cap * sizeof(int32_t);
+    A((void**)&e->n0, dc); A((void**)&e->ne, dc); A((void**)&e->Tg, dc); A((void**)&e->E, dc);
+    A((void**)&e->ns, dc * g->nspecies);
+    A((void**)&e->phase, cap); A((void**)&e->want_ee, cap);
+    A((void**)&e->status, ic); A((void**)&e->iters, ic);
+    A((void**)&e->l_done, ic); A((void**)&e->l_fb, ic); A((void**)&e->l_sw, ic); A((void**)&e->l_in, ic);
+    A((void**)&e->cnt, 4 * sizeof(int32_t));
+    if (e->fcap > 0) {
+        const int f = e->fcap;
+        A(&e->J64, (size_t)f * N * ld * sizeof(double));
+        A((void**)&e->piv64, (size_t)f * N * sizeof(int32_t)); A((void**)&e->info64, (size_t)f * sizeof(int32_t));
+        A((void**)&e->act64a, (size_t)f * sizeof(int32_t)); A((void**)&e->act64b, (size_t)f * sizeof(int32_t));
+        A((void**)&e->xs64, (size_t)f * (N + 1) * sizeof(double)); A((void**)&e->rs64, (size_t)f * (N + 1) * sizeof(double));
+        A((void**)&e->sg64, (size_t)f * sizeof(double));
+    }
+    if (!ok) { engine_free(e); delete e; return BTE_ERR_ALLOC; }
+    e->main = Lane{e->w.act, e->w.act2, e->w.J, e->w.piv, e->w.info, e->w.xs, e->w.rowscale, e->w.sigma};
+    e->f64 = Lane{e->act64a, e->act64b, e->J64, e->piv64, e->info64, e->xs64, e->rs64, e->sg64};
+    e->free_slots.resize(cap);
+    for (int i = 0; i < cap; ++i) e->free_slots[i] = cap - 1 - i;  // pop_back hands out 0, 1, 2, ...
+    SolveCtx c = engine_ctx(e, 0);
+    if (c.res_smem > 48 * 1024) cudaFuncSetAttribute(k_residual, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.res_smem);
+    if (c.ref_smem > 48 * 1024) cudaFuncSetAttribute(k_refine_residual, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.ref_smem);
+    const size_t rm_smem = (size_t)2 * n * sizeof(double);
+    if (rm_smem > 48 * 1024) cudaFuncSetAttribute(k_ref_merit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rm_smem);
+    *out = e;
+    return BTE_OK;
+}
+
+void bte_engine_destroy_impl(BteEngine* e) {
+    if (!e) return;
+    engine_free(e);
+    delete e;
+}
+
+int bte_engine_free_slots(const BteEngine* e) { return (int)e->free_slots.size(); }
+int bte_engine_active(const BteEngine* e) { return e->nmain + e->nf64 + (int)e->f64_wait.size(); }
+int bte_engine_fp64_capacity(const BteEngine* e) { return e->fcap; }
+int bte_engine_capacity(const BteEngine* e) { return e->cap; }
+BteGrid* bte_engine_grid(const BteEngine* e) { return e->g; }
+size_t bte_engine_bytes(const BteEngine* e) { return e->bytes; }
+
+// residual, r0 and the reference merit at the start of a phase, for the m slots in `list`
+static int engine_start_phase(BteEngine* e, SolveCtx& c, const int* list, int m, cudaStream_t s) {
+    if (m <= 0) return BTE_OK;
+    BteGrid* g = e->g;
+    BteWork* w = &e->w;
+    const int n = g->n;
+    Profiler& pf = g_prof;
+    CKR(pf.run(PF_RESIDUAL, s, m * res_flops_pt(g, c.ee), m * res_bytes_pt(g, false), 1, [&] {
+        k_residual<<<m, 256, c.res_smem, s>>>(c.gv, c.pp, c.ee, list, m, w->h, nullptr, 0, nullptr, nullptr, nullptr,
+                                              w->F, w->aux, w->scal, w->r, nullptr);
+    }));
+    CKR(pf.run(PF_OTHER, s, 0, 0, 2, [&] {
+        k_copy_list<<<nblk(m, 256), 256, 0, s>>>(m, list, w->r, w->r0);
+        k_ref_merit<<<m, 256, (size_t)2 * n * sizeof(double), s>>>(c.gv, m, list, w->F, w->ref_r0);
+    }));
+    return BTE_OK;
+}
+
+int bte_engine_admit_impl(BteEngine* e, int m, const double* n0, const double* ne, const double* ns_by_n0,
+                          const double* Tg, const double* E, const double* f0, int want_ee, int32_t* slots_out,
+                          cudaStream_t s) {
+    if (m <= 0) return BTE_OK;
+    if (m > (int)e->free_slots.size()) return BTE_ERR_STATE;
+    BteGrid* g = e->g;
+    const int n = g->n;
+    std::vector<int32_t> sl(m);
+    for (int i = 0; i < m; ++i) { sl[i] = e->free_slots.back(); e->free_slots.pop_back(); }
+    SolveCtx c = engine_ctx(e, s);
+    Profiler& pf = g_prof;
+    CKR(cudaMemcpyAsync(e->l_in, sl.data(), m * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    CKR(pf.run(PF_OTHER, s, 0, 0, 1, [&] {
+        k_engine_admit<<<m, 256, 0, s>>>(m, e->l_in, n, g->d_u, f0, e->w.h, e->w.h0, n0, ne, Tg, E, ns_by_n0,
+                                         g->nspecies, e->n0, e->ne, e->Tg, e->E, e->ns, e->cap, e->phase, e->want_ee,
+                                         want_ee ? 1 : 0, e->status, e->iters, e->w.nit);
+    }));
+    int rc = engine_start_phase(e, c, e->l_in, m, s);
+    if (rc) return rc;
+    CKR(cudaMemcpyAsync(e->main.act + e->nmain, e->l_in, m * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+    e->nmain += m;
+    CKR(cudaStreamSynchronize(s));  // the host list `sl` and the slot order are settled
+    for (int i = 0; i < m; ++i) slots_out[i] = sl[i];
+    return BTE_OK;
+}
+
+int bte_engine_step_impl(BteEngine* e, int* n_done, int32_t* done_out, cudaStream_t s) {
+    *n_done = 0;
+    BteGrid* g = e->g;
+    BteWork* w = &e->w;
+    const int n = g->n;
+    SolveCtx c = engine_ctx(e, s);
+    Profiler& pf = g_prof;
+    const bool mixed = (e->prec == BTE_PREC_MIXED);
+    // points waiting for the FP64 lane move in while it has room
+    const int room = e->fcap - e->nf64;
+    const int k = std::min<int>(room, (int)e->f64_wait.size());
+    if (mixed && k > 0) {
+        std::vector<int32_t> mv(k);
+        for (int i = 0; i < k; ++i) { mv[i] = e->f64_wait.front(); e->f64_wait.pop_front(); }
+        CKR(cudaMemcpyAsync(e->l_in, mv.data(), k * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+        CKR(pf.run(PF_OTHER, s, 0, 0, 1, [&] {
+            k_engine_to_fp64<<<k, 256, 0, s>>>(k, e->l_in, n, e->status, w->reason, w->nit, w->h0, w->h);
+        }));
+        CKR(pf.run(PF_RESIDUAL, s, k * res_flops_pt(g, c.ee), k * res_bytes_pt(g, false), 1, [&] {
+            k_residual<<<k, 256, c.res_smem, s>>>(c.gv, c.pp, c.ee, e->l_in, k, w->h, nullptr, 0, nullptr, nullptr,
+                                                  nullptr, w->F, w->aux, w->scal, w->r, nullptr);
+        }));
+        CKR(cudaMemcpyAsync(e->f64.act + e->nf64, e->l_in, k * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+        CKR(cudaStreamSynchronize(s));  // `mv` is read by the copy above
+        e->nf64 += k;
+    }
+    CKR(cudaMemsetAsync(e->cnt, 0, 4 * sizeof(int32_t), s));
+    if (e->nmain > 0) {
+        const int nold = e->nmain;
+        const int r = newton_iteration(c, e->main, nold, e->prec);
+        if (r < 0) return r;
+        e->nmain = r;
+        CKR(pf.run(PF_OTHER, s, 0, 0, 1, [&] {
+            k_engine_sort<<<nblk(nold, 256), 256, 0, s>>>(nold, e->main.act2, e->status, e->phase, e->want_ee,
+                                                          mixed ? 1 : 0, e->l_done, e->l_fb, e->l_sw, e->cnt);
+        }));
+    }
+    if (e->nf64 > 0) {
+        const int nold = e->nf64;
+        const int r = newton_iteration(c, e->f64, nold, BTE_PREC_FP64);
+        if (r < 0) return r;
+        e->nf64 = r;
+        CKR(pf.run(PF_OTHER, s, 0, 0, 1, [&] {
+            k_engine_sort<<<nblk(nold, 256), 256, 0, s>>>(nold, e->f64.act2, e->status, e->phase, e->want_ee, 0,
+                                                          e->l_done, e->l_fb, e->l_sw, e->cnt);
+        }));
+    }
+    int hc[4] = {0, 0, 0, 0};
+    CKR(cudaMemcpyAsync(hc, e->cnt, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    CKR(cudaStreamSynchronize(s));
+    const int nd = hc[0], nfb = hc[1], nsw = hc[2];
+    if (nfb > 0) {
+        std::vector<int32_t> fb(nfb);
+        CKR(cudaMemcpyAsync(fb.data(), e->l_fb, nfb * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        CKR(cudaStreamSynchronize(s));
+        for (int v : fb) e->f64_wait.push_back(v);
+        pf.count_fallback(nfb, nullptr);
+    }
+    if (nsw > 0) {
+        const double c_gamma = std::sqrt(2.0 * (BTE_QE / BTE_ME));
+        const double mm_fac = std::sqrt(1.0 / (4.0 * M_PI)) * 4.0 * M_PI;
+        const double sc3 = 2.0 * std::pow(g->vth / c_gamma, 3);
+        CKR(pf.run(PF_OTHER, s, 0, 0, 1, [&] {
+            k_engine_phase1<<<nsw, 256, 0, s>>>(nsw, e->l_sw, n, g->d_mass, mm_fac, sc3, g->d_u, w->h, w->h0,
+                                                e->phase, e->status, w->nit);
+        }));
+        int rc = engine_start_phase(e, c, e->l_sw, nsw, s);
+        if (rc) return rc;
+        CKR(cudaMemcpyAsync(e->main.act + e->nmain, e->l_sw, nsw * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+        e->nmain += nsw;
+    }
+    if (nd > 0) CKR(cudaMemcpyAsync(done_out, e->l_done, nd * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    CKR(cudaStreamSynchronize(s));
+    *n_done = nd;
+    return BTE_OK;
+}
+
+int bte_engine_collect_impl(BteEngine* e, int m, const int32_t* slots, double* f, int32_t* status, int32_t* iters,
+                            cudaStream_t s) {
+    if (m <= 0) return BTE_OK;
+    BteGrid* g = e->g;
+    for (int i = 0; i < m; ++i)
+        if (slots[i] < 0 || slots[i] >= e->cap) return BTE_ERR_ARG;
+    CKR(cudaMemcpyAsync(e->l_in, slots, m * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    const double c_gamma = std::sqrt(2.0 * (BTE_QE / BTE_ME));
+    const double mm_fac = std::sqrt(1.0 / (4.0 * M_PI)) * 4.0 * M_PI;
+    const double sc3 = 2.0 * std::pow(g->vth / c_gamma, 3);
+    CKR(g_prof.run(PF_OTHER, s, 0, 0, 1, [&] {
+        k_engine_collect<<<m, 256, 0, s>>>(m, e->l_in, g->n, g->d_mass, mm_fac, sc3, e->w.h, e->status, e->iters, f,
+                                           status, iters);
+    }));
+    CKR(cudaStreamSynchronize(s));
+    for (int i = 0; i < m; ++i) e->free_slots.push_back(slots[i]);
+    return BTE_OK;
+}

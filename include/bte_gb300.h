@@ -188,6 +188,38 @@ int bte_stats_reset(int enable_timing);
  * Replaces bte_0d3v_batched.profile_stats (bte_0d3v_batched.py:1248-1315). */
 int bte_stats(double* out, int count);
 
+/* ---- Serving engine: continuous batching of steady-state solves on one grid ----
+ * The reference has no serving loop; this is the device side of the request loop in
+ * boltzmann_gb300/serving.py. An engine owns `capacity` point slots on one grid (state,
+ * Jacobian buffers and parameters resident on the device). Points are admitted into free
+ * slots between Newton iterations and retire when their own solve ends, so requests that
+ * arrive while others run share the same kernel launches. Each admitted point runs the
+ * reference driver's solve sequence (bte_0d3v_batched_driver.py:192-204): a steady solve
+ * without e-e collisions from its initial state, then, if `ee` was set at admission, one
+ * with them from that result; per point the arithmetic is that of two bte_solve_steady
+ * calls. In the mixed form a point whose FP32 solve fails continues in an FP64 lane of
+ * `fp64_capacity` slots. One engine is driven by one host thread on one stream at a time;
+ * engines of different grids may run concurrently on different streams. */
+typedef struct BteEngine bte_engine;
+int bte_engine_create(bte_grid* g, int capacity, int fp64_capacity, const bte_solve_opts* opts, bte_engine** out);
+int bte_engine_destroy(bte_engine* e);
+/* Admit P points (device arrays: n0, ne, Tg, E [P]; ns_by_n0 [n_species x P]; f0 [P x n],
+ * any positive multiple of the initial state). Fails with BTE_ERR_STATE if fewer than P slots
+ * are free. slots (host, P) receives the slot of each point. */
+int bte_engine_admit(bte_engine* e, int P, const double* n0, const double* ne, const double* ns_by_n0,
+                     const double* Tg, const double* E, const double* f0, int ee, int32_t* slots, void* stream);
+/* One Newton iteration of every running point. n_done (host) receives the number of points
+ * whose solve ended in this step and done_slots (host, capacity) their slots. */
+int bte_engine_step(bte_engine* e, int* n_done, int32_t* done_slots, void* stream);
+/* Results of P finished slots (host list): f [P x n] the normalized distribution
+ * (normalized_distribution, bte_0d3v_batched.py:1204-1217), status and iters (device int32,
+ * may be NULL: total Newton iterations of both solves). The slots become free. */
+int bte_engine_collect(bte_engine* e, int P, const int32_t* slots, double* f, int32_t* status, int32_t* iters,
+                       void* stream);
+/* ints4 = {capacity, free slots, running points, fp64 capacity}; bytes = device memory the
+ * engine holds (its per-slot footprint is bytes / capacity). */
+int bte_engine_info(const bte_engine* e, int* ints4, size_t* bytes);
+
 /* Last CUDA error string seen by the library on this thread (never NULL). */
 const char* bte_last_error(void);
 
