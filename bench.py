@@ -48,6 +48,10 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-points", type=int, default=2)
+    ap.add_argument("--serve-requests", type=int, default=40,
+                    help="requests of the serving mix (Poisson arrivals, 1-512 points, 15 grid sizes)")
+    ap.add_argument("--serve-budget-gb", type=float, default=16.0, help="HBM budget of admitted points")
+    ap.add_argument("--no-serve", action="store_true")
     return ap.parse_args()
 
 
@@ -257,6 +261,82 @@ def run_gb300(a, rank, ws):
                 plain=plain, setup_s=t_setup)
 
 
+def _serve_run(xs, specs, precision, a, rate=None):
+    """One serving run: requests submitted at their arrival times (all at once if rate is None)."""
+    from boltzmann_gb300.serving import BteServer, SolveRequest, wait_all, latency_summary
+    grids = sorted({(r["n_sp"], r["l_max"]) for r in specs})
+    mk = lambda r: SolveRequest(n_sp=r["n_sp"], l_max=r["l_max"], n0=r["n0"], ne=r["ne"], Tg=r["Tg"], E=r["E"],
+                                ns_by_n0=r["ns_by_n0"])
+    t_setup = time.perf_counter()
+    srv = BteServer(xs, grids, precision=precision, hbm_budget_bytes=int(a.serve_budget_gb * (1 << 30)),
+                    capacity=512, fp64_capacity=64)
+    try:
+        s0 = specs[0]
+        warm = [srv.submit(mk(dict(n_sp=g[0], l_max=g[1], n0=s0["n0"][:2], ne=s0["ne"][:2], Tg=s0["Tg"][:2],
+                                   E=s0["E"][:2], ns_by_n0=s0["ns_by_n0"][:, :2]))) for g in grids]
+        wait_all(warm, timeout=600)
+        t_setup = time.perf_counter() - t_setup
+        t0 = time.perf_counter()
+        reqs = []
+        for r in specs:
+            if rate is not None:
+                dt = t0 + r["t"] - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+            reqs.append(srv.submit(mk(r)))
+        wait_all(reqs, timeout=3600)
+        summ = latency_summary(reqs)
+        summ["peak_budget_used_gb"] = srv.peak_used / (1 << 30)
+        summ["setup_s"] = t_setup
+        summ["status_counts"] = {str(k): int(v) for k, v in zip(*np.unique(
+            np.concatenate([q.qoi["status"] for q in reqs]), return_counts=True))}
+    finally:
+        srv.close()
+    return summ, reqs
+
+
+def serve_bench(a):
+    """Serving mix: Poisson arrivals of requests of 1-512 points on grids N_sp in {64..256} x
+    l_max in {1,2,3} (seed 20261204). Capacity of each form from a run with every request
+    queued at t = 0; latency from Poisson arrivals at 80% of the plain FP64 capacity."""
+    import torch
+    from boltzmann_gb300.workloads import write_synthetic_lxcat, serving_requests
+    xs = write_synthetic_lxcat()
+    try:
+        specs = serving_requests(a.serve_requests, float("inf"))
+        pts = sum(len(r["n0"]) for r in specs)
+        sat = {}
+        for prec in ("mixed", "fp64"):
+            summ, _ = _serve_run(xs, specs, prec, a)
+            sat[prec] = summ
+            torch.cuda.empty_cache()
+        cap_fp64 = sat["fp64"]["solves_per_s"]
+        rate = 0.8 * cap_fp64 / (pts / len(specs))  # requests per second
+        specs_p = serving_requests(a.serve_requests, rate)
+        pois, res = {}, {}
+        for prec in ("mixed", "fp64"):
+            summ, reqs = _serve_run(xs, specs_p, prec, a, rate=rate)
+            pois[prec] = summ
+            res[prec] = reqs
+            torch.cuda.empty_cache()
+        err = np.concatenate([np.linalg.norm(m.ff - p.ff, axis=0) / np.linalg.norm(p.ff, axis=0)
+                              for m, p in zip(res["mixed"], res["fp64"])])
+    finally:
+        os.unlink(xs)
+    return {
+        "workload": "%d requests (1-512 points, N_sp in {64,96,128,192,256} x l_max in {1,2,3}, E/N log-uniform "
+                    "[1,1000] Td, ionization degree log-uniform [1e-8,1e-3], e-e warm start then e-e on), seed 20261204; "
+                    "%d points" % (len(specs), pts),
+        "hbm_budget_gb": a.serve_budget_gb,
+        "saturation": {"mixed": sat["mixed"], "fp64": sat["fp64"],
+                       "mixed_over_fp64": sat["mixed"]["solves_per_s"] / cap_fp64},
+        "poisson": {"rate_requests_per_s": rate, "offered_solves_per_s": 0.8 * cap_fp64,
+                    "mixed": pois["mixed"], "fp64": pois["fp64"]},
+        "edf_rel_err_mixed_vs_fp64": {"max": float(err.max()), "p50": float(np.median(err)),
+                                      "p99": float(np.percentile(err, 99)), "points_above_1e-8": int(np.sum(err > 1e-8))},
+    }
+
+
 def roofline(st, peaks):
     fams = {k: v for k, v in st.items() if isinstance(v, dict) and "ms" in v}
     dom = max(fams, key=lambda k: fams[k]["ms"])
@@ -338,6 +418,7 @@ def main():
     r = run_gb300(a, rank, ws)
     if rank != 0:
         return
+    serve = None if (a.no_serve or ws > 1) else serve_bench(a)
     cpu = None if a.no_cpu else cpu_sample(a, a.cpu_points, 3)
     st = r["stats"]
     steps_ms = sorted(r["steps_ms"])
@@ -352,7 +433,7 @@ def main():
         "fp64_fallback_points_per_step": st["fp64_fallback_points"] / a.steps,
         "fp64_fallback_reasons": st["fp64_fallback_reasons"],
         "roofline": roofline(st, peaks), "cpu_baseline": cpu, "clocks": r["clocks"],
-        "plain_fp64": r["plain"], "setup_s": r["setup_s"],
+        "plain_fp64": r["plain"], "serving": serve, "setup_s": r["setup_s"],
         "newton_iters": {"mean": float(np.mean(r["iters"])), "max": int(np.max(r["iters"]))},
         "status_counts": {str(k): int(v) for k, v in zip(*np.unique(r["status"], return_counts=True))},
     }

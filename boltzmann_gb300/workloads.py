@@ -103,3 +103,28 @@ def config_parameters(name: str, n_pts: int | None = None):
         return dict(n0=n0, ne=np.zeros(n), Tg=np.full(n, 300.0), E=100.0 * n0 * TD,
                     ns_by_n0=np.ones((1, n)), EbyN=np.full(n, 100.0))
     return batch_parameters(n, c["seed"], ion_deg_range=c["ion"], ee=c["ee"])
+
+
+# Serving mix: Poisson arrivals of requests of 1..512 points on grids with N_sp in
+# {64, 96, 128, 192, 256} and l_max in {1, 2, 3}; E/N and ionization degree as the batched
+# workload; seed 20261204.
+SERVE_N_SP = (64, 96, 128, 192, 256)
+SERVE_L_MAX = (1, 2, 3)
+
+
+def serving_requests(n_req: int, rate_per_s: float, seed: int = 20261204, max_points: int = 512,
+                     n_sp_choices=SERVE_N_SP, l_max_choices=SERVE_L_MAX):
+    """Requests as dicts (arrival time in s from the start, n_sp, l_max and the per-point
+    parameters of batch_parameters). rate_per_s = inf gives every arrival at t = 0."""
+    rng = np.random.default_rng(seed)
+    out = []
+    t = 0.0
+    for i in range(n_req):
+        if np.isfinite(rate_per_s):
+            t += rng.exponential(1.0 / rate_per_s)
+        P = int(rng.integers(1, max_points + 1))
+        n_sp = int(rng.choice(n_sp_choices))
+        l_max = int(rng.choice(l_max_choices))
+        prm = batch_parameters(P, int(rng.integers(0, 2**31 - 1)))
+        out.append(dict(t=t, n_sp=n_sp, l_max=l_max, **prm))
+    return out
