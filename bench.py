@@ -319,8 +319,13 @@ def serve_bench(a):
             pois[prec] = summ
             res[prec] = reqs
             torch.cuda.empty_cache()
-        err = np.concatenate([np.linalg.norm(m.ff - p.ff, axis=0) / np.linalg.norm(p.ff, axis=0)
-                              for m, p in zip(res["mixed"], res["fp64"])])
+        # per-point EDF difference over points both forms converged (status 0 or 1)
+        err, n_unconv = [], 0
+        for m, p in zip(res["mixed"], res["fp64"]):
+            ok = (m.qoi["status"] <= 1) & (p.qoi["status"] <= 1)
+            n_unconv += int(np.sum(~ok))
+            err.append((np.linalg.norm(m.ff - p.ff, axis=0) / np.linalg.norm(p.ff, axis=0))[ok])
+        err = np.concatenate(err)
     finally:
         os.unlink(xs)
     return {
@@ -333,7 +338,8 @@ def serve_bench(a):
         "poisson": {"rate_requests_per_s": rate, "offered_solves_per_s": 0.8 * cap_fp64,
                     "mixed": pois["mixed"], "fp64": pois["fp64"]},
         "edf_rel_err_mixed_vs_fp64": {"max": float(err.max()), "p50": float(np.median(err)),
-                                      "p99": float(np.percentile(err, 99)), "points_above_1e-8": int(np.sum(err > 1e-8))},
+                                      "p99": float(np.percentile(err, 99)), "points_above_1e-8": int(np.sum(err > 1e-8)),
+                                      "points_compared": int(err.size), "points_unconverged_in_either": n_unconv},
     }
 
 

@@ -258,6 +258,33 @@ __global__ void k_export(ExportView v, int which, double* out, size_t count) {
 }
 
 // Maxwellian projection (bte_0d3v_batched.py:481-520 via utils.function_to_basis, utils.py:475-532)
+// int v^3 phi_p phi_k dv over the whole radial domain (the 1D3V spatial-advection radial
+// integral, bte_1d3v_solver.py:529-564): per-interval Gauss-Legendre, exact for the degree-9
+// integrand; one thread per (p, k), zero outside |p - k| <= 3
+__global__ void k_radial_v3(int nsp, const int* __restrict__ iv_span, int q, const double* __restrict__ x,
+                            const double* __restrict__ w, const int* __restrict__ span, const double* __restrict__ B,
+                            double* out) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nsp * nsp) return;
+    const int p = e / nsp, k = e % nsp;
+    double s = 0.0;
+    if (abs(p - k) <= BTE_SP_ORDER) {
+        // the supports of p and k overlap on knot spans max(p,k) .. min(p,k) + 3
+        for (int j = max(p, k); j <= min(p, k) + BTE_SP_ORDER; ++j) {
+            const int iv = iv_span[j];
+            if (iv < 0) continue;
+            for (int gq = 0; gq < q; ++gq) {
+                const int idx = iv * q + gq;
+                const int jp = p - (span[idx] - BTE_SP_ORDER), jk = k - (span[idx] - BTE_SP_ORDER);
+                if (jp < 0 || jp > 3 || jk < 0 || jk > 3) continue;
+                const double xx = x[idx];
+                s += w[idx] * xx * xx * xx * B[(idx * 3) * 4 + jp] * B[(idx * 3) * 4 + jk];
+            }
+        }
+    }
+    out[e] = s;
+}
+
 __global__ void k_maxwell_rhs(int nsp, const int* __restrict__ iv_span, int q, const double* __restrict__ x,
                               const double* __restrict__ w, const int* __restrict__ span, const double* __restrict__ B,
                               double* radial) {
@@ -332,6 +359,7 @@ int bte_grid_export(const bte_grid* g, int which, double* out, size_t count, voi
         case BTE_OP_MASS: case BTE_OP_MINV: case BTE_OP_ADV_RAW: case BTE_OP_COL_GT_RAW: need = n * n; break;
         case BTE_OP_HL: case BTE_OP_GL: if (!g->ee) return fail(BTE_ERR_STATE, "grid built without e-e"); need = n * n; break;
         case BTE_OP_COL_RAW: need = (size_t)g->nspecies * n * n; break;
+        case BTE_OP_RADIAL_V3: need = nsp * nsp; break;
         case BTE_OP_MASS_VEC: case BTE_OP_TEMP_VEC: need = n; break;
         case BTE_OP_MOBILITY: case BTE_OP_DIFFUSION: need = nsp; break;
         case BTE_OP_RATES: need = (size_t)g->nproc * nsp; break;
@@ -342,6 +370,12 @@ int bte_grid_export(const bte_grid* g, int which, double* out, size_t count, voi
     }
     if (count != need) return fail(BTE_ERR_ARG, "count does not match the operator size");
     cudaSetDevice(g->device);
+    if (which == BTE_OP_RADIAL_V3) {
+        k_radial_v3<<<(unsigned)((need + 127) / 128), 128, 0, (cudaStream_t)stream>>>(
+            g->nsp, g->d_span_iv, g->q5.q, g->q5.x, g->q5.w, g->q5.span, g->q5.B, out);
+        CUDA_OR_FAIL(cudaGetLastError(), "k_radial_v3");
+        return BTE_OK;
+    }
     ExportView v{g->nsp, g->nsh, g->n, g->lmax, g->nspecies, g->nproc, g->ntri, g->d_t, g->d_Mr, g->d_Minv, g->d_mm1,
                  g->d_mm2, g->d_q0, g->d_q1, g->d_cgT, g->d_adv_coef, g->d_mass, g->d_temp, g->d_mob, g->d_diff,
                  g->d_rate, g->d_HL, g->d_GL, g->d_CA, g->d_CB, g->d_tri};

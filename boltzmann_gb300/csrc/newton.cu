@@ -1041,25 +1041,28 @@ static double jac_flops_pt(const BteGrid* g, int ee) {
 static double lu_flops(int N) { return (2.0 / 3.0) * (double)N * N * N + (double)N * N; }
 
 // points with status >= 2 (not converged) -> act list; their status reset to running
+// A point's Newton budget (max_iter) covers both forms: a point that used it up in the
+// mixed form ends with MAXITER; one whose line search, factorization or refinement failed
+// (or whose residual became non-finite) continues in FP64 with the iterations it has left.
 __global__ void k_collect_failed(int P, int* status, int* act_out, int* nout, int* reason) {
     int pt = blockIdx.x * blockDim.x + threadIdx.x;
     if (pt >= P) return;
     reason[pt] = status[pt];
-    if (status[pt] >= BTE_ST_MAXITER) {
+    if (status[pt] >= BTE_ST_LINESEARCH) {
         status[pt] = -1;
         act_out[atomicAdd(nout, 1)] = pt;
     }
 }
 
-// a point handed over because its refinement stalled keeps its last accepted iterate (every
-// iterate the mixed form accepted decreased the FP64 merit); the others restart from h0
+// a point handed to the FP64 form keeps its last accepted iterate (every iterate the mixed
+// form accepted decreased the FP64 merit) and its iteration count; only a point whose
+// residual became non-finite restarts from h0
 __global__ void k_restore(int n, int nact, const int* __restrict__ act, const int* __restrict__ reason,
                           const double* __restrict__ h0, double* h, int* nit) {
     int slot = blockIdx.x;
     if (slot >= nact) return;
     int pt = act[slot];
-    if (threadIdx.x == 0) nit[pt] = 0;
-    if (reason[pt] == BTE_ST_NEED_FP64) return;
+    if (reason[pt] != BTE_ST_NONFINITE) return;
     for (int i = threadIdx.x; i < n; i += blockDim.x) h[(size_t)pt * n + i] = h0[(size_t)pt * n + i];
 }
 
@@ -1382,7 +1385,7 @@ __global__ void k_engine_sort(int nold, const int* __restrict__ old, const int* 
     const int pt = old[i];
     const int st = status[pt];
     if (st < 0) return;  // still running
-    if (can_fb && st >= BTE_ST_MAXITER) { fb[atomicAdd(&cnt[1], 1)] = pt; return; }
+    if (can_fb && st >= BTE_ST_LINESEARCH) { fb[atomicAdd(&cnt[1], 1)] = pt; return; }
     if (st <= BTE_ST_ROUNDOFF && phase[pt] == 0 && want_ee[pt]) { sw[atomicAdd(&cnt[2], 1)] = pt; return; }
     done[atomicAdd(&cnt[0], 1)] = pt;
 }
@@ -1395,8 +1398,8 @@ __global__ void k_engine_to_fp64(int m, const int* __restrict__ list, int n, int
     const int pt = list[i];
     const int st = status[pt];
     __syncthreads();
-    if (threadIdx.x == 0) { reason[pt] = st; status[pt] = -1; nit[pt] = 0; }
-    if (st == BTE_ST_NEED_FP64) return;
+    if (threadIdx.x == 0) { reason[pt] = st; status[pt] = -1; }
+    if (st != BTE_ST_NONFINITE) return;
     for (int k = threadIdx.x; k < n; k += blockDim.x) h[(size_t)pt * n + k] = h0[(size_t)pt * n + k];
 }
 

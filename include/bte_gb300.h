@@ -101,6 +101,8 @@ int bte_grid_info(const bte_grid* g, int* ints8, double* dbls4);
 #define BTE_OP_GL 12        /* n x n        compute_rosenbluth_potentials_op (gl)    */
 #define BTE_OP_CC_A 13      /* n x n x n    coulomb_collision_op_assembly (cc_a)     */
 #define BTE_OP_CC_B 14      /* n x n x n    coulomb_collision_op_assembly (cc_b)     */
+#define BTE_OP_RADIAL_V3 15 /* n_sp x n_sp  int v^3 phi_p phi_k dv: the 1D3V x-advection radial
+                                   integral (bte_1d3v_solver.py:529-564, compute_spatial_advection_op) */
 int bte_grid_export(const bte_grid* g, int which, double* out, size_t count, void* stream);
 
 /* Maxwellian initial state for P points (device f, P x n).
