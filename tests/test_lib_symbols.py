@@ -9,8 +9,10 @@ ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
 
 
 def declared_symbols():
-    src = open(os.path.join(ROOT, "include", "bte_gb300.h")).read()
-    return sorted(set(re.findall(r"^(?:int|const char\*)\s+(bte_\w+)\s*\(", src, flags=re.M)))
+    """Every entry point declared in include/*.h."""
+    inc = os.path.join(ROOT, "include")
+    src = "".join(open(os.path.join(inc, f)).read() for f in sorted(os.listdir(inc)) if f.endswith(".h"))
+    return sorted(set(re.findall(r"^(?:int|long long|const char\*)\s+(bte\w+)\s*\(", src, flags=re.M)))
 
 
 @pytest.fixture(scope="module")
@@ -22,7 +24,8 @@ def lib():
 
 def test_header_declares_entry_points():
     syms = declared_symbols()
-    for s in ["bte_grid_create", "bte_solve_steady", "bte_qoi", "bte_lu_factor", "bte_lu_solve"]:
+    for s in ["bte_grid_create", "bte_solve_steady", "bte_qoi", "bte_lu_factor", "bte_lu_solve", "bte_engine_step",
+              "bte1d_step_x", "bte1d_step_v", "bte1d_lmat"]:
         assert s in syms
 
 
