@@ -16,7 +16,7 @@ PREC_FP64 = 0
 PREC_MIXED = 1
 
 OP = dict(KNOTS=0, MASS=1, MINV=2, ADV_RAW=3, COL_RAW=4, COL_GT_RAW=5, MASS_VEC=6, TEMP_VEC=7,
-          MOBILITY=8, DIFFUSION=9, RATES=10, HL=11, GL=12, CC_A=13, CC_B=14)
+          MOBILITY=8, DIFFUSION=9, RATES=10, HL=11, GL=12, CC_A=13, CC_B=14, RADIAL_V3=15)
 
 STATUS = {0: "converged", 1: "roundoff", 2: "max_iter", 3: "line_search", 4: "non_finite", 5: "singular"}
 
@@ -24,7 +24,8 @@ EXPORTED = ["bte_grid_create", "bte_grid_destroy", "bte_grid_info", "bte_grid_ex
             "bte_solve_steady", "bte_qoi", "bte_lu_factor", "bte_lu_solve", "bte_last_error",
             "bte_radial_components", "bte_stats_reset", "bte_stats", "bte_solve_info", "bte_lu_factor_ex",
             "bte_engine_create", "bte_engine_destroy", "bte_engine_admit", "bte_engine_step", "bte_engine_collect",
-            "bte_engine_info"]
+            "bte_engine_info", "bte1d_create", "bte1d_destroy", "bte1d_step_x", "bte1d_step_v", "bte1d_lmat",
+            "bte1d_ords_to_lm", "bte1d_lm_to_ords", "bte1d_launches", "bte1d_last_error"]
 
 STAT_FAMILIES = ["residual", "jacobian", "lu_factor", "lu_solve", "refine", "other"]
 
@@ -37,7 +38,7 @@ class GridDesc(C.Structure):
         ("proc_type", C.POINTER(C.c_int)), ("proc_species", C.POINTER(C.c_int)),
         ("proc_threshold", C.POINTER(C.c_double)), ("proc_attach", C.POINTER(C.c_double)),
         ("sigma_offsets", C.POINTER(C.c_int)), ("sigma_energy", C.POINTER(C.c_double)),
-        ("sigma_values", C.POINTER(C.c_double)), ("device", C.c_int),
+        ("sigma_values", C.POINTER(C.c_double)), ("device", C.c_int), ("plain_knots", C.c_int),
     ]
 
 
@@ -92,6 +93,17 @@ def load() -> C.CDLL:
     lib.bte_engine_step.argtypes = [vp, C.POINTER(C.c_int), i32p, vp]
     lib.bte_engine_collect.argtypes = [vp, C.c_int, i32p, vp, vp, vp, vp]
     lib.bte_engine_info.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_size_t)]
+    dp = C.POINTER(C.c_double)
+    lib.bte1d_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int] + [dp] * 9 + [C.c_int, C.POINTER(C.c_void_p)]
+    lib.bte1d_destroy.argtypes = [vp]
+    lib.bte1d_step_x.argtypes = [vp, C.c_double, vp, vp]
+    lib.bte1d_step_v.argtypes = [vp, C.c_double, vp, vp, C.c_double, C.c_double, C.c_int, dp, vp]
+    lib.bte1d_lmat.argtypes = [vp, C.c_double, vp, vp, vp, vp]
+    lib.bte1d_ords_to_lm.argtypes = [vp, vp, vp, vp]
+    lib.bte1d_lm_to_ords.argtypes = [vp, vp, vp, vp]
+    lib.bte1d_launches.argtypes = [vp]
+    lib.bte1d_launches.restype = C.c_longlong
+    lib.bte1d_last_error.restype = C.c_char_p
     if hasattr(lib, "bte_initialize_noalloc"):
         lib.bte_initialize_noalloc.argtypes = [vp, C.c_int, vp, vp]
     if hasattr(lib, "bte_radial_components"):

@@ -170,7 +170,7 @@ class bte_0d3v_batched:
             ev_max=float(self._par_ev_range[grid_idx][1]), Te=float(self._par_ap_Te[grid_idx]), mByM=mByM,
             n_processes=len(names), n_species=len(species), proc_type=ip(types), proc_species=ip(spec),
             proc_threshold=dp(thr), proc_attach=dp(att), sigma_offsets=ip(offs), sigma_energy=dp(se),
-            sigma_values=dp(sv), device=int(self._dev_id))
+            sigma_values=dp(sv), device=int(self._dev_id), plain_knots=int(getattr(self, "_plain_knots", 0)))
         if int(self._args.sp_order) != 3:
             raise NotImplementedError("only cubic B-splines (sp_order 3) are supported")
         lib = _lib.load()

@@ -1,0 +1,257 @@
+"""GB300 1D3V Boltzmann step: spectral v-space (B-splines x spherical harmonics), discrete
+ordinates in v-theta, Chebyshev collocation in x.
+
+Counterpart of the spectral path of the reference's `bte_1d3v`
+(`BESolver/python/bte_1d3v_solver.py:218-2244`) with its Strang split
+(`step`, :1885-1889): x-advection over dt/2 (`step_bte_x`, :912-982), the v-space step over dt
+(`step_bte_v`, :984-1137), x-advection over dt/2. The time-step work runs in the CUDA library
+(`include/bte1d_gb300.h`); this class builds the setup operators:
+
+* the v-space operators come from the library's own device assembly of the grid (the same
+  operators `bte_0d3v_batched` uses): Cv = tau n0 np0 M^-1 (C_en + Tg C_gT), Av = tau M^-1 A;
+* the radial x-advection operator adv_x = M_r^-1 vth (tau / L) int v^3 phi_p phi_k and its
+  eigendecomposition (:621-625), the ordinate rule (`gl_vt`, spec_spherical.py:1020-1064), the
+  ordinate <-> harmonic projections (:997-1008) and the Chebyshev derivative
+  (collocation_op.py:8-33) are small dense set-up matrices built on the host.
+
+Differences from the reference, by design: the v-step's GMRES is preconditioned with each
+point's own block (I - dt (Cv + E_x Av))^-1 factored in FP32, where the reference uses the
+inverse of the nearest of `num_pc_ops` E values; the x-step solves its backward-Euler systems
+with LU factors, where the reference multiplies by their explicit inverses. Both reach the
+same solution to the solver tolerance. Only the BE Chebyshev x-space and the spectral v-space
+(the reference's `xspace_type = 1`, `vspace_type = 1`) are provided.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import types
+
+import numpy as np
+
+from . import _lib
+
+QE = 1.602176634e-19
+ME = 9.1093837139e-31
+KB = 1.380649e-23
+TORR = 101325.0 / 760.0
+NP0 = 8e16                    # nominal electron density (bte_1d3v_solver.py:103)
+
+
+def ordinates(Nvt):
+    """gl_vt(Nvt, hspace_split=True, mode="npsp") (spec_spherical.py:1060-1064): a Gauss-Legendre
+    rule of Nvt/2 points on each half of cos(theta) in [-1, 0] and [0, 1]."""
+    gx, gw = np.polynomial.legendre.leggauss(Nvt // 2)
+    mu = np.append(0.5 * gx - 0.5, 0.5 * gx + 0.5)
+    return np.arccos(mu), np.append(0.5 * gw, 0.5 * gw)
+
+
+def real_sph_m0(l, theta):
+    """Real spherical harmonic Y_l^0(theta): sqrt((2l + 1) / 4 pi) P_l(cos theta)."""
+    c = np.zeros(l + 1)
+    c[l] = 1.0
+    return np.sqrt((2 * l + 1) / (4 * np.pi)) * np.polynomial.legendre.legval(np.cos(theta), c)
+
+
+def sph_ords_projections(theta, w, l_max):
+    """(psh2o [Nvt x nsh], po2sh [nsh x Nvt]) of spec_spherical.py:997-1008 for m = 0 modes."""
+    Vq = np.array([real_sph_m0(l, theta) for l in range(l_max + 1)])
+    return Vq.T.copy(), (Vq * w[None, :] * 2 * np.pi)
+
+
+def chebyshev(Np):
+    """Chebyshev-Gauss-Lobatto points -cos(pi i / (Np - 1)) and the collocation derivative
+    (collocation_op.py:8-33: derivative Vandermonde times the inverse value Vandermonde)."""
+    deg = Np - 1
+    xp = -np.cos(np.pi * np.linspace(0, deg, Np) / deg)
+    V0 = np.polynomial.chebyshev.chebvander(xp, deg)
+    V0inv = np.linalg.solve(V0, np.identity(Np))
+    V1 = np.array([np.polynomial.Chebyshev.basis(i).deriv(m=1)(xp) for i in range(Np)]).reshape((-1, Np)).T
+    return xp, V1 @ V0inv
+
+
+def load_params(par):
+    """The reference's [bte] parameter table (bte_1d3v_solver.py:77-216) from a TOML file path or
+    a dict; returns a namespace with the derived quantities the step uses."""
+    if isinstance(par, (str, os.PathLike)):
+        import tomllib
+        with open(par, "rb") as fh:
+            tp = tomllib.load(fh)["bte"]
+    else:
+        tp = dict(par)
+    p = types.SimpleNamespace(**tp)
+    p.L = 0.5 * tp["L"]
+    p.f = tp["freq"]
+    p.tau = 1.0 / p.f
+    p.Tg = tp["Tg"]
+    p.p0 = tp["p0"]
+    n0 = p.p0 * TORR / (KB * p.Tg) if p.Tg != 0 else 3.22e22 * p.p0
+    p.np0 = NP0
+    p.n0 = n0 / NP0
+    p.l_max = tp["lmax"]
+    p.gmres_rsrt_iter = tp.get("gmres_rsrt_iter", 10)
+    p.gmres_maxiter = p.gmres_rsrt_iter * tp["gmres_rsrt"]
+    if tp.get("xspace_type", 1) != 1 or tp.get("vspace_type", 1) != 1:
+        raise NotImplementedError("only the BE Chebyshev x-space and the spectral v-space are provided")
+    if tp.get("ev_extend", 0) != 0:
+        raise NotImplementedError("only ev_extend = 0 (the v-grid ends at ev_max)")
+    return p
+
+
+class bte_1d3v:
+    """Spectral 1D3V solver on one GPU. `par` is the reference's parameter file (TOML with a
+    [bte] table) or the same table as a dict; `collisions` in it names an LXCat file."""
+
+    def __init__(self, par, device=0):
+        import torch
+        from .bte_0d3v_batched import bte_0d3v_batched, vspace_grid_extension
+        self.torch = torch
+        self.params = p = load_params(par)
+        self.device = device
+        torch.cuda.set_device(device)
+        Nr = p.Nr + 1
+        nsh = p.l_max + 1
+        self.dof_vr, self.dof_vt, self.dof_x = Nr, p.Nvt, p.Np
+        self.num_sh = nsh
+        self.dof_v = Nr * nsh
+        # the velocity grid and its operators, assembled on the device
+        args = types.SimpleNamespace(threads=1, sp_order=p.sp_order, spline_qpts=p.spline_qpts, ee_collisions=0,
+                                     verbose=0, use_gpu=1, Efreq=0.0, dt=p.dt, cycles=1, solver_type="steady-state",
+                                     l_max=p.l_max, Nr=p.Nr, n_pts=p.Np, precision="fp64")
+        s = bte_0d3v_batched(args, np.array([float(p.ev_max)]), np.array([float(p.Te)]), np.array([p.Nr]),
+                             [[[l, 0] for l in range(nsh)]], 1, [p.collisions])
+        s._dev_id = device
+        s._plain_knots = 1  # the 1D3V basis has no threshold knots (bte_1d3v_solver.py:356, sig_pts=None)
+        s.assemble_operators(0, vspace_ext=vspace_grid_extension.NONE)
+        self.grid = s
+        info = s._grid_info[0]
+        self.vth = info["vth"]
+        n = info["n"]
+        Minv = s.export_operator(0, "MINV")
+        col = s.export_operator(0, "COL_RAW").sum(dim=0)
+        colT = s.export_operator(0, "COL_GT_RAW")
+        adv = s.export_operator(0, "ADV_RAW") * ((1.0 / self.vth) * (QE / ME))
+        self.op_col_en = Minv @ col
+        self.op_col_gT = Minv @ colT
+        self.op_adv_v = Minv @ adv
+        Cv = p.tau * p.n0 * p.np0 * (self.op_col_en + p.Tg * self.op_col_gT)
+        Av = p.tau * self.op_adv_v
+        # radial x-advection operator and its eigendecomposition (bte_1d3v_solver.py:529-564,621-625)
+        Mr_inv = Minv[0::nsh, 0::nsh]
+        v3 = torch.empty((Nr, Nr), dtype=torch.float64, device="cuda")
+        _lib.check(_lib.load().bte_grid_export(s._grid[0], _lib.OP["RADIAL_V3"], _lib.ptr(v3), v3.numel(),
+                                               C.c_void_p(torch.cuda.current_stream().cuda_stream)), "bte_grid_export")
+        adv_x = (Mr_inv @ (self.vth * (p.tau / p.L) * v3)).cpu().numpy()
+        d, Q = np.linalg.eig(adv_x)
+        if np.max(np.abs(d.imag)) > 1e-12 * np.max(np.abs(d.real)):
+            raise RuntimeError("the radial x-advection operator has complex eigenvalues")
+        d, Q = d.real.copy(), Q.real.copy()
+        Qinv = np.linalg.inv(Q)
+        self.op_adv_x, self.op_adv_x_d, self.op_adv_x_q, self.op_adv_x_qinv = adv_x, d, Q, Qinv
+        self.xp_vt, self.xp_vt_qw = ordinates(p.Nvt)
+        self.op_psh2o, self.op_po2sh = sph_ords_projections(self.xp_vt, self.xp_vt_qw, p.l_max)
+        self.xp, self.Dp = chebyshev(p.Np)
+        lib = _lib.load()
+        dp = lambda a: np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(C.POINTER(C.c_double))
+        self._keep = [np.ascontiguousarray(a, dtype=np.float64) for a in
+                      (Q, Qinv, d, np.cos(self.xp_vt), self.Dp, self.op_po2sh, self.op_psh2o,
+                       Cv.cpu().numpy(), Av.cpu().numpy())]
+        h = C.c_void_p()
+        rc = lib.bte1d_create(int(device), Nr, nsh, int(p.Nvt), int(p.Np), *[dp(a) for a in self._keep],
+                              int(p.gmres_rsrt), C.byref(h))
+        if rc != 0:
+            raise RuntimeError("bte1d_create failed (%d): %s" % (rc, lib.bte1d_last_error().decode()))
+        self._h = h
+        self.mass_op = s.export_operator(0, "MASS_VEC")
+        self.gmres_info = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            _lib.load().bte1d_destroy(h)
+            self._h = None
+
+    # ------------------------------------------------------------------ helpers
+    def _s(self):
+        return C.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise RuntimeError("%s failed (%d): %s" % (what, rc, _lib.load().bte1d_last_error().decode()))
+
+    def _dev(self, a, shape):
+        t = self.torch.as_tensor(a, dtype=self.torch.float64, device="cuda")
+        return t.reshape(shape).contiguous()
+
+    # ------------------------------------------------------------------ reference interface
+    def init(self, dt):
+        """The reference's init(dt) (:1333-1344) builds the preconditioner matrices; here the
+        per-point blocks are factored inside each v-step, so only dt is recorded."""
+        self.params.dt = dt
+
+    def ords_to_sph(self, x):
+        """(Nr * Nvt, Nx) ordinates -> (Nr * nsh, Nx) harmonic coefficients (:678-685)."""
+        V = self._dev(x, (self.dof_vr * self.dof_vt, self.dof_x))
+        U = self.torch.empty((self.dof_x, self.dof_v), dtype=self.torch.float64, device="cuda")
+        self._check(_lib.load().bte1d_ords_to_lm(self._h, _lib.ptr(V), _lib.ptr(U), self._s()), "bte1d_ords_to_lm")
+        return U.t().contiguous()
+
+    def sph_to_ords(self, x):
+        """(Nr * nsh, Nx) harmonic coefficients -> (Nr * Nvt, Nx) ordinates (:687-694)."""
+        U = self._dev(x, (self.dof_v, self.dof_x)).t().contiguous()
+        V = self.torch.empty((self.dof_vr * self.dof_vt, self.dof_x), dtype=self.torch.float64, device="cuda")
+        self._check(_lib.load().bte1d_lm_to_ords(self._h, _lib.ptr(U), _lib.ptr(V), self._s()), "bte1d_lm_to_ords")
+        return V
+
+    def lmat_mvec(self, E, x, dt):
+        """Lmat_mvec of step_bte_v (:1051-1055): x - dt tau (n0 np0 (C + Tg C_T) x + E A x), x (n, Nx)."""
+        X = self._dev(x, (self.dof_v, self.dof_x)).t().contiguous()
+        Ed = self._dev(E, (self.dof_x,))
+        Y = self.torch.empty_like(X)
+        self._check(_lib.load().bte1d_lmat(self._h, float(dt), _lib.ptr(Ed), _lib.ptr(X), _lib.ptr(Y), self._s()),
+                    "bte1d_lmat")
+        return Y.t().contiguous()
+
+    def step_bte_x(self, v, time, dt, verbose=0):
+        """Backward-Euler x-advection over dt (:912-982); returns the new (Nr * Nvt, Nx) state."""
+        V = self._dev(v, (self.dof_vr * self.dof_vt, self.dof_x)).clone()
+        self._check(_lib.load().bte1d_step_x(self._h, float(dt), _lib.ptr(V), self._s()), "bte1d_step_x")
+        return V
+
+    def step_bte_v(self, E, v, dv, time, dt, verbose=0, atol=None, rtol=None, max_iter=None):
+        """v-space step over dt at field E (:984-1137); returns the new ordinates state."""
+        p = self.params
+        V = self._dev(v, (self.dof_vr * self.dof_vt, self.dof_x)).clone()
+        Ed = self._dev(E, (self.dof_x,))
+        info = (C.c_double * 4)()
+        rc = _lib.load().bte1d_step_v(self._h, float(dt), _lib.ptr(Ed), _lib.ptr(V),
+                                       float(p.rtol if rtol is None else rtol), float(p.atol if atol is None else atol),
+                                       int(p.gmres_maxiter if max_iter is None else max_iter), info, self._s())
+        self._check(rc, "bte1d_step_v")
+        self.gmres_info = {"iterations": int(info[0]), "residual_abs": info[1], "residual_rel": info[2],
+                           "status": int(info[3])}
+        if info[3] != 0:
+            raise RuntimeError("GMRES did not converge: iterations=%d ||res||/||b||=%.4e" % (info[0], info[2]))
+        return V
+
+    def step(self, E, v, dv, time, dt, verbose=0):
+        """One Strang-split step (:1885-1889): x over dt/2, v over dt, x over dt/2."""
+        v = self.step_bte_x(v, time, 0.5 * dt)
+        v = self.step_bte_v(E, v, None, time, dt)
+        return self.step_bte_x(v, time + 0.5 * dt, 0.5 * dt)
+
+    def initial_condition(self, type=0):
+        """initial_condition(type=0) (:1274-1286, maxwellian_eedf :1217-1272): a Maxwellian at the
+        normalisation temperature at every point, mass-normalized, times the density profile."""
+        if type != 0:
+            raise NotImplementedError
+        p = self.params
+        xx = p.L * (self.xp + 1)
+        ne = 1e6 * (1e7 + 1e9 * (1 - 0.5 * xx / p.L) ** 2 * (0.5 * xx / p.L) ** 2) / p.np0
+        f0 = self.torch.as_tensor(self.grid.initialize(0, 1)[:, 0], device="cuda")
+        h = f0 / (self.mass_op @ f0)
+        vo = (self.torch.as_tensor(self.op_psh2o, device="cuda") @ h.reshape(self.dof_vr, self.num_sh).t()).t()
+        return vo.reshape(-1, 1) * self.torch.as_tensor(ne, device="cuda")[None, :]
+
+    def launches(self):
+        return int(_lib.load().bte1d_launches(self._h))

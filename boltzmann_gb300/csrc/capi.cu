@@ -77,6 +77,7 @@ int bte_grid_create(const bte_grid_desc* d, bte_grid** out, void* stream) {
     if (d->n_processes < 1 || d->n_species < 1) return fail(BTE_ERR_ARG, "need at least one process and species");
     if (!(d->ev_max > 0) || !(d->Te > 0)) return fail(BTE_ERR_ARG, "ev_max and Te must be positive");
     if (d->vspace_ext != 0 && d->vspace_ext != 1) return fail(BTE_ERR_ARG, "vspace_ext must be 0 (none) or 1 (linear)");
+    if (d->plain_knots != 0 && d->plain_knots != 1) return fail(BTE_ERR_ARG, "plain_knots must be 0 or 1");
     for (int i = 0; i < d->n_processes; ++i) {
         if (d->proc_type[i] < 0 || d->proc_type[i] > 3) return fail(BTE_ERR_ARG, "unknown process type");
         if (d->proc_species[i] < 0 || d->proc_species[i] >= d->n_species) return fail(BTE_ERR_ARG, "bad species index");
@@ -119,7 +120,7 @@ int bte_grid_create(const bte_grid_desc* d, bte_grid** out, void* stream) {
     for (double sv : sig) dg.push_back(std::sqrt(sv) * cg / g->vth);
     const double k0 = std::sqrt(0.0) * cg / g->vth, k1 = std::sqrt(d->ev_max) * cg / g->vth;
     g->knots = make_knots(g->nsp, k0, d->vspace_ext == 1 ? 1.2 * k1 : k1, dg);
-    snap_knots(g->knots, k0, k1, dg);
+    if (!d->plain_knots) snap_knots(g->knots, k0, k1, dg);
     for (size_t j = 0; j + 1 < g->knots.size(); ++j) {
         if (g->knots[j] != g->knots[j + 1]) g->span_iv.push_back(g->nint++);
         else g->span_iv.push_back(-1);

@@ -55,6 +55,9 @@ typedef struct {
     const double* sigma_energy;   /* host, eV, increasing per process                          */
     const double* sigma_values;   /* host, m^2                                                 */
     int device;                   /* CUDA device ordinal                                       */
+    int plain_knots;              /* 0: knots snapped to the process thresholds (the 0D3V
+                                     solver, basis.py:356-362); 1: uniform knots only (the 1D3V
+                                     solver's basis, bte_1d3v_solver.py:356, sig_pts=None)    */
 } bte_grid_desc;
 
 typedef struct {

@@ -263,7 +263,7 @@ class Operators:
     (bte_0d3v_batched.py:310-479), with `vspace_ext` NONE or LINEAR and CG splines."""
 
     def __init__(self, processes, ev_max, Te, n_sp, l_max, sp_order=3, spline_qpts=5,
-                 extend_linear=False, ee=True, dense_coulomb=True):
+                 extend_linear=False, ee=True, dense_coulomb=True, snap=True):
         self.processes = processes
         self.sp_order = sp_order
         self.num_p = n_sp
@@ -280,7 +280,8 @@ class Operators:
         k_domain = (0.0, np.sqrt(ev_max) * C_GAMMA / vth)
         dom = (k_domain[0], 1.2 * k_domain[1]) if extend_linear else k_domain
         t = uniform_knots(dom, n_sp, sp_order)
-        t = snap_knots(t, k_domain, sp_order, dg_nodes)
+        if snap:  # the 1D3V solver's basis has no threshold knots (bte_1d3v_solver.py:356)
+            t = snap_knots(t, k_domain, sp_order, dg_nodes)
         self.knots = t
         self.k_domain = k_domain
         self.basis = B = Basis(t, sp_order)
