@@ -24,7 +24,7 @@ EXPORTED = ["bte_grid_create", "bte_grid_destroy", "bte_grid_info", "bte_grid_ex
             "bte_solve_steady", "bte_qoi", "bte_lu_factor", "bte_lu_solve", "bte_last_error",
             "bte_radial_components", "bte_stats_reset", "bte_stats", "bte_solve_info", "bte_lu_factor_ex",
             "bte_engine_create", "bte_engine_destroy", "bte_engine_admit", "bte_engine_step", "bte_engine_collect",
-            "bte_engine_info", "bte1d_create", "bte1d_destroy", "bte1d_step_x", "bte1d_step_v", "bte1d_lmat",
+            "bte_engine_info", "bte1d_create", "bte1d_destroy", "bte1d_step_x", "bte1d_step_v", "bte1d_lmat", "bte1d_block_solve",
             "bte1d_ords_to_lm", "bte1d_lm_to_ords", "bte1d_launches", "bte1d_last_error"]
 
 STAT_FAMILIES = ["residual", "jacobian", "lu_factor", "lu_solve", "refine", "other"]
@@ -99,6 +99,7 @@ def load() -> C.CDLL:
     lib.bte1d_step_x.argtypes = [vp, C.c_double, vp, vp]
     lib.bte1d_step_v.argtypes = [vp, C.c_double, vp, vp, C.c_double, C.c_double, C.c_int, dp, vp]
     lib.bte1d_lmat.argtypes = [vp, C.c_double, vp, vp, vp, vp]
+    lib.bte1d_block_solve.argtypes = [vp, C.c_double, vp, vp, vp, vp]
     lib.bte1d_ords_to_lm.argtypes = [vp, vp, vp, vp]
     lib.bte1d_lm_to_ords.argtypes = [vp, vp, vp, vp]
     lib.bte1d_launches.argtypes = [vp]

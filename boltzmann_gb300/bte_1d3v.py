@@ -212,6 +212,15 @@ class bte_1d3v:
                     "bte1d_lmat")
         return Y.t().contiguous()
 
+    def block_solve(self, E, x, dt):
+        """Per-point block inverse (I - dt (Cv + E_x Av))^-1 x in FP32 (the v-step's preconditioner), x (n, Nx)."""
+        X = self._dev(x, (self.dof_v, self.dof_x)).t().contiguous()
+        Ed = self._dev(E, (self.dof_x,))
+        Y = self.torch.empty_like(X)
+        self._check(_lib.load().bte1d_block_solve(self._h, float(dt), _lib.ptr(Ed), _lib.ptr(X), _lib.ptr(Y),
+                                                  self._s()), "bte1d_block_solve")
+        return Y.t().contiguous()
+
     def step_bte_x(self, v, time, dt, verbose=0):
         """Backward-Euler x-advection over dt (:912-982); returns the new (Nr * Nvt, Nx) state."""
         V = self._dev(v, (self.dof_vr * self.dof_vt, self.dof_x)).clone()

@@ -485,6 +485,27 @@ int bte1d_step_v(Bte1d* h, double dt, const double* E, double* V, double rtol, d
     return BTE_OK;
 }
 
+// Block preconditioner: factor each point's block I - dt (Cv + E_x Av) in FP32 and apply its
+// inverse to X (x-major v-space layout) -> Y, in FP64 storage
+int bte1d_block_solve(Bte1d* h, double dt, const double* E, const double* X, double* Y, void* stream) {
+    if (!h || !E || !X || !Y) { g_err1d = "null argument"; return BTE_ERR_ARG; }
+    cudaSetDevice(h->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    const int n = h->n, Nx = h->Nx;
+    const size_t N = (size_t)n * Nx;
+    const long long vs = (long long)n * h->vld;
+    k_build_vblocks<<<dim3(std::min<unsigned>(nb((size_t)n * n, 256), 32), Nx), 256, 0, s>>>(n, Nx, dt, h->CvT, h->AvT, E,
+                                                                                        h->VB, h->vld, vs);
+    CK1(cudaGetLastError());
+    CK1(bte_lu_factor_t<float>(Nx, n, n, h->VB, h->vld, vs, h->Vpiv, h->Vinfo, s, 0));
+    k_to_f32<<<nb(N, 256), 256, 0, s>>>(N, X, h->Zf);
+    CK1(bte_lu_solve_t<float>(Nx, n, h->VB, h->vld, vs, h->Vpiv, h->Zf, 0, s));
+    k_to_f64<<<nb(N, 256), 256, 0, s>>>(N, h->Zf, Y);
+    CK1(cudaGetLastError());
+    h->launches += 5;
+    return BTE_OK;
+}
+
 // ordinates <-> spherical harmonics (ords_to_sph / sph_to_ords, bte_1d3v_solver.py:678-694) in
 // the x-major v-space layout
 int bte1d_ords_to_lm(Bte1d* h, const double* V, double* U, void* stream) {

@@ -27,7 +27,10 @@ namespace {
 constexpr int LU_THREADS = 256;
 constexpr int LU_MAX_N = LU_THREADS * 8;
 
-template <typename T> __device__ inline T tabs(T v) { return v < T(0) ? -v : v; }
+// |v| with the sign bit cleared: -0.0 must give +0.0, because the FP32 pivot search compares
+// the bit patterns of |v| (a -0.0 kept its sign bit and outranked every positive value)
+__device__ inline float tabs(float v) { return fabsf(v); }
+__device__ inline double tabs(double v) { return fabs(v); }
 
 template <typename T> struct LuOcc { static constexpr int value = 1; };
 template <> struct LuOcc<float> { static constexpr int value = 2; };

@@ -49,6 +49,11 @@ int bte1d_step_v(bte1d* h, double dt, const double* E, double* V, double rtol, d
  * bte_1d3v_solver.py:1051-1055). */
 int bte1d_lmat(bte1d* h, double dt, const double* E, const double* X, double* Y, void* stream);
 
+/* Block preconditioner of the v-step: Y = B_x^-1 X per point, B_x = I - dt (Cv + E_x Av)
+ * factored in FP32 (x-major v-space layout). The reference's Mmat_mvec applies the inverse of
+ * the nearest of num_pc_ops E values instead (bte_1d3v_solver.py:889-910,1057-1064). */
+int bte1d_block_solve(bte1d* h, double dt, const double* E, const double* X, double* Y, void* stream);
+
 /* ordinates <-> spherical harmonics (ords_to_sph / sph_to_ords, bte_1d3v_solver.py:678-694);
  * U in the x-major v-space layout. */
 int bte1d_ords_to_lm(bte1d* h, const double* V, double* U, void* stream);

@@ -61,3 +61,33 @@ def test_lu_zero_pivot_reported():
                                  C.c_void_p(info.data_ptr()), st), "lu_factor")
     torch.cuda.synchronize()
     assert int(info.item()) == 18
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+@pytest.mark.parametrize("N", [32, 64, 200])
+def test_lu_negative_zero_is_not_a_pivot(dtype, N):
+    """-0.0 entries below a nonzero diagonal (as -dt * 0 produces) must never be chosen as
+    pivots: an identity with -0.0 below the diagonal factors with the identity permutation."""
+    import torch
+    from boltzmann_gb300 import _lib
+    lib = _lib.load()
+    P = 3
+    A = np.tril(np.full((N, N), -0.0), -1) + np.eye(N)
+    A = np.broadcast_to(A, (P, N, N)).copy()
+    tdt = torch.float64 if dtype == "f64" else torch.float32
+    dA = torch.as_tensor(A, dtype=tdt, device="cuda").contiguous()
+    assert bool(torch.signbit(dA[0, 1, 0]))
+    piv = torch.empty((P, N), dtype=torch.int32, device="cuda")
+    info = torch.empty(P, dtype=torch.int32, device="cuda")
+    b = torch.arange(P * N, dtype=tdt, device="cuda").reshape(P, N).contiguous()
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    dt = 0 if dtype == "f64" else 1
+    _lib.check(lib.bte_lu_factor(dt, P, N, C.c_void_p(dA.data_ptr()), N, N * N, C.c_void_p(piv.data_ptr()),
+                                 C.c_void_p(info.data_ptr()), st), "lu_factor")
+    x = b.clone()
+    _lib.check(lib.bte_lu_solve(dt, P, N, C.c_void_p(dA.data_ptr()), N, N * N, C.c_void_p(piv.data_ptr()),
+                                C.c_void_p(x.data_ptr()), st), "lu_solve")
+    torch.cuda.synchronize()
+    assert np.all(info.cpu().numpy() == 0)
+    assert np.array_equal(piv.cpu().numpy(), np.broadcast_to(np.arange(N), (P, N)))
+    assert torch.equal(x, b)
