@@ -72,7 +72,8 @@ def test_lu_negative_zero_is_not_a_pivot(dtype, N):
     from boltzmann_gb300 import _lib
     lib = _lib.load()
     P = 3
-    A = np.tril(np.full((N, N), -0.0), -1) + np.eye(N)
+    A = np.eye(N)
+    A[np.tril_indices(N, -1)] = -0.0  # assigned, not added: -0.0 + 0.0 is +0.0
     A = np.broadcast_to(A, (P, N, N)).copy()
     tdt = torch.float64 if dtype == "f64" else torch.float32
     dA = torch.as_tensor(A, dtype=tdt, device="cuda").contiguous()
