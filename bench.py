@@ -52,6 +52,8 @@ def parse():
                     help="requests of the serving mix (Poisson arrivals, 1-512 points, 15 grid sizes)")
     ap.add_argument("--serve-budget-gb", type=float, default=16.0, help="HBM budget of admitted points")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-1d", action="store_true", help="skip the 1D3V (config 4) leg")
+    ap.add_argument("--steps-1d", type=int, default=20)
     return ap.parse_args()
 
 
@@ -343,6 +345,103 @@ def serve_bench(a):
     }
 
 
+C4 = dict(L=2.54e-2, V0=100.0, freq=13.56e6, Tg=300.0, p0=1.0, atol=1e-14, rtol=1e-10, gmres_rsrt=30,
+          gmres_rsrt_iter=20, max_iter=300, Np=200, Nr=63, Nvt=16, lmax=1, dt=1e-3, ev_max=80.0, ev_extend=0,
+          sp_order=3, spline_qpts=5, Te=4.0, xspace_type=1, vspace_type=1)
+
+
+def c4_efield(xp, t, p):
+    """Synthetic field of the 1D3V workload: (V0 / gap) sin(2 pi t) ramped over x, so that E
+    varies along x (t in RF periods)."""
+    return (p["V0"] / p["L"]) * np.sin(2 * np.pi * t) * 0.5 * (1.0 + xp)
+
+
+def bench_1d(a, peaks):
+    """1D3V spectral Strang step (config 4: 200 Chebyshev points, 64 B-splines x l_max 1, 16
+    ordinates, dt = 1e-3 RF period, GMRES restart 30 / rtol 1e-10) on one GPU."""
+    import torch
+    from boltzmann_gb300.bte_1d3v import bte_1d3v
+    from boltzmann_gb300.workloads import write_synthetic_lxcat
+    xs = write_synthetic_lxcat()
+    p = dict(C4, collisions=xs)
+    try:
+        t0 = time.perf_counter()
+        b = bte_1d3v(p)
+        t_setup = time.perf_counter() - t0
+        v = b.initial_condition()
+        dt, t = p["dt"], 0.25
+        for _ in range(3):
+            v = b.step(c4_efield(b.xp, t, p), v, None, t, dt)
+            t += dt
+        torch.cuda.synchronize()
+        s = torch.cuda.current_stream()
+        its, L0 = [], b.launches()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        tx = tv = 0.0
+        ev[0].record(s)
+        for _ in range(a.steps_1d):
+            E = c4_efield(b.xp, t, p)
+            v = b.step(E, v, None, t, dt)
+            its.append(b.gmres_info["iterations"])
+            t += dt
+        ev[1].record(s)
+        torch.cuda.synchronize()
+        ms = ev[0].elapsed_time(ev[1]) / a.steps_1d
+        launches = (b.launches() - L0) / a.steps_1d
+        # split: x half-steps and v-step timed separately
+        for _ in range(5):
+            E = c4_efield(b.xp, t, p)
+            ev[0].record(s)
+            v1 = b.step_bte_x(v, t, 0.5 * dt)
+            ev[1].record(s)
+            v2 = b.step_bte_v(E, v1, None, t, dt)
+            ev[2].record(s)
+            v = b.step_bte_x(v2, t, 0.5 * dt)
+            ev[3].record(s)
+            torch.cuda.synchronize()
+            tx += ev[0].elapsed_time(ev[1]) + ev[2].elapsed_time(ev[3])
+            tv += ev[1].elapsed_time(ev[2])
+        tx, tv = tx / 5, tv / 5
+        # end to end through the public API with host arrays
+        vh = v.cpu().numpy()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(5):
+            E = c4_efield(b.xp, t, p)
+            vh = b.step(E, vh, None, t, dt).cpu().numpy()
+        e2e_ms = (time.perf_counter() - t0) / 5 * 1e3
+        Nr, Nvt, Nx = p["Nr"] + 1, p["Nvt"], p["Np"]
+        # x-step: each half step reads the Nr*Nvt LU factors (Nx^2 doubles) and V in, V out
+        xbytes = 2 * (Nr * Nvt * Nx * Nx * 8 + 2 * Nr * Nvt * Nx * 8)
+        hbm = peaks.get("hbm_gbs")
+        out = {
+            "workload": "1D3V spectral Strang step: 200 Chebyshev points x 64 B-splines x l_max 1 x 16 ordinates, "
+                        "BE Chebyshev x-advection, GMRES(30) rtol 1e-10 v-solve, E(x,t) = (V0/gap) sin(2 pi t) (1+x)/2",
+            "value": 1e3 / ms, "unit": "steps/s", "ms_per_step": ms, "setup_s": t_setup,
+            "gmres_iterations": {"mean": float(np.mean(its)), "max": int(np.max(its))},
+            "gpu_launches_per_step": launches, "x_steps_ms": tx, "v_step_ms": tv,
+            "e2e": {"value": 1e3 / e2e_ms, "unit": "steps/s", "h2d_bytes_per_step": int(vh.nbytes + Nx * 8),
+                    "d2h_bytes_per_step": int(vh.nbytes), "path": "bte_1d3v.step() with NumPy host arrays"},
+            "roofline_x_step": {"bound": "hbm", "achieved": xbytes / (tx * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+                                "frac": (xbytes / (tx * 1e-3) / 1e9) / hbm if hbm else None,
+                                "alg_bytes_per_step": xbytes},
+        }
+        if not a.no_cpu:
+            from oracle.bte1d_oracle import Oracle1D
+            o = Oracle1D(xs, Nx, p["Nr"], Nvt, p["lmax"], p["ev_max"], p["Te"], p["L"], p["freq"], p["Tg"], p["p0"])
+            vo = v.cpu().numpy()
+            t0 = time.perf_counter()
+            o.step(c4_efield(o.xp, t, p), vo, dt)
+            sec = time.perf_counter() - t0
+            import multiprocessing
+            out["cpu_baseline"] = {"value": 1.0 / sec, "unit": "steps/s", "cores": multiprocessing.cpu_count(),
+                                   "kind": "port", "sample": "one Strang step of the same workload (NumPy; the v-step "
+                                   "solved per point directly, the x-step through explicit inverses as the reference)"}
+    finally:
+        os.unlink(xs)
+    return out
+
+
 def roofline(st, peaks):
     fams = {k: v for k, v in st.items() if isinstance(v, dict) and "ms" in v}
     dom = max(fams, key=lambda k: fams[k]["ms"])
@@ -425,6 +524,7 @@ def main():
     if rank != 0:
         return
     serve = None if (a.no_serve or ws > 1) else serve_bench(a)
+    one_d = None if (a.no_1d or ws > 1) else bench_1d(a, peaks)
     cpu = None if a.no_cpu else cpu_sample(a, a.cpu_points, 3)
     st = r["stats"]
     steps_ms = sorted(r["steps_ms"])
@@ -439,7 +539,7 @@ def main():
         "fp64_fallback_points_per_step": st["fp64_fallback_points"] / a.steps,
         "fp64_fallback_reasons": st["fp64_fallback_reasons"],
         "roofline": roofline(st, peaks), "cpu_baseline": cpu, "clocks": r["clocks"],
-        "plain_fp64": r["plain"], "serving": serve, "setup_s": r["setup_s"],
+        "plain_fp64": r["plain"], "serving": serve, "bte_1d3v": one_d, "setup_s": r["setup_s"],
         "newton_iters": {"mean": float(np.mean(r["iters"])), "max": int(np.max(r["iters"]))},
         "status_counts": {str(k): int(v) for k, v in zip(*np.unique(r["status"], return_counts=True))},
     }
