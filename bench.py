@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-points", type=int, default=2)
-    ap.add_argument("--serve-requests", type=int, default=40,
+    ap.add_argument("--serve-requests", type=int, default=16,
                     help="requests of the serving mix (Poisson arrivals, 1-512 points, 15 grid sizes)")
     ap.add_argument("--serve-budget-gb", type=float, default=16.0, help="HBM budget of admitted points")
     ap.add_argument("--no-serve", action="store_true")
