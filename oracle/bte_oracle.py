@@ -755,3 +755,62 @@ def processes_from_lxcat(path):
     data = read_cross_section_data(path)
     mByM = data["E + Ar -> E + Ar"]["mass_ratio"]
     return [Process(k, v, mByM) for k, v in data.items()]
+
+
+def transient_solve(ops: Operators, prm: Params, f0, dt, cycles, efreq, eRe, eIm, atol, rtol, max_iter, ee):
+    """solve(..., "transient"), bte_0d3v_batched.py:1063-1155, with newton_solver_batched
+    (:59-126): backward Euler in the mass-conserving coordinates du (u + Q du), the Jacobian
+    frozen at the step's start and inverted once (a chord iteration, no line search), the
+    batch stopping when all points meet rtol or all meet atol; t is in RF periods and
+    tau = 1 / efreq (1e-7 without a field frequency); E(t) = eRe cos 2 pi t + eIm sin 2 pi t
+    when efreq > 0. Returns (u, qoi of the last completed cycle average, info)."""
+    vth = ops.vth
+    tau = 1e-7 if efreq == 0 else 1.0 / efreq
+    io_freq = int(1.0 / dt)
+    steps_total = int(cycles / dt)
+    Q = ops.Qmat
+    u = f0 / np.dot(ops.u, f0)
+    P = f0.shape[1]
+    m = Q.shape[1]
+    du = np.zeros((m, P))
+    cyc = np.zeros_like(u)
+    cyc_v = np.zeros_like(u)
+    I = np.eye(m)
+    tt = 0.0
+    iters = []
+    for ts in range(steps_total + 1):
+        E = (eRe * np.cos(2 * np.pi * (tt + dt)) + eIm * np.sin(2 * np.pi * (tt + dt))) if efreq > 0 else prm.E
+        pt = Params(prm.n0, prm.ne, prm.Tg, E, prm.ns_by_n0)
+        res, jac, _ = rhs_and_jacobian(ops, pt, ee)
+        J = np.einsum("i,jk->ijk", np.ones(P), I) - dt * tau * jac(u)
+        Jinv = np.linalg.inv(J)
+        x = du
+        r0n = np.linalg.norm(x - dt * tau * res(u + Q @ x), axis=0)
+        count = 0
+        converged = False
+        while True:
+            rr = x - dt * tau * res(u + Q @ x)
+            rn = np.linalg.norm(rr, axis=0)
+            converged = bool(np.all(rn / r0n < rtol) or np.all(rn < atol))
+            if converged or count >= max_iter:
+                break
+            x = x + np.einsum("ijk,ki->ji", Jinv, -rr)
+            count += 1
+        iters.append(count)
+        if not converged:
+            raise RuntimeError("transient Newton step did not converge at t = %.3e" % tt)
+        if ts > 0 and ts % io_freq == 0:
+            cyc *= 0.5 * dt
+            cyc_v = cyc.copy()
+            cyc[:] = 0
+            if ts == steps_total:
+                break
+        cyc += u
+        du = x
+        u = u + Q @ du
+        cyc += u
+        tt += dt
+    h = normalized_distribution(ops, cyc_v)
+    E_last = prm.E
+    qoi = compute_qois(ops, Params(prm.n0, prm.ne, prm.Tg, E_last, prm.ns_by_n0), h, effective_mobility=False)
+    return u, qoi, dict(iters=np.array(iters), cycle_avg=h)

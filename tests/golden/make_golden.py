@@ -10,6 +10,8 @@ compressed .npz fixtures next to this file:
   ee_small_reference.npz  16 B-splines, l_max 2, e-e on, 3 points: the Coulomb trilinear
                         tensors (sparse), Rosenbluth operators, warm-started converged EDFs
                         and QoIs.
+  transient_reference.npz 32 B-splines, l_max 1, 2 points, one RF period of the transient
+                        solve at dt = 0.05 period: final state and cycle-averaged QoIs.
 
 Usage:  python tests/golden/make_golden.py
 """
@@ -88,6 +90,27 @@ def ee_small(m, xs):
     np.savez_compressed(os.path.join(HERE, "ee_small_reference.npz"), **out)
 
 
+def transient(m, xs):
+    """solve(..., "transient") of the reference (bte_0d3v_batched.py:1063-1155): 32 B-splines,
+    l_max 1, e-e off, 2 points driven at 13.56 MHz, dt = 0.05 RF period over one period."""
+    n_sp, l_max, P = 32, 1, 2
+    s, args = make_solver(m, xs, n_sp, l_max, False, P)
+    args.dt, args.cycles, args.Efreq, args.solver_type = 0.05, 1.0, 13.56e6, "transient"
+    n0 = np.full(P, N0_1TORR_300K)
+    prm = dict(n0=n0, ne=np.zeros(P), Tg=np.full(P, 300.0), E=np.array([50.0, 200.0]) * n0 * 1e-21,
+               ns_by_n0=np.ones((1, P)))
+    eRe, eIm = np.array([120.0, 400.0]) * n0 * 1e-21, np.array([30.0, -100.0]) * n0 * 1e-21
+    f0 = s.initialize(0, P, "maxwellian")
+    set_params(s, prm)
+    s.set_boltzmann_parameter(0, "eRe", eRe)
+    s.set_boltzmann_parameter(0, "eIm", eIm)
+    u, qoi = s.solve(0, f0, 1e-30, 1e-10, 200, "transient")
+    out = dict(n0=prm["n0"], ne=prm["ne"], Tg=prm["Tg"], E=prm["E"], ns_by_n0=prm["ns_by_n0"], eRe=eRe, eIm=eIm,
+               dt=args.dt, cycles=args.cycles, Efreq=args.Efreq, f0=f0, u=np.asarray(u), energy=qoi["energy"],
+               mobility=qoi["mobility"], diffusion=qoi["diffusion"], rates=qoi["rates"])
+    np.savez_compressed(os.path.join(HERE, "transient_reference.npz"), **out)
+
+
 def main():
     xs = write_synthetic_lxcat(os.path.join("/tmp", "eAr_golden.lxcat"))
     cwd = os.getcwd()
@@ -95,6 +118,7 @@ def main():
     try:
         c1(m, xs)
         ee_small(m, xs)
+        transient(m, xs)
     finally:
         os.chdir(cwd)
         os.unlink(xs)

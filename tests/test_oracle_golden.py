@@ -104,3 +104,18 @@ def test_ci_known_answer_ee_off():
     rec_rates = [2.1420903714100646e-14, 1.6840849820164827e-14]
     assert abs(q["rates"][0][0] / rec_rates[0] - 1) < 2e-4
     assert abs(q["rates"][-1][0] / rec_rates[1] - 1) < 2e-4
+
+
+def test_transient_solve(synthetic_xs):
+    """The oracle's transient solve (backward Euler with a chord Newton per step, cycle-averaged
+    QoIs) against the reference's own solve(..., "transient") over one RF period."""
+    from oracle import bte_oracle as O
+    g = np.load(os.path.join(GOLDEN, "transient_reference.npz"))
+    ops = O.Operators(O.processes_from_lxcat(synthetic_xs), 80.0, 4.0, 32, 1, ee=False)
+    P = O.Params(g["n0"], g["ne"], g["Tg"], g["E"], g["ns_by_n0"])
+    u, q, _ = O.transient_solve(ops, P, g["f0"], float(g["dt"]), float(g["cycles"]), float(g["Efreq"]), g["eRe"],
+                                g["eIm"], 1e-30, 1e-10, 200, False)
+    # both stop their chord iterations at rtol 1e-10
+    assert np.max(np.abs(u - g["u"])) / np.max(np.abs(g["u"])) < 1e-9
+    for k in ("energy", "mobility", "diffusion"):
+        assert np.max(np.abs(q[k] - g[k]) / np.abs(g[k])) < 1e-9
