@@ -24,7 +24,7 @@ EXPORTED = ["bte_grid_create", "bte_grid_destroy", "bte_grid_info", "bte_grid_ex
             "bte_solve_steady", "bte_qoi", "bte_lu_factor", "bte_lu_solve", "bte_last_error",
             "bte_radial_components", "bte_stats_reset", "bte_stats", "bte_solve_info", "bte_lu_factor_ex",
             "bte_engine_create", "bte_engine_destroy", "bte_engine_admit", "bte_engine_step", "bte_engine_collect",
-            "bte_engine_info", "bte1d_create", "bte1d_destroy", "bte1d_step_x", "bte1d_step_v", "bte1d_lmat", "bte1d_block_solve",
+            "bte_engine_info", "bte_solve_transient", "bte1d_create", "bte1d_destroy", "bte1d_step_x", "bte1d_step_v", "bte1d_lmat", "bte1d_block_solve",
             "bte1d_ords_to_lm", "bte1d_lm_to_ords", "bte1d_launches", "bte1d_last_error"]
 
 STAT_FAMILIES = ["residual", "jacobian", "lu_factor", "lu_solve", "refine", "other"]
@@ -52,9 +52,8 @@ class SolveOpts(C.Structure):
 
 class TransientOpts(C.Structure):
     _fields_ = [
-        ("atol", C.c_double), ("rtol", C.c_double), ("max_iter", C.c_int), ("ee", C.c_int),
-        ("precision", C.c_int), ("dt", C.c_double), ("tau", C.c_double), ("efreq", C.c_double),
-        ("t0", C.c_double), ("n_steps", C.c_int), ("reserved", C.c_int * 5),
+        ("atol", C.c_double), ("rtol", C.c_double), ("max_iter", C.c_int), ("ee", C.c_int), ("precision", C.c_int),
+        ("dt", C.c_double), ("cycles", C.c_double), ("efreq", C.c_double), ("reserved", C.c_int * 6),
     ]
 
 
@@ -109,9 +108,7 @@ def load() -> C.CDLL:
         lib.bte_initialize_noalloc.argtypes = [vp, C.c_int, vp, vp]
     if hasattr(lib, "bte_radial_components"):
         lib.bte_radial_components.argtypes = [vp, C.c_int, vp, C.c_int, vp, vp, vp]
-    if hasattr(lib, "bte_solve_transient"):
-        lib.bte_solve_transient.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
-                                            C.POINTER(TransientOpts), vp]
+    lib.bte_solve_transient.argtypes = [vp, C.c_int] + [vp] * 11 + [C.POINTER(TransientOpts), vp]
     _lib = lib
     return lib
 

@@ -323,7 +323,48 @@ class bte_0d3v_batched:
         return ff, qoi
 
     def transient_solve(self, grid_idx, f0, atol, rtol, max_iter):
-        raise NotImplementedError("transient solves are not available in this build")
+        """solve(..., "transient") (bte_0d3v_batched.py:1063-1155): backward Euler over
+        args.cycles RF periods in steps of args.dt, the field eRe cos 2 pi t + eIm sin 2 pi t
+        when args.Efreq > 0. Returns (u, qoi): the final state (mass-normalized, as the
+        reference returns it) and the QoIs of the last completed cycle average
+        (effective_mobility False), plus per-point `status` and `iters`. A step that does not
+        converge raises, where the reference exits."""
+        torch = _torch()
+        on_host = not torch.is_tensor(f0)
+        n_pts = f0.shape[1]
+        prof = self.profile_tt_all[grid_idx]
+        torch.cuda.synchronize()
+        prof[pp.SOLVE].start()
+        f = self._dev(f0).t().contiguous()
+        n0, ne, Tg, E, ns = self._params(grid_idx, n_pts)
+        efreq = float(getattr(self._args, "Efreq", 0.0) or 0.0)
+        prm = self._par_bte_params[grid_idx]
+        if efreq > 0:
+            eRe, eIm = self._dev(prm["eRe"], (n_pts,)), self._dev(prm["eIm"], (n_pts,))
+        else:
+            eRe = eIm = None
+        f_avg = torch.empty_like(f)
+        status = torch.empty(n_pts, dtype=torch.int32, device="cuda")
+        iters = torch.empty(n_pts, dtype=torch.int32, device="cuda")
+        opts = _lib.TransientOpts(atol=float(atol), rtol=float(rtol), max_iter=int(max_iter),
+                                  ee=int(getattr(self._args, "ee_collisions", 0)), precision=self._precision(),
+                                  dt=float(self._args.dt), cycles=float(self._args.cycles), efreq=efreq)
+        stream = torch.cuda.current_stream().cuda_stream
+        vp = lambda t: C.c_void_p(0) if t is None else _ptr(t)
+        _lib.check(_lib.load().bte_solve_transient(self._grid[grid_idx], n_pts, _ptr(n0), _ptr(ne), _ptr(ns), _ptr(Tg),
+                                                   _ptr(E), vp(eRe), vp(eIm), _ptr(f), _ptr(f_avg), _ptr(status),
+                                                   _ptr(iters), C.byref(opts), C.c_void_p(stream)),
+                   "bte_solve_transient")
+        qoi = self._qoi_dev(grid_idx, f_avg, n0, E, effective_mobility=False)
+        qoi["status"] = status
+        qoi["iters"] = iters
+        u = f.t()
+        torch.cuda.synchronize()
+        prof[pp.SOLVE].stop()
+        if on_host:
+            u = u.cpu().numpy()
+            qoi = {k: v.cpu().numpy() for k, v in qoi.items()}
+        return u, qoi
 
     # ------------------------------------------------------------------ QoIs
     def _qoi_dev(self, grid_idx, f_pm, n0, E, effective_mobility=True):

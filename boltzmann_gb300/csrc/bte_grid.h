@@ -104,6 +104,9 @@ size_t bte_engine_bytes(const BteEngine* e);
 int bte_engine_fp64_capacity(const BteEngine* e);
 int bte_engine_capacity(const BteEngine* e);
 BteGrid* bte_engine_grid(const BteEngine* e);
+int bte_transient_impl(BteGrid* g, int P, const double* n0, const double* ne, const double* ns_by_n0,
+                       const double* Tg, const double* E, const double* eRe, const double* eIm, double* f,
+                       double* f_avg, int32_t* status, int32_t* iters, const bte_transient_opts* o, cudaStream_t s);
 int bte_solve_impl(BteGrid* g, int P, const double* n0, const double* ne, const double* ns_by_n0,
                    const double* Tg, const double* E, double* f, int32_t* status, int32_t* iters,
                    const bte_solve_opts* opts, cudaStream_t s);

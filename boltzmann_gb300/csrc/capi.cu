@@ -554,6 +554,25 @@ int bte_engine_info(const bte_engine* e, int* ints4, size_t* bytes) {
     return BTE_OK;
 }
 
+int bte_solve_transient(bte_grid* g, int P, const double* n0, const double* ne, const double* ns_by_n0,
+                        const double* Tg, const double* E, const double* eRe, const double* eIm, double* f,
+                        double* f_avg, int32_t* status, int32_t* iters, const bte_transient_opts* opts, void* stream) {
+    if (!g || !opts || P < 0) return fail(BTE_ERR_ARG, "bad argument");
+    if (P == 0) return BTE_OK;
+    if (!n0 || !ne || !ns_by_n0 || !Tg || !E || !f || !status || !iters) return fail(BTE_ERR_ARG, "null buffer");
+    if (opts->efreq > 0 && (!eRe || !eIm)) return fail(BTE_ERR_ARG, "eRe and eIm are needed with a field frequency");
+    if (opts->precision != BTE_PREC_FP64 && opts->precision != BTE_PREC_MIXED) return fail(BTE_ERR_ARG, "bad precision");
+    if (!(opts->dt > 0) || !(opts->cycles >= 0) || opts->max_iter < 1 || opts->efreq < 0)
+        return fail(BTE_ERR_ARG, "bad transient options");
+    if (opts->ee && !g->ee) return fail(BTE_ERR_STATE, "e-e requested but the grid was built without Coulomb operators");
+    cudaSetDevice(g->device);
+    int rc = bte_transient_impl(g, P, n0, ne, ns_by_n0, Tg, E, eRe, eIm, f, f_avg, status, iters, opts,
+                                (cudaStream_t)stream);
+    if (rc == BTE_ERR_STATE) return fail(rc, "a transient step did not converge within max_iter chord iterations");
+    if (rc != BTE_OK) return fail(rc, std::string("transient solve failed: ") + cudaGetErrorString(cudaGetLastError()));
+    return BTE_OK;
+}
+
 int bte_solve_steady(bte_grid* g, int P, const double* n0, const double* ne, const double* ns_by_n0, const double* Tg,
                      const double* E, double* f, int32_t* status, int32_t* iters, const bte_solve_opts* opts,
                      void* stream) {

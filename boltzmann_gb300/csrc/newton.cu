@@ -446,7 +446,9 @@ __global__ void k_refine_check(int nact, const int* __restrict__ act, const doub
 }
 
 // ---------------------------------------------------------------------------------
-// Bordered Jacobian, one warp per row, lanes along columns (row-major output):
+// Bordered Jacobian, one warp per row, lanes along columns (row-major output), with the
+// F_raw block scaled by jscale and jshift * M added (steady solve: 1, 0; transient backward
+// Euler: -dt tau, 1):
 //   J[a][j] = static(a, j) - mu M[a][j] - (M h)[a] w[j]
 //             + ne gamma (K1[a][j] + (K2a HL)[a][j] + (K2b GL)[a][j]) + ne U[a] dgamma[j]
 //   J[a][n] = -beta Mp[a] / Mpmax,   J[n][j] = beta u[j] / umax,   J[n][n] = 0
@@ -502,7 +504,7 @@ __global__ void __launch_bounds__(JAC_WARPS * 32)
 k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int nact, const double* __restrict__ h,
            const double* __restrict__ F, const double* __restrict__ aux, const double* __restrict__ scal,
            T* __restrict__ J, int ld, long long stride, double beta_scale, double* __restrict__ rowscale,
-           int stage_hl) {
+           int stage_hl, double jscale, double jshift) {
     extern __shared__ __align__(16) unsigned char jsm[];
     const int slot = blockIdx.y;
     if (slot >= nact) return;
@@ -535,7 +537,9 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
     const double* ax = aux + (size_t)pt * 4 * n;
     const double* sc = scal + (size_t)pt * SC_COUNT;
     const double n0 = pp.n0[pt], Tg = pp.Tg[pt], E = pp.E[pt];
-    const double beta = beta_scale * n0;
+    // border scale: per unit n0 for the steady Jacobian (it matches the collision operator);
+    // absolute for the backward-Euler matrix (it matches the mass matrix)
+    const double beta = (jshift != 0.0) ? beta_scale : beta_scale * n0;
     if (a == n) {  // constraint row
         double uh = 0.0;
         for (int j = lane; j < n; j += 32) {
@@ -619,7 +623,7 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
                 v += -mh_t * wj;
                 if (ee) v += dgt_t * (T)g.temp[j] - dgm_t * (T)g.mass[j];
             }
-            Jr[j] = v;
+            Jr[j] = v * (T)jscale;
             continue;
         }
         // l = 0 block and band: every term summed in FP64 and rounded once (the l = 0 rows
@@ -659,6 +663,8 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
                 v += negam * k1;
             }
         }
+        v *= jscale;
+        if (band && s == q) v += jshift * g.Mr[p * BTE_NB + dk + BTE_BAND];
         Jr[j] = (T)v;
     }
     __syncwarp();
@@ -1126,7 +1132,7 @@ static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
             CKR(pf.run(PF_JACOBIAN, s, nact * jac_flops_pt(g, ee), jb, 1, [&] {
                 k_jacobian<float><<<gj, JAC_WARPS * 32, jac_smem<float>(g, ee), s>>>(gv, pp, ee, L.act, nact, w->h, w->F, w->aux, w->scal,
                                                                   (float*)L.J, ld, jstride, beta_scale, L.rowscale,
-                                                                  jac_smem<float>(g, ee) > 0);
+                                                                  jac_smem<float>(g, ee) > 0, 1.0, 0.0);
             }));
             CKR(pf.run(PF_LU, s, nact * lu_flops(N), lub, 1, [&] {
                 le = bte_lu_factor_t<float>(nact, N, N + 1, (float*)L.J, ld, jstride, L.piv, L.info, s, 0);
@@ -1164,7 +1170,7 @@ static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
             CKR(pf.run(PF_JACOBIAN, s, nact * jac_flops_pt(g, ee), jb, 1, [&] {
                 k_jacobian<double><<<gj, JAC_WARPS * 32, jac_smem<double>(g, ee), s>>>(gv, pp, ee, L.act, nact, w->h, w->F, w->aux, w->scal,
                                                                    (double*)L.J, ld, jstride, beta_scale, L.rowscale,
-                                                                  jac_smem<double>(g, ee) > 0);
+                                                                  jac_smem<double>(g, ee) > 0, 1.0, 0.0);
             }));
             CKR(pf.run(PF_LU, s, nact * lu_flops(N), lub, 1, [&] {
                 le = bte_lu_factor_t<double>(nact, N, N + 1, (double*)L.J, ld, jstride, L.piv, L.info, s, 0);
@@ -1663,4 +1669,278 @@ int bte_engine_collect_impl(BteEngine* e, int m, const int32_t* slots, double* f
     CKR(cudaStreamSynchronize(s));
     for (int i = 0; i < m; ++i) e->free_slots.push_back(slots[i]);
     return BTE_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// Transient solve (solve(..., "transient"), bte_0d3v_batched.py:1063-1155, with
+// newton_solver_batched, :59-126): backward Euler, t in RF periods, tau = 1 / efreq
+// (1e-7 without a field frequency). Each step solves, for the increment delta with
+// u . delta = 0 (the reference's du in the mass-conserving coordinates Q du),
+//     M delta - dt tau F_raw(h + delta) - lambda M p = 0,
+// by a chord iteration: the bordered Jacobian M - dt tau dF_raw/dh is built and factored once
+// per step at the step's start state, as the reference inverts its Jacobian once per step,
+// and reused for every iteration (no line search). A point's step ends when
+// ||(I - p p^T) M^-1 G|| <= atol or <= rtol times its first value; the previous step's
+// increment starts the next step's iteration, as in the reference. The cycle average of
+// the state (trapezoid over each RF period) is kept for the QoIs.
+// ---------------------------------------------------------------------------------
+__global__ void k_add_iter(int P, const int* __restrict__ done, int* iters) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < P && !done[i]) iters[i] += 1;
+}
+
+__global__ void k_set_efield(int P, const double* __restrict__ eRe, const double* __restrict__ eIm, double t,
+                             const double* __restrict__ E0, int harmonic, double* E) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    E[i] = harmonic ? eRe[i] * cos(2.0 * BTE_PI * t) + eIm[i] * sin(2.0 * BTE_PI * t) : E0[i];
+}
+
+// G = M delta - c F  (M: the banded radial mass matrix, identical per harmonic)
+__global__ void k_transient_G(GridView g, int nact, const int* __restrict__ act, const double* __restrict__ dh,
+                              int ldd, const double* __restrict__ F, double c, double* G) {
+    const int slot = blockIdx.x;
+    if (slot >= nact) return;
+    const int pt = act[slot];
+    const int n = g.n, nsh = g.nsh, nsp = g.nsp;
+    const double* d = dh + (size_t)pt * ldd;
+    for (int a = threadIdx.x; a < n; a += blockDim.x) {
+        const int p = a / nsh, q = a % nsh;
+        double m = 0.0;
+        for (int dk = -BTE_BAND; dk <= BTE_BAND; ++dk) {
+            const int k = p + dk;
+            if (k >= 0 && k < nsp) m += g.Mr[p * BTE_NB + dk + BTE_BAND] * d[k * nsh + q];
+        }
+        G[(size_t)pt * n + a] = m - c * F[(size_t)pt * n + a];
+    }
+}
+
+// points whose step converged leave the list; the others go on
+__global__ void k_transient_conv(int nact, const int* __restrict__ act, const double* __restrict__ r,
+                                 const double* __restrict__ r0, double atol, double rtol, int* done, int* act_out,
+                                 int* nout) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nact) return;
+    const int pt = act[i];
+    const double rr = r[pt];
+    if (rr <= atol || rr <= rtol * r0[pt]) { done[pt] = 1; return; }
+    act_out[atomicAdd(nout, 1)] = pt;
+}
+
+// right-hand side of the chord step for every point (zero for points already done), row-scaled
+// as the factored Jacobian: [-G; -beta u . delta]
+template <typename T>
+__global__ void k_transient_rhs(int P, int n, const double* __restrict__ G, const double* __restrict__ u,
+                                const double* __restrict__ dh, int ldd, double beta, const double* __restrict__ rowscale,
+                                const int* __restrict__ done, T* xs) {
+    __shared__ double red[32];
+    const int pt = blockIdx.x;
+    if (pt >= P) return;
+    const int N = n + 1;
+    T* x = xs + (size_t)pt * N;
+    if (done[pt]) {
+        for (int a = threadIdx.x; a < N; a += blockDim.x) x[a] = T(0);
+        return;
+    }
+    const double* d = dh + (size_t)pt * ldd;
+    const double* rs = rowscale + (size_t)pt * N;
+    double ud = 0.0;
+    for (int a = threadIdx.x; a < n; a += blockDim.x) {
+        x[a] = (T)(-G[(size_t)pt * n + a] * rs[a]);
+        ud += u[a] * d[a];
+    }
+    ud = block_sum(ud, red);
+    if (threadIdx.x == 0) x[n] = (T)(-beta * ud * rs[n]);
+}
+
+template <typename T>
+__global__ void k_transient_update(int P, int n, const int* __restrict__ done, const T* __restrict__ xs, double* dh,
+                                   int ldd) {
+    const int pt = blockIdx.x;
+    if (pt >= P || done[pt]) return;
+    for (int a = threadIdx.x; a < n; a += blockDim.x) dh[(size_t)pt * ldd + a] += (double)xs[(size_t)pt * (n + 1) + a];
+}
+
+// avg += h (the trapezoid sums of the cycle average)
+__global__ void k_accumulate(size_t m, const double* __restrict__ h, double* avg) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m) avg[i] += h[i];
+}
+// h += delta (state update)
+__global__ void k_apply_increment(int P, int n, const double* __restrict__ dh, int ldd, double* h) {
+    const int pt = blockIdx.x;
+    if (pt >= P) return;
+    for (int a = threadIdx.x; a < n; a += blockDim.x) h[(size_t)pt * n + a] += dh[(size_t)pt * ldd + a];
+}
+__global__ void k_scale_into(size_t m, double c, double* a, double* b) {  // b = c a, a = 0
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m) { b[i] = c * a[i]; a[i] = 0.0; }
+}
+
+int bte_transient_impl(BteGrid* g, int P, const double* n0, const double* ne, const double* ns_by_n0,
+                       const double* Tg, const double* E, const double* eRe, const double* eIm, double* f,
+                       double* f_avg, int32_t* status, int32_t* iters, const bte_transient_opts* o, cudaStream_t s) {
+    if (P <= 0) return BTE_OK;
+    BteWork* w = bte_work_get(g);
+    const int prec = o->precision;
+    int rc = ensure_work(w, g, P, prec);
+    if (rc) return rc;
+    const int n = g->n, N = n + 1;
+    double *Et = nullptr, *avg = nullptr, *avgv = nullptr, *G = nullptr;
+    int32_t* all = nullptr;
+    CKR(cudaMallocAsync((void**)&all, (size_t)P * sizeof(int32_t), s));
+    CKR(cudaMallocAsync((void**)&Et, (size_t)P * sizeof(double), s));
+    CKR(cudaMallocAsync((void**)&avg, (size_t)P * n * sizeof(double), s));
+    CKR(cudaMallocAsync((void**)&avgv, (size_t)P * n * sizeof(double), s));
+    CKR(cudaMallocAsync((void**)&G, (size_t)P * n * sizeof(double), s));
+    bte_solve_opts so{};
+    so.atol = o->atol; so.rtol = o->rtol; so.max_iter = o->max_iter; so.ee = o->ee; so.precision = prec;
+    SolveCtx c{};
+    c.g = g; c.w = w; c.gv = view_of(g); c.pp = PointParams{n0, ne, Tg, Et, ns_by_n0, P, nullptr};
+    c.P = P; c.n = n; c.N = N; c.ld = (N + 1 + 3) & ~3; c.ldd = N + 1;
+    c.ee = (o->ee && g->ee) ? 1 : 0;
+    c.jstride = (long long)N * c.ld;
+    c.beta_scale = g->q0max / (g->umax > 0 ? g->umax : 1.0);
+    c.res_smem = (size_t)5 * n * sizeof(double);
+    c.o = &so; c.status = status; c.iters = iters; c.s = s;
+    if (c.res_smem > 48 * 1024) CKR(cudaFuncSetAttribute(k_residual, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.res_smem));
+    const size_t rm_smem = (size_t)2 * n * sizeof(double);
+    if (rm_smem > 48 * 1024) CKR(cudaFuncSetAttribute(k_ref_merit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rm_smem));
+    Profiler& pf = g_prof;
+    auto other = [&](auto&& fn) { return pf.run(PF_OTHER, s, 0, 0, 1, fn); };
+    const int harmonic = o->efreq > 0 ? 1 : 0;
+    const double tau = harmonic ? 1.0 / o->efreq : 1e-7;
+    const double cdt = o->dt * tau;
+    const int steps_total = (int)(o->cycles / o->dt);
+    const int io_freq = std::max(1, (int)(1.0 / o->dt));
+    const int ld = c.ld, ldd = c.ldd;
+    const long long js = c.jstride;
+    // border scale of the backward-Euler matrix: the mass matrix's magnitude over u's
+    std::vector<double> mr((size_t)g->nsp * BTE_NB);
+    CKR(cudaMemcpy(mr.data(), g->d_Mr, mr.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    double mmax = 0.0;
+    for (double v : mr) mmax = std::max(mmax, std::fabs(v));
+    const double beta = mmax / (g->umax > 0 ? g->umax : 1.0);
+    // state h = f / (u . f), increment 0, cycle sums 0
+    CKR(other([&] { k_mass_normalize<<<P, 256, 0, s>>>(n, g->d_u, f, w->h, P); }));
+    CKR(cudaMemsetAsync(w->dh, 0, (size_t)P * ldd * sizeof(double), s));
+    CKR(cudaMemsetAsync(avg, 0, (size_t)P * n * sizeof(double), s));
+    CKR(cudaMemsetAsync(avgv, 0, (size_t)P * n * sizeof(double), s));
+    CKR(other([&] { k_fill_int<<<nblk(P, 256), 256, 0, s>>>(status, 0, P); }));
+    CKR(other([&] { k_fill_int<<<nblk(P, 256), 256, 0, s>>>(iters, 0, P); }));
+    CKR(other([&] { k_fill_dbl<<<nblk(P, 256), 256, 0, s>>>(w->alpha, 1.0, P); }));
+    CKR(other([&] { k_iota<<<nblk(P, 256), 256, 0, s>>>(all, P); }));
+    double t = 0.0;
+    int failed = 0;
+    for (int ts = 0; ts <= steps_total; ++ts) {
+        if (ts > 0 && ts % io_freq == 0 && ts == steps_total) {
+            // the reference computes this last step but stops before applying it
+            CKR(other([&] { k_scale_into<<<nblk(P * n, 256), 256, 0, s>>>((size_t)P * n, 0.5 * o->dt, avg, avgv); }));
+            break;
+        }
+        CKR(other([&] { k_set_efield<<<nblk(P, 256), 256, 0, s>>>(P, eRe, eIm, t + o->dt, E, harmonic, Et); }));
+        // the step's Jacobian at the current state, factored once
+        CKR(pf.run(PF_RESIDUAL, s, 0, 0, 1, [&] {
+            k_residual<<<P, 256, c.res_smem, s>>>(c.gv, c.pp, c.ee, all, P, w->h, nullptr, 0, nullptr, nullptr, nullptr,
+                                                  w->F, w->aux, w->scal, w->r, nullptr);
+        }));
+        dim3 gj(nblk(N, JAC_WARPS), P);
+        cudaError_t le = cudaSuccess;
+        if (prec == BTE_PREC_MIXED) {
+            CKR(pf.run(PF_JACOBIAN, s, 0, 0, 1, [&] {
+                k_jacobian<float><<<gj, JAC_WARPS * 32, jac_smem<float>(g, c.ee), s>>>(
+                    c.gv, c.pp, c.ee, all, P, w->h, w->F, w->aux, w->scal, (float*)w->J, ld, js, beta, w->rowscale,
+                    jac_smem<float>(g, c.ee) > 0, -cdt, 1.0);
+            }));
+            CKR(pf.run(PF_LU, s, P * lu_flops(N), 0, 1, [&] {
+                le = bte_lu_factor_t<float>(P, N, N, (float*)w->J, ld, js, w->piv, w->info, s, 0);
+            }));
+        } else {
+            CKR(pf.run(PF_JACOBIAN, s, 0, 0, 1, [&] {
+                k_jacobian<double><<<gj, JAC_WARPS * 32, jac_smem<double>(g, c.ee), s>>>(
+                    c.gv, c.pp, c.ee, all, P, w->h, w->F, w->aux, w->scal, (double*)w->J, ld, js, beta, w->rowscale,
+                    jac_smem<double>(g, c.ee) > 0, -cdt, 1.0);
+            }));
+            CKR(pf.run(PF_LU, s, P * lu_flops(N), 0, 1, [&] {
+                le = bte_lu_factor_t<double>(P, N, N, (double*)w->J, ld, js, w->piv, w->info, s, 0);
+            }));
+        }
+        CKR(le);
+        // chord iterations
+        CKR(other([&] { k_fill_int<<<nblk(P, 256), 256, 0, s>>>(w->refdone, 0, P); }));
+        CKR(cudaMemcpyAsync(w->act, all, P * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+        int nact = P;
+        for (int it = 0;; ++it) {
+            CKR(pf.run(PF_RESIDUAL, s, 0, 0, 1, [&] {
+                k_residual<<<nact, 256, c.res_smem, s>>>(c.gv, c.pp, c.ee, w->act, nact, w->h, w->dh, ldd, w->alpha,
+                                                         nullptr, w->ht, w->Ft, w->auxt, w->scalt, w->rt, nullptr);
+            }));
+            CKR(other([&] {
+                k_transient_G<<<nact, 256, 0, s>>>(c.gv, nact, w->act, w->dh, ldd, w->Ft, cdt, G);
+                k_ref_merit<<<nact, 256, rm_smem, s>>>(c.gv, nact, w->act, G, w->rt);
+            }));
+            if (it == 0) CKR(other([&] { k_copy_list<<<nblk(nact, 256), 256, 0, s>>>(nact, w->act, w->rt, w->r0); }));
+            CKR(cudaMemsetAsync(w->cnt, 0, sizeof(int32_t), s));
+            CKR(other([&] {
+                k_transient_conv<<<nblk(nact, 256), 256, 0, s>>>(nact, w->act, w->rt, w->r0, o->atol, o->rtol,
+                                                                 w->refdone, w->act2, w->cnt);
+            }));
+            int hn = 0;
+            CKR(cudaMemcpyAsync(&hn, w->cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+            CKR(cudaStreamSynchronize(s));
+            pf.drain(s);
+            if (hn == 0) break;
+            if (it >= o->max_iter) { failed = 1; break; }
+            // the points still iterating take one chord step
+            if (prec == BTE_PREC_MIXED) {
+                CKR(other([&] {
+                    k_transient_rhs<float><<<P, 256, 0, s>>>(P, n, G, g->d_u, w->dh, ldd, beta, w->rowscale,
+                                                             w->refdone, reinterpret_cast<float*>(w->xs));
+                }));
+                CKR(pf.run(PF_LUSOLVE, s, 0, 0, 1, [&] {
+                    le = bte_lu_solve_t<float>(P, N, (const float*)w->J, ld, js, w->piv, reinterpret_cast<float*>(w->xs),
+                                               0, s);
+                }));
+                CKR(le);
+                CKR(other([&] {
+                    k_transient_update<float><<<P, 256, 0, s>>>(P, n, w->refdone, reinterpret_cast<float*>(w->xs), w->dh,
+                                                                ldd);
+                }));
+            } else {
+                CKR(other([&] {
+                    k_transient_rhs<double><<<P, 256, 0, s>>>(P, n, G, g->d_u, w->dh, ldd, beta, w->rowscale,
+                                                              w->refdone, w->xs);
+                }));
+                CKR(pf.run(PF_LUSOLVE, s, 0, 0, 1, [&] {
+                    le = bte_lu_solve_t<double>(P, N, (const double*)w->J, ld, js, w->piv, w->xs, 0, s);
+                }));
+                CKR(le);
+                CKR(other([&] { k_transient_update<double><<<P, 256, 0, s>>>(P, n, w->refdone, w->xs, w->dh, ldd); }));
+            }
+            CKR(other([&] { k_add_iter<<<nblk(P, 256), 256, 0, s>>>(P, w->refdone, iters); }));
+            std::swap(w->act, w->act2);
+            nact = hn;
+        }
+        if (failed) break;
+        if (ts > 0 && ts % io_freq == 0)
+            CKR(other([&] { k_scale_into<<<nblk(P * n, 256), 256, 0, s>>>((size_t)P * n, 0.5 * o->dt, avg, avgv); }));
+        CKR(other([&] { k_accumulate<<<nblk(P * n, 256), 256, 0, s>>>((size_t)P * n, w->h, avg); }));
+        CKR(other([&] { k_apply_increment<<<P, 256, 0, s>>>(P, n, w->dh, ldd, w->h); }));
+        CKR(other([&] { k_accumulate<<<nblk(P * n, 256), 256, 0, s>>>((size_t)P * n, w->h, avg); }));
+        t += o->dt;
+    }
+    if (failed) CKR(other([&] { k_fill_int<<<nblk(P, 256), 256, 0, s>>>(status, BTE_ST_MAXITER, P); }));
+    // outputs: the state, and the normalized distribution of the last completed cycle average
+    CKR(cudaMemcpyAsync(f, w->h, (size_t)P * n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    const double c_gamma = std::sqrt(2.0 * (BTE_QE / BTE_ME));
+    const double mm_fac = std::sqrt(1.0 / (4.0 * M_PI)) * 4.0 * M_PI;
+    const double sc3 = 2.0 * std::pow(g->vth / c_gamma, 3);
+    if (f_avg) CKR(other([&] { k_normalized_distribution<<<P, 256, 0, s>>>(n, g->d_mass, mm_fac, sc3, avgv, f_avg, P); }));
+    CKR(cudaFreeAsync(all, s));
+    CKR(cudaFreeAsync(Et, s));
+    CKR(cudaFreeAsync(avg, s));
+    CKR(cudaFreeAsync(avgv, s));
+    CKR(cudaFreeAsync(G, s));
+    CKR(cudaStreamSynchronize(s));
+    return failed ? BTE_ERR_STATE : BTE_OK;
 }

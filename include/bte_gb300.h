@@ -73,6 +73,18 @@ typedef struct {
     int reserved[5];
 } bte_solve_opts;
 
+/* Options of the transient solve (the reference's args.dt / cycles / Efreq). */
+typedef struct {
+    double atol, rtol;   /* per point: ||r|| <= atol or ||r|| <= rtol ||r_0|| ends a step's chord iteration */
+    int max_iter;        /* chord iterations per step */
+    int ee;              /* include e-e collisions (grid must have them) */
+    int precision;       /* BTE_PREC_FP64 or BTE_PREC_MIXED (FP32 factorization of the step Jacobian) */
+    double dt;           /* time step in RF periods */
+    double cycles;       /* simulated time in RF periods */
+    double efreq;        /* field frequency in Hz; 0: constant field E and tau = 1e-7 s */
+    int reserved[6];
+} bte_transient_opts;
+
 /* Build a grid and assemble every operator on the device (FP64).
  * Replaces bte_0d3v_batched.__init__ + assemble_operators
  * (BESolver/python/bte_0d3v_batched.py:138-306, 310-479). */
@@ -145,6 +157,20 @@ int bte_solve_steady(bte_grid* g, int P, const double* n0, const double* ne, con
 /* Per-point merit norms ||Q^T M^-1 F|| of the last bte_solve_steady on this grid (device
  * buffers [P]): at the returned state and at the initial state. Replaces the residual
  * printout of steady_state_solve (bte_0d3v_batched.py:960-963, 970-971). */
+/* Transient solve of P points: backward Euler over `cycles` RF periods in steps of dt
+ * (t in periods, tau = 1 / efreq), E(t) = eRe cos 2 pi t + eIm sin 2 pi t when efreq > 0,
+ * else the constant E; each step by a chord Newton iteration on the mass-conserving
+ * increment with the Jacobian frozen at the step's start. f [P x n] in: initial state;
+ * out: the final state (mass-normalized, as the reference returns u). f_avg [P x n] (may be
+ * NULL): normalized distribution of the last completed cycle average, for bte_qoi with
+ * effective_mobility = 0. status [P] 0, or BTE_ST_MAXITER if a step did not converge (the
+ * call then returns BTE_ERR_STATE); iters [P] total chord iterations.
+ * Replaces bte_0d3v_batched.solve(..., "transient") (bte_0d3v_batched.py:1063-1155) with
+ * newton_solver_batched (:59-126). */
+int bte_solve_transient(bte_grid* g, int P, const double* n0, const double* ne, const double* ns_by_n0,
+                        const double* Tg, const double* E, const double* eRe, const double* eIm, double* f,
+                        double* f_avg, int32_t* status, int32_t* iters, const bte_transient_opts* opts, void* stream);
+
 int bte_solve_info(bte_grid* g, int P, double* r_final, double* r_initial, void* stream);
 
 /* Quantities of interest of P normalized distributions (device f [P x n]); outputs

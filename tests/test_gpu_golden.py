@@ -50,3 +50,20 @@ def test_ee_against_reference(synthetic_xs, precision, tol):
     assert np.max(err) < tol, err
     for k in ("energy", "mobility", "diffusion"):
         assert relmax(q[k], g[k]) < tol
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_transient_matches_reference(synthetic_xs, precision):
+    """solve(..., "transient") on the GPU against the reference's own transient solve over one
+    RF period (golden vectors); both stop each step's chord iteration at rtol 1e-10."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "transient_reference.npz"))
+    s, args = gpu_solver(synthetic_xs, 32, 1, False, 2, precision=precision)
+    args.dt, args.cycles, args.Efreq = float(g["dt"]), float(g["cycles"]), float(g["Efreq"])
+    for k in ["n0", "ne", "ns_by_n0", "Tg", "E", "eRe", "eIm"]:
+        s.set_boltzmann_parameter(0, k, g[k])
+    u, qoi = s.solve(0, g["f0"], 1e-30, 1e-10, 200, "transient")
+    assert np.all(qoi["status"] == 0)
+    assert relmax(u, g["u"]) < 1e-8
+    for k in ("energy", "mobility", "diffusion"):
+        assert np.max(np.abs(qoi[k] - g[k]) / np.abs(g[k])) < 1e-8
