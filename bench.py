@@ -86,13 +86,8 @@ def barrier(ws):
 
 
 def max_over_ranks(x, ws):
-    if ws == 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from boltzmann_gb300.sharding import max_over_ranks as mor
+    return mor(x, ws)
 
 
 class Clocks:
