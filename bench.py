@@ -446,13 +446,14 @@ def roofline(st, peaks):
     bytes_pl = v["bytes"] / max(v["launches"], 1)
     flops_pl = v["flops"] / max(v["launches"], 1)
     achieved = bytes_pl / per_launch_s / 1e9
+    # DRAM traffic of one launch of the dominant family, from the ncu capture summarized in
+    # profiles/: its bytes per algorithmic byte, scaled to this run's average launch
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
-        try:
-            traffic = json.load(open(tpath)).get(dom)
-        except Exception:
-            traffic = None
+        rec = json.load(open(tpath)).get(dom)
+        if rec and rec.get("alg_bytes_per_launch"):
+            traffic = rec["dram_bytes_per_launch"] / rec["alg_bytes_per_launch"] * bytes_pl
     return {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm if hbm else None, "traffic": traffic,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if hbm else "fallback 6800 GB/s",
