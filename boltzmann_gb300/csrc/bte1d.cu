@@ -12,7 +12,8 @@
 // x-step (step_bte_x, bte_1d3v_solver.py:912-982, BE Chebyshev form): V' = Q^-1 V in the radial
 // index (adv_x = Q diag(d) Q^-1), inflow values zeroed (x = -1 for cos(theta) >= 0, x = +1
 // otherwise), one backward-Euler solve (I + h d_r cos(theta_j) D_L/R) per (r, j) over x, and
-// V = Q V'. The Nr * Nvt matrices are LU-factored once per step size.
+// V = Q V'. The Nr * Nvt matrices are inverted once per step size (LU factors, then one
+// identity column per pass), so each step is an HBM-bound batched product with the inverses.
 //
 // v-step (step_bte_v, bte_1d3v_solver.py:984-1137): U = P_o2sh V, then
 //   (I - dt (Cv + E_x Av)) U_new = U  at every x (Cv = tau n0 np0 (C_en + Tg C_gT), Av = tau A,
@@ -77,6 +78,36 @@ __global__ void k_build_xshift(int Nr, int Nvt, int Nx, double h, const double* 
         double v = (a == zrow) ? 0.0 : f * D[(size_t)a * Nx + b];
         if (a == b) v += 1.0;
         A[(size_t)m * stride + (size_t)a * ld + b] = v;
+    }
+}
+
+// right-hand sides e_c for every system (column c of the identity)
+__global__ void k_unit_rhs(int P, int Nx, int c, double* B) {
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)P * Nx) return;
+    B[e] = ((int)(e % Nx) == c) ? 1.0 : 0.0;
+}
+// column c of each inverse, stored as row c of its transpose: XT[m][c][:] = x_m
+__global__ void k_store_invcol(int P, int Nx, int c, const double* __restrict__ B, double* XT) {
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)P * Nx) return;
+    const size_t m = e / Nx, i = e % Nx;
+    XT[(m * Nx + c) * Nx + i] = B[e];
+}
+// out[m][i] = sum_k A^-1[m][i][k] in[m][k] with the transposed inverse XT[m][k][i]: one CTA
+// per system, threads along i (coalesced rows of XT), in[m][:] staged in shared memory
+__global__ void __launch_bounds__(256) k_xstep_apply(int Nx, const double* __restrict__ XT,
+                                                     const double* __restrict__ in, double* __restrict__ out) {
+    extern __shared__ double sv[];
+    const int m = blockIdx.x;
+    const double* A = XT + (size_t)m * Nx * Nx;
+    for (int k = threadIdx.x; k < Nx; k += blockDim.x) sv[k] = in[(size_t)m * Nx + k];
+    __syncthreads();
+    for (int i = threadIdx.x; i < Nx; i += blockDim.x) {
+        double acc = 0.0;
+#pragma unroll 4
+        for (int k = 0; k < Nx; ++k) acc += A[(size_t)k * Nx + i] * sv[k];
+        out[(size_t)m * Nx + i] = acc;
     }
 }
 
@@ -222,6 +253,7 @@ struct Bte1d {
     // x-step factors
     double hx = -1.0;
     double* XA = nullptr;
+    double* XI = nullptr;  // transposed inverses of the x-step matrices, Nr * Nvt x Nx x Nx
     int32_t *Xpiv = nullptr, *Xinfo = nullptr;
     int xld = 0;
     // v-step buffers
@@ -234,6 +266,7 @@ struct Bte1d {
     int kcap = 0;
     double *part = nullptr, *hd = nullptr;
     double* Vt = nullptr;  // ordinates scratch
+    double* Vt2 = nullptr;
     std::vector<void*> allocs;
     long long launches = 0;
 };
@@ -284,6 +317,7 @@ int bte1d_create(int device, int Nr, int nsh, int Nvt, int Nx, const double* Q, 
     A((void**)&h->Ps, (size_t)nsh * Nvt * 8); A((void**)&h->Po, (size_t)Nvt * nsh * 8);
     A((void**)&h->CvT, (size_t)n * n * 8); A((void**)&h->AvT, (size_t)n * n * 8);
     A((void**)&h->XA, (size_t)Nr * Nvt * Nx * h->xld * 8);
+    A((void**)&h->XI, (size_t)Nr * Nvt * Nx * Nx * 8);
     A((void**)&h->Xpiv, (size_t)Nr * Nvt * Nx * 4); A((void**)&h->Xinfo, (size_t)Nr * Nvt * 4);
     A((void**)&h->VB, (size_t)Nx * n * h->vld * 4);
     A((void**)&h->Vpiv, (size_t)Nx * n * 4); A((void**)&h->Vinfo, (size_t)Nx * 4);
@@ -292,6 +326,7 @@ int bte1d_create(int device, int Nr, int nsh, int Nvt, int Nx, const double* Q, 
     A((void**)&h->Kr, (size_t)(restart + 1) * nu * 8);
     A((void**)&h->part, (size_t)(restart + 1) * RED_BLOCKS * 8); A((void**)&h->hd, (size_t)(restart + 1) * 8);
     A((void**)&h->Vt, nv * 8);
+    A((void**)&h->Vt2, nv * 8);
     if (rc != BTE_OK) { free1d(h); delete h; return rc; }
     // transposed v-space operators; inflow side of each ordinate
     std::vector<double> CvT((size_t)n * n), AvT((size_t)n * n);
@@ -341,16 +376,25 @@ int bte1d_step_x(Bte1d* h, double hstep, double* V, void* stream) {
         CK1(cudaStreamSynchronize(s));
         for (int v : info)
             if (v != 0) { g_err1d = "x-advection matrix is singular"; return BTE_ERR_STATE; }
+        // explicit inverses, one identity column per pass (as the reference applies them,
+        // :780-887): each step then streams them once, an HBM-bound batched product
+        const int P = Nr * Nvt;
+        for (int c = 0; c < Nx; ++c) {
+            k_unit_rhs<<<nb((size_t)P * Nx, 256), 256, 0, s>>>(P, Nx, c, h->Vt);
+            CK1(bte_lu_solve_t<double>(P, Nx, h->XA, h->xld, xs, h->Xpiv, h->Vt, 0, s));
+            k_store_invcol<<<nb((size_t)P * Nx, 256), 256, 0, s>>>(P, Nx, c, h->Vt, h->XI);
+        }
+        CK1(cudaGetLastError());
         h->hx = hstep;
-        h->launches += 2;
+        h->launches += 2 + 3 * (long long)Nx;
     }
     const size_t smem = (size_t)Nr * Nr * 8;
     if (smem > 48 * 1024) CK1(cudaFuncSetAttribute(k_radial_mix, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_radial_mix<<<dim3(nb(C, 128), Nr), 128, smem, s>>>(Nr, C, h->Qinv, V, h->Vt);
     k_zero_inflow<<<nb((size_t)Nr * Nvt, 256), 256, 0, s>>>(Nr, Nvt, Nx, h->right, h->Vt);
     CK1(cudaGetLastError());
-    CK1(bte_lu_solve_t<double>(Nr * Nvt, Nx, h->XA, h->xld, xs, h->Xpiv, h->Vt, 0, s));
-    k_radial_mix<<<dim3(nb(C, 128), Nr), 128, smem, s>>>(Nr, C, h->Q, h->Vt, V);
+    k_xstep_apply<<<Nr * Nvt, 256, (size_t)Nx * 8, s>>>(Nx, h->XI, h->Vt, h->Vt2);
+    k_radial_mix<<<dim3(nb(C, 128), Nr), 128, smem, s>>>(Nr, C, h->Q, h->Vt2, V);
     CK1(cudaGetLastError());
     h->launches += 4;
     return BTE_OK;

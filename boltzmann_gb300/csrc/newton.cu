@@ -445,6 +445,18 @@ __global__ void k_refine_check(int nact, const int* __restrict__ act, const doub
     if (last) done[pt] = 1;
 }
 
+// After the first refinement pass: a correction below first_tol of the step means the FP32
+// step was already accurate to ~first_tol (the corrected step to ~first_tol^2), so the
+// refinement of this point ends; a point whose FP32 factors could not resolve its Jacobian
+// shows a correction near 1, never this small.
+__global__ void k_refine_first(int nact, const int* __restrict__ act, const double* __restrict__ c_cur, int* done,
+                               double first_tol) {
+    int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= nact) return;
+    int pt = act[slot];
+    if (!done[pt] && c_cur[pt] <= first_tol) done[pt] = 1;
+}
+
 // ---------------------------------------------------------------------------------
 // Bordered Jacobian, one warp per row, lanes along columns (row-major output), with the
 // F_raw block scaled by jscale and jshift * M added (steady solve: 1, 0; transient backward
@@ -623,7 +635,7 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
                 v += -mh_t * wj;
                 if (ee) v += dgt_t * (T)g.temp[j] - dgm_t * (T)g.mass[j];
             }
-            Jr[j] = v * (T)jscale;
+            Jr[j] = (jshift != 0.0) ? v * (T)jscale : v;
             continue;
         }
         // l = 0 block and band: every term summed in FP64 and rounded once (the l = 0 rows
@@ -663,8 +675,10 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
                 v += negam * k1;
             }
         }
-        v *= jscale;
-        if (band && s == q) v += jshift * g.Mr[p * BTE_NB + dk + BTE_BAND];
+        if (jshift != 0.0) {  // backward-Euler form only: the steady kernel spends no FP64 op here
+            v *= jscale;
+            if (band && s == q) v += jshift * g.Mr[p * BTE_NB + dk + BTE_BAND];
+        }
         Jr[j] = (T)v;
     }
     __syncwarp();
@@ -1159,6 +1173,8 @@ static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
                                                          w->refdone);
                 }));
                 CKR(le);
+                if (rf == 0)
+                    CKR(other([&] { k_refine_first<<<nblk(nact, 256), 256, 0, s>>>(nact, L.act, ccur, w->refdone, 1e-5); }));
                 if (rf >= 1)
                     CKR(other([&] {
                         k_refine_check<<<nblk(nact, 256), 256, 0, s>>>(nact, L.act, cprev, ccur, status, w->refdone,
@@ -1782,7 +1798,10 @@ int bte_transient_impl(BteGrid* g, int P, const double* n0, const double* ne, co
                        double* f_avg, int32_t* status, int32_t* iters, const bte_transient_opts* o, cudaStream_t s) {
     if (P <= 0) return BTE_OK;
     BteWork* w = bte_work_get(g);
-    const int prec = o->precision;
+    // the step Jacobian M - dt tau dF/dh carries the B-spline mass matrix's conditioning
+    // (1e5 and more at the configs' grids) on top of the step's own; FP32 factors do not
+    // resolve it, so both forms factor it in FP64
+    const int prec = BTE_PREC_FP64;
     int rc = ensure_work(w, g, P, prec);
     if (rc) return rc;
     const int n = g->n, N = n + 1;

@@ -78,7 +78,9 @@ typedef struct {
     double atol, rtol;   /* per point: ||r|| <= atol or ||r|| <= rtol ||r_0|| ends a step's chord iteration */
     int max_iter;        /* chord iterations per step */
     int ee;              /* include e-e collisions (grid must have them) */
-    int precision;       /* BTE_PREC_FP64 or BTE_PREC_MIXED (FP32 factorization of the step Jacobian) */
+    int precision;       /* BTE_PREC_FP64 or BTE_PREC_MIXED; the step Jacobian M - dt tau dF/dh is
+                            factored in FP64 in both (it carries the mass matrix's conditioning,
+                            beyond FP32 factors) */
     double dt;           /* time step in RF periods */
     double cycles;       /* simulated time in RF periods */
     double efreq;        /* field frequency in Hz; 0: constant field E and tau = 1e-7 s */
