@@ -496,6 +496,7 @@ struct OpsT<float> {
 };
 
 constexpr int JAC_WARPS = 8;
+constexpr int MIXED_HANDOVER_ITER = 30;  // mixed-form iterations before a running point moves to FP64
 
 // Row equilibration of one bordered row (matrix part [0, N) and the RHS column N): the
 // row is divided by its largest |entry| so that the factorization sees rows of unit
@@ -792,9 +793,13 @@ __global__ void k_accept(int n, int nact, const int* __restrict__ act, const int
 }
 
 // convergence test and compaction of the active list
+// handover_iter > 0 (the mixed form): a point still running after that many iterations is
+// handed to the FP64 form with the rest of its budget, so one slow point does not hold a
+// whole batch in the mixed form until max_iter
 __global__ void k_converge(int nact, const int* __restrict__ act, const double* __restrict__ r,
                            const double* __restrict__ r0, double atol, double rtol, int* nit, int max_iter,
-                           int* status, int* act_out, int* nout, const int32_t* __restrict__ info, int check_info) {
+                           int handover_iter, int* status, int* act_out, int* nout,
+                           const int32_t* __restrict__ info, int check_info) {
     int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= nact) return;
     int pt = act[slot];
@@ -805,6 +810,7 @@ __global__ void k_converge(int nact, const int* __restrict__ act, const double* 
         else if (r[pt] <= atol + rtol * r0[pt]) st = BTE_ST_CONVERGED;
         else if (check_info && info[slot] != 0) st = BTE_ST_SINGULAR;
         else if (it >= max_iter) st = BTE_ST_MAXITER;
+        else if (handover_iter > 0 && it >= handover_iter) st = BTE_ST_NEED_FP64;
         status[pt] = st;
     }
     if (st < 0) {
@@ -1227,7 +1233,9 @@ static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
         CKR(cudaMemsetAsync(w->cnt, 0, sizeof(int32_t), s));
         CKR(other([&] {
             k_converge<<<nblk(nact, 256), 256, 0, s>>>(nact, L.act, w->r, w->r0, o->atol, o->rtol,
-                                                      w->nit, o->max_iter, status, L.act2, w->cnt, L.info, 0);
+                                                      w->nit, o->max_iter,
+                                                      prec == BTE_PREC_MIXED ? MIXED_HANDOVER_ITER : 0, status, L.act2,
+                                                      w->cnt, L.info, 0);
         }));
         int hn = 0;
         CKR(cudaMemcpyAsync(&hn, w->cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
