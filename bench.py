@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--serve-budget-gb", type=float, default=16.0, help="HBM budget of admitted points")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-1d", action="store_true", help="skip the 1D3V (config 4) leg")
+    ap.add_argument("--c5-points", type=int, default=256, help="points of the config-5 sample (0: skip)")
+    ap.add_argument("--c5-plain-points", type=int, default=32)
     ap.add_argument("--steps-1d", type=int, default=20)
     return ap.parse_args()
 
@@ -340,6 +342,66 @@ def serve_bench(a):
     }
 
 
+def bench_c5(a):
+    """Config 5 (256 B-splines x l_max 4: n = 1280, 1281 x 1281 bordered systems, e-e on, ionization
+    degree 1e-6..1e-2, seed 20261205) on a sample of its 16384 points: one full EDF solve of
+    the sample in the mixed form, timed after one warm-up, and the plain FP64 form on the first
+    points for the error."""
+    import torch
+    from boltzmann_gb300.workloads import write_synthetic_lxcat, config_parameters, CONFIGS
+    c = CONFIGS["c5"]
+    xs = write_synthetic_lxcat()
+    try:
+        ns = types.SimpleNamespace(n_sp=c["n_sp"], l_max=c["l_max"], n_pts=a.c5_points)
+        prm = config_parameters("c5", c["n_pts"])
+        sub = {k: (v[..., :a.c5_points] if isinstance(v, np.ndarray) else v) for k, v in prm.items()}
+        s, args, t_setup = make_solver(xs, ns, "mixed", 0)
+        for k in ["n0", "ne", "ns_by_n0", "Tg", "E"]:
+            s.set_boltzmann_parameter(0, k, sub[k])
+        f0 = torch.as_tensor(s.initialize(0, a.c5_points), device="cuda")
+        full_solve(s, args, f0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        ff, q = full_solve(s, args, f0)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        ffm = ff.cpu().numpy()
+        stm = q["status"].cpu().numpy()
+        del s
+        torch.cuda.empty_cache()
+        m = a.c5_plain_points
+        ns.n_pts = m
+        sp, argsp, _ = make_solver(xs, ns, "fp64", 0)
+        for k in ["n0", "ne", "ns_by_n0", "Tg", "E"]:
+            sp.set_boltzmann_parameter(0, k, sub[k][..., :m])
+        f0p = torch.as_tensor(sp.initialize(0, m), device="cuda")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ffp, qp = full_solve(sp, argsp, f0p)
+        torch.cuda.synchronize()
+        pms = (time.perf_counter() - t0) * 1e3
+        ffp = ffp.cpu().numpy()
+        stp = qp["status"].cpu().numpy()
+        ok = (stm[:m] <= 1) & (stp <= 1)
+        err = (np.linalg.norm(ffm[:, :m] - ffp, axis=0) / np.linalg.norm(ffp, axis=0))[ok]
+        del sp
+        torch.cuda.empty_cache()
+    finally:
+        os.unlink(xs)
+    return {"workload": "config 5 sample: first %d of its 16384 points (256 B-splines x l_max 4, n = 1280, e-e on, "
+                        "ionization degree 1e-6..1e-2, seed 20261205)" % a.c5_points,
+            "value": a.c5_points / (ms / 1e3), "unit": "solves/s", "ms_per_step": ms, "setup_s": t_setup,
+            "status_counts": {str(k): int(v) for k, v in zip(*np.unique(stm, return_counts=True))},
+            "newton_iters": {"mean": float(np.mean(q["iters"].cpu().numpy())),
+                             "max": int(np.max(q["iters"].cpu().numpy()))},
+            "plain_fp64": {"points": m, "value": m / (pms / 1e3), "ms_per_step": pms,
+                           "edf_rel_err_mixed_vs_fp64": {"max": float(err.max()) if err.size else None,
+                                                         "p50": float(np.median(err)) if err.size else None,
+                                                         "points_compared": int(err.size)}}}
+
+
 C4 = dict(L=2.54e-2, V0=100.0, freq=13.56e6, Tg=300.0, p0=1.0, atol=1e-14, rtol=1e-10, gmres_rsrt=30,
           gmres_rsrt_iter=20, max_iter=300, Np=200, Nr=63, Nvt=16, lmax=1, dt=1e-3, ev_max=80.0, ev_extend=0,
           sp_order=3, spline_qpts=5, Te=4.0, xspace_type=1, vspace_type=1)
@@ -521,6 +583,7 @@ def main():
         return
     serve = None if (a.no_serve or ws > 1) else serve_bench(a)
     one_d = None if (a.no_1d or ws > 1) else bench_1d(a, peaks)
+    c5 = None if (a.c5_points <= 0 or ws > 1) else bench_c5(a)
     cpu = None if a.no_cpu else cpu_sample(a, a.cpu_points, 3)
     st = r["stats"]
     steps_ms = sorted(r["steps_ms"])
@@ -535,7 +598,7 @@ def main():
         "fp64_fallback_points_per_step": st["fp64_fallback_points"] / a.steps,
         "fp64_fallback_reasons": st["fp64_fallback_reasons"],
         "roofline": roofline(st, peaks), "cpu_baseline": cpu, "clocks": r["clocks"],
-        "plain_fp64": r["plain"], "serving": serve, "bte_1d3v": one_d, "setup_s": r["setup_s"],
+        "plain_fp64": r["plain"], "serving": serve, "bte_1d3v": one_d, "c5_sample": c5, "setup_s": r["setup_s"],
         "newton_iters": {"mean": float(np.mean(r["iters"])), "max": int(np.max(r["iters"]))},
         "status_counts": {str(k): int(v) for k, v in zip(*np.unique(r["status"], return_counts=True))},
     }
