@@ -512,6 +512,21 @@ __device__ inline void equilibrate_row(T* Jr, int N, int lane, double* scale_out
     if (lane == 0 && scale_out) *scale_out = (double)sc;
 }
 
+// Byte offset of the staged HL / GL rows in k_jacobian's dynamic shared memory: before them
+// sit the per-point column vectors of the l = 0 columns (FP64 W sums, their T copy, T copies
+// of the temperature and mass rows) and the per-species scalars n0 * ns.
+template <typename T>
+__host__ __device__ inline size_t jac_col_bytes(int nsp, int nspecies) {
+    return (((size_t)nsp + nspecies) * sizeof(double) + (size_t)3 * nsp * sizeof(T) + 15) & ~(size_t)15;
+}
+
+// One bordered Jacobian row per warp. The row's entries fall in three groups, each
+// handled by its own pass so that the lanes of a warp do the same work (an FP64
+// instruction costs a full FP64-pipe slot however few lanes are active):
+//   (1) l > 0 columns off the band: the dense Coulomb product only, T arithmetic;
+//   (2) l = 0 columns off the band: rank-1 terms, plus the inelastic l = 0 block on
+//       l = 0 rows, summed in FP64 there (they cancel nearly equal terms at low E/N);
+//   (3) the band (p - 3 .. p + 3 splines x all modes): every term summed in FP64.
 template <typename T>
 __global__ void __launch_bounds__(JAC_WARPS * 32)
 k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int nact, const double* __restrict__ h,
@@ -523,15 +538,31 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
     if (slot >= nact) return;
     const int pt = act[slot];
     if (pp.eept) ee = pp.eept[pt];
-    const int n = g.n, nsh = g.nsh, nsp = g.nsp, N = n + 1;
+    const int n = g.n, nsh = g.nsh, nsp = g.nsp, N = n + 1, nspc = g.nspecies;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int a = blockIdx.x * JAC_WARPS + wid;  // row
+    const double n0 = pp.n0[pt], Tg = pp.Tg[pt], E = pp.E[pt];
+    // per-point column vectors of the l = 0 columns and the species scalars
+    double* sWd = reinterpret_cast<double*>(jsm);
+    double* sNs = sWd + nsp;
+    T* sWt = reinterpret_cast<T*>(sNs + nspc);
+    T* sTt = sWt + nsp;
+    T* sMt = sTt + nsp;
+    for (int sp = threadIdx.x; sp < nspc; sp += blockDim.x) sNs[sp] = n0 * pp.ns[(size_t)sp * pp.P + pt];
+    for (int c = threadIdx.x; c < nsp; c += blockDim.x) {
+        double w = 0.0;
+        for (int sp = 0; sp < nspc; ++sp) w += n0 * pp.ns[(size_t)sp * pp.P + pt] * g.W[(size_t)sp * n + c * nsh];
+        sWd[c] = w;
+        sWt[c] = (T)w;
+        sTt[c] = (T)g.temp[c * nsh];
+        sMt[c] = (T)g.mass[c * nsh];
+    }
     // rows of HL / GL this CTA's rows touch (p - 3 .. p + 3), staged in shared memory
     const int a0 = blockIdx.x * JAC_WARPS;
     const int prow0 = max(0, min(a0, n - 1) / nsh - BTE_BAND);
     const int prow1 = min(nsp - 1, min(a0 + JAC_WARPS - 1, n - 1) / nsh + BTE_BAND);
     const int nr = prow1 - prow0 + 1;
-    T* sHL = reinterpret_cast<T*>(jsm);
+    T* sHL = reinterpret_cast<T*>(jsm + jac_col_bytes<T>(nsp, nspc));
     T* sGL = sHL + (size_t)nr * nsh * nsp;
     if (stage_hl && ee) {
         const T* HLg = OpsT<T>::HL(g);
@@ -542,17 +573,17 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
             sHL[e] = HLg[src];
             sGL[e] = GLg[src];
         }
-        __syncthreads();
     }
+    __syncthreads();
     if (a > n) return;
     T* Jr = J + (size_t)slot * stride + (size_t)a * ld;
     const double* hp = h + (size_t)pt * n;
     const double* ax = aux + (size_t)pt * 4 * n;
     const double* sc = scal + (size_t)pt * SC_COUNT;
-    const double n0 = pp.n0[pt], Tg = pp.Tg[pt], E = pp.E[pt];
+    const bool be = (jshift != 0.0);
     // border scale: per unit n0 for the steady Jacobian (it matches the collision operator);
     // absolute for the backward-Euler matrix (it matches the mass matrix)
-    const double beta = (jshift != 0.0) ? beta_scale : beta_scale * n0;
+    const double beta = be ? beta_scale : beta_scale * n0;
     if (a == n) {  // constraint row
         double uh = 0.0;
         for (int j = lane; j < n; j += 32) {
@@ -605,80 +636,99 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
     }
     const T* HL = OpsT<T>::HL(g);
     const T* GL = OpsT<T>::GL(g);
-    const double cadv = E * g.c_adv;
-    const T mh_t = (T)mh, negam_t = (T)negam, dgt_t = (T)dg_t, dgm_t = (T)dg_m;
-    for (int j = lane; j < N + 1; j += 32) {
-        if (j == n) { Jr[j] = (T)(-beta * g.Mp[a]); continue; }
-        if (j == n + 1) { Jr[j] = (T)(-F[(size_t)pt * n + a]); continue; }
-        const int c = j / nsh, s = j % nsh;
-        const int dk = c - p;
-        const bool band = (dk >= -BTE_BAND && dk <= BTE_BAND);
-        // dense Coulomb product in T
+    // dense Coulomb product of column (c, s) in T: sum_dr K2[s][dr] HL/GL[s][p + dr - 3][c]
+    auto coulomb = [&](int c, int s) -> T {
+        const T* hl = stage_hl ? sHL + ((ptrdiff_t)s * nr - prow0) * nsp + c : HL + (size_t)s * nsp * nsp + c;
+        const T* gl = stage_hl ? sGL + ((ptrdiff_t)s * nr - prow0) * nsp + c : GL + (size_t)s * nsp * nsp + c;
         T acc = T(0);
-        if (ee) {
-            const T* hl = stage_hl ? sHL + ((ptrdiff_t)s * nr - prow0) * nsp + c : HL + (size_t)s * nsp * nsp + c;
-            const T* gl = stage_hl ? sGL + ((ptrdiff_t)s * nr - prow0) * nsp + c : GL + (size_t)s * nsp * nsp + c;
 #pragma unroll
-            for (int dr = 0; dr < BTE_NB; ++dr) {
-                int r = p + dr - BTE_BAND;
-                if (r < 0 || r >= nsp) continue;
-                acc += k2a[s * BTE_NB + dr] * hl[(size_t)r * nsp] + k2b[s * BTE_NB + dr] * gl[(size_t)r * nsp];
-            }
+        for (int dr = 0; dr < BTE_NB; ++dr) {
+            int r = p + dr - BTE_BAND;
+            if (r < 0 || r >= nsp) continue;
+            acc += k2a[s * BTE_NB + dr] * hl[(size_t)r * nsp] + k2b[s * BTE_NB + dr] * gl[(size_t)r * nsp];
         }
-        if (!band && !(q == 0 && s == 0)) {
-            // away from the band and the l = 0 block only the Coulomb product and the rank-1
-            // terms (l = 0 columns) contribute: no cancellation, T arithmetic
-            T v = negam_t * acc;
-            if (s == 0) {
-                T wj = T(0);
-                for (int sp = 0; sp < g.nspecies; ++sp)
-                    wj += (T)(n0 * pp.ns[(size_t)sp * pp.P + pt] * g.W[(size_t)sp * n + j]);
-                v += -mh_t * wj;
-                if (ee) v += dgt_t * (T)g.temp[j] - dgm_t * (T)g.mass[j];
-            }
-            Jr[j] = (jshift != 0.0) ? v * (T)jscale : v;
-            continue;
-        }
-        // l = 0 block and band: every term summed in FP64 and rounded once (the l = 0 rows
-        // cancel nearly equal terms at low E/N)
-        double wj = 0.0;
-        if (s == 0)
-            for (int sp = 0; sp < g.nspecies; ++sp) wj += n0 * pp.ns[(size_t)sp * pp.P + pt] * g.W[(size_t)sp * n + j];
-        double v = -mh * wj + ((ee && s == 0) ? (dg_t * g.temp[j] - dg_m * g.mass[j]) : 0.0) + negam * (double)acc;
-        if (q == 0 && s == 0)
-            for (int sp = 0; sp < g.nspecies; ++sp)
-                v += (n0 * pp.ns[(size_t)sp * pp.P + pt]) * g.q0[((size_t)sp * nsp + p) * nsp + c];
-        if (band) {
-            const int bi = p * BTE_NB + dk + BTE_BAND;
-            if (s == q) {
-                if (q == 0) v += (n0 * Tg) * g.cgT[bi];
-                else
-                    for (int sp = 0; sp < g.nspecies; ++sp)
-                        v += (n0 * pp.ns[(size_t)sp * pp.P + pt]) * g.q1[((size_t)sp * nsp + p) * BTE_NB + dk + BTE_BAND];
-                v -= mu * g.Mr[bi];
-            }
-            if (s == q + 1) v += cadv * (g.mm1[bi] * g.adv_coef[q * 4 + 0] + g.adv_coef[q * 4 + 1] * g.mm2[bi]);
-            if (s == q - 1) v += cadv * (g.mm1[bi] * g.adv_coef[q * 4 + 2] + g.adv_coef[q * 4 + 3] * g.mm2[bi]);
+        return acc;
+    };
+    const double cadv = E * g.c_adv;
+    const T mh_t = (T)mh, negam_t = (T)negam, dgt_t = (T)dg_t, dgm_t = (T)dg_m, jscale_t = (T)jscale;
+    if (lane == 0) {
+        Jr[n] = (T)(-beta * g.Mp[a]);
+        Jr[n + 1] = (T)(-F[(size_t)pt * n + a]);
+    }
+    // (1) l > 0 columns off the band
+    const int nh = nsh - 1;
+    for (int e = lane; e < nsp * nh; e += 32) {
+        const int c = e / nh, s = 1 + e % nh;
+        if (c >= p - BTE_BAND && c <= p + BTE_BAND) continue;
+        T v = ee ? negam_t * coulomb(c, s) : T(0);
+        Jr[c * nsh + s] = be ? v * jscale_t : v;
+    }
+    // (2) l = 0 columns off the band
+    for (int c = lane; c < nsp; c += 32) {
+        if (c >= p - BTE_BAND && c <= p + BTE_BAND) continue;
+        const int j = c * nsh;
+        const T acc = ee ? coulomb(c, 0) : T(0);
+        if (q == 0) {
+            double v = -mh * sWd[c];
             if (ee) {
-                // K1[(p,q)][(c,s)] = sum_{t=(q,s,s')} sum_dr C[t][p][dk][dr] pot[(p+dr, s')]
-                double k1 = 0.0;
-                for (int t = 0; t < g.ntri; ++t) {
-                    if (g.tri[3 * t] != q || g.tri[3 * t + 1] != s) continue;
-                    const int s2 = g.tri[3 * t + 2];
-                    const double* ca = g.CA + ((size_t)t * nsp + p) * BTE_NB * BTE_NB + (dk + BTE_BAND) * BTE_NB;
-                    const double* cb = g.CB + ((size_t)t * nsp + p) * BTE_NB * BTE_NB + (dk + BTE_BAND) * BTE_NB;
-                    for (int dr = -BTE_BAND; dr <= BTE_BAND; ++dr) {
-                        int rr = p + dr;
-                        if (rr < 0 || rr >= nsp) continue;
-                        k1 += ca[dr + BTE_BAND] * ax[rr * nsh + s2] + cb[dr + BTE_BAND] * ax[n + rr * nsh + s2];
-                    }
-                }
-                v += negam * k1;
+                v += dg_t * g.temp[j] - dg_m * g.mass[j];
+                v += negam * (double)acc;
             }
+            const double* q0 = g.q0 + (size_t)p * nsp + c;
+            for (int sp = 0; sp < nspc; ++sp) v += sNs[sp] * q0[(size_t)sp * nsp * nsp];
+            if (be) v *= jscale;
+            Jr[j] = (T)v;
+        } else {
+            T v = negam_t * acc;
+            v += -mh_t * sWt[c];
+            if (ee) v += dgt_t * sTt[c] - dgm_t * sMt[c];
+            Jr[j] = be ? v * jscale_t : v;
         }
-        if (jshift != 0.0) {  // backward-Euler form only: the steady kernel spends no FP64 op here
+    }
+    // (3) the band
+    for (int e = lane; e < BTE_NB * nsh; e += 32) {
+        const int dk = e / nsh - BTE_BAND, s = e % nsh;
+        const int c = p + dk;
+        if (c < 0 || c >= nsp) continue;
+        const int j = c * nsh + s;
+        const int bi = p * BTE_NB + dk + BTE_BAND;
+        double v = 0.0;
+        if (s == 0) {
+            v = -mh * sWd[c];
+            if (ee) v += dg_t * g.temp[j] - dg_m * g.mass[j];
+        }
+        if (ee) v += negam * (double)coulomb(c, s);
+        if (s == q) {
+            if (q == 0) {
+                const double* q0 = g.q0 + (size_t)p * nsp + c;
+                for (int sp = 0; sp < nspc; ++sp) v += sNs[sp] * q0[(size_t)sp * nsp * nsp];
+                v += (n0 * Tg) * g.cgT[bi];
+            } else {
+                for (int sp = 0; sp < nspc; ++sp) v += sNs[sp] * g.q1[((size_t)sp * nsp + p) * BTE_NB + dk + BTE_BAND];
+            }
+            v -= mu * g.Mr[bi];
+        }
+        if (s == q + 1) v += cadv * (g.mm1[bi] * g.adv_coef[q * 4 + 0] + g.adv_coef[q * 4 + 1] * g.mm2[bi]);
+        if (s == q - 1) v += cadv * (g.mm1[bi] * g.adv_coef[q * 4 + 2] + g.adv_coef[q * 4 + 3] * g.mm2[bi]);
+        if (ee) {
+            // K1[(p,q)][(c,s)] = sum_{t=(q,s,s')} sum_dr C[t][p][dk][dr] pot[(p+dr, s')]
+            double k1 = 0.0;
+            for (int t = 0; t < g.ntri; ++t) {
+                if (g.tri[3 * t] != q || g.tri[3 * t + 1] != s) continue;
+                const int s2 = g.tri[3 * t + 2];
+                const double* ca = g.CA + ((size_t)t * nsp + p) * BTE_NB * BTE_NB + (dk + BTE_BAND) * BTE_NB;
+                const double* cb = g.CB + ((size_t)t * nsp + p) * BTE_NB * BTE_NB + (dk + BTE_BAND) * BTE_NB;
+                for (int dr = -BTE_BAND; dr <= BTE_BAND; ++dr) {
+                    int rr = p + dr;
+                    if (rr < 0 || rr >= nsp) continue;
+                    k1 += ca[dr + BTE_BAND] * ax[rr * nsh + s2] + cb[dr + BTE_BAND] * ax[n + rr * nsh + s2];
+                }
+            }
+            v += negam * k1;
+        }
+        if (be) {  // backward-Euler form only: the steady kernel spends no FP64 op here
             v *= jscale;
-            if (band && s == q) v += jshift * g.Mr[p * BTE_NB + dk + BTE_BAND];
+            if (s == q) v += jshift * g.Mr[bi];
         }
         Jr[j] = (T)v;
     }
@@ -920,18 +970,28 @@ static int ensure_work(BteWork* w, const BteGrid* g, int P, int prec) {
 static inline unsigned nblk(int n, int b) { return (unsigned)((n + b - 1) / b); }
 
 // shared memory of a Jacobian CTA when its HL / GL rows are staged (0: read from global)
+// Dynamic shared memory of k_jacobian: the per-point column vectors, and (with e-e on) the
+// HL / GL rows of the CTA's splines when they fit in 96 KB (else they are read from HBM).
+struct JacSmem {
+    size_t bytes;
+    int stage;
+};
 template <typename T>
-static size_t jac_smem(const BteGrid* g, int ee) {
-    if (!ee) return 0;
+static JacSmem jac_smem(const BteGrid* g, int ee) {
+    JacSmem r{jac_col_bytes<T>(g->nsp, g->nspecies), 0};
     const int rows = (JAC_WARPS + g->nsh - 1) / g->nsh + 1 + 2 * BTE_BAND;
-    size_t b = (size_t)2 * rows * g->nsh * g->nsp * sizeof(T);
-    if (b > 96 * 1024) return 0;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_jacobian<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-        attr_set = true;
+    const size_t hl = (size_t)2 * rows * g->nsh * g->nsp * sizeof(T);
+    if (ee && r.bytes + hl <= 96 * 1024) {
+        r.bytes += hl;
+        r.stage = 1;
     }
-    return b;
+    // opt in above the default 48 KB once per device (the launch fails loudly past the limit)
+    static unsigned set_mask = 0;
+    if (r.bytes > 48 * 1024 && g->device < 32 && !(set_mask & (1u << g->device))) {
+        cudaFuncSetAttribute(k_jacobian<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        set_mask |= 1u << g->device;
+    }
+    return r;
 }
 
 BteWork* bte_work_get(BteGrid* g) {
@@ -1150,9 +1210,10 @@ static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
         if (prec == BTE_PREC_MIXED) {
             float* xs = reinterpret_cast<float*>(L.xs);
             CKR(pf.run(PF_JACOBIAN, s, nact * jac_flops_pt(g, ee), jb, 1, [&] {
-                k_jacobian<float><<<gj, JAC_WARPS * 32, jac_smem<float>(g, ee), s>>>(gv, pp, ee, L.act, nact, w->h, w->F, w->aux, w->scal,
-                                                                  (float*)L.J, ld, jstride, beta_scale, L.rowscale,
-                                                                  jac_smem<float>(g, ee) > 0, 1.0, 0.0);
+                const JacSmem jm = jac_smem<float>(g, ee);
+                k_jacobian<float><<<gj, JAC_WARPS * 32, jm.bytes, s>>>(gv, pp, ee, L.act, nact, w->h, w->F, w->aux, w->scal,
+                                                                 (float*)L.J, ld, jstride, beta_scale, L.rowscale,
+                                                                 jm.stage, 1.0, 0.0);
             }));
             CKR(pf.run(PF_LU, s, nact * lu_flops(N), lub, 1, [&] {
                 le = bte_lu_factor_t<float>(nact, N, N + 1, (float*)L.J, ld, jstride, L.piv, L.info, s, 0);
@@ -1190,9 +1251,10 @@ static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
         } else {
             double* xs = L.xs;
             CKR(pf.run(PF_JACOBIAN, s, nact * jac_flops_pt(g, ee), jb, 1, [&] {
-                k_jacobian<double><<<gj, JAC_WARPS * 32, jac_smem<double>(g, ee), s>>>(gv, pp, ee, L.act, nact, w->h, w->F, w->aux, w->scal,
-                                                                   (double*)L.J, ld, jstride, beta_scale, L.rowscale,
-                                                                  jac_smem<double>(g, ee) > 0, 1.0, 0.0);
+                const JacSmem jm = jac_smem<double>(g, ee);
+                k_jacobian<double><<<gj, JAC_WARPS * 32, jm.bytes, s>>>(gv, pp, ee, L.act, nact, w->h, w->F, w->aux, w->scal,
+                                                                  (double*)L.J, ld, jstride, beta_scale, L.rowscale,
+                                                                  jm.stage, 1.0, 0.0);
             }));
             CKR(pf.run(PF_LU, s, nact * lu_flops(N), lub, 1, [&] {
                 le = bte_lu_factor_t<double>(nact, N, N + 1, (double*)L.J, ld, jstride, L.piv, L.info, s, 0);
@@ -1875,18 +1937,20 @@ int bte_transient_impl(BteGrid* g, int P, const double* n0, const double* ne, co
         cudaError_t le = cudaSuccess;
         if (prec == BTE_PREC_MIXED) {
             CKR(pf.run(PF_JACOBIAN, s, 0, 0, 1, [&] {
-                k_jacobian<float><<<gj, JAC_WARPS * 32, jac_smem<float>(g, c.ee), s>>>(
+                const JacSmem jm = jac_smem<float>(g, c.ee);
+                k_jacobian<float><<<gj, JAC_WARPS * 32, jm.bytes, s>>>(
                     c.gv, c.pp, c.ee, all, P, w->h, w->F, w->aux, w->scal, (float*)w->J, ld, js, beta, w->rowscale,
-                    jac_smem<float>(g, c.ee) > 0, -cdt, 1.0);
+                    jm.stage, -cdt, 1.0);
             }));
             CKR(pf.run(PF_LU, s, P * lu_flops(N), 0, 1, [&] {
                 le = bte_lu_factor_t<float>(P, N, N, (float*)w->J, ld, js, w->piv, w->info, s, 0);
             }));
         } else {
             CKR(pf.run(PF_JACOBIAN, s, 0, 0, 1, [&] {
-                k_jacobian<double><<<gj, JAC_WARPS * 32, jac_smem<double>(g, c.ee), s>>>(
+                const JacSmem jm = jac_smem<double>(g, c.ee);
+                k_jacobian<double><<<gj, JAC_WARPS * 32, jm.bytes, s>>>(
                     c.gv, c.pp, c.ee, all, P, w->h, w->F, w->aux, w->scal, (double*)w->J, ld, js, beta, w->rowscale,
-                    jac_smem<double>(g, c.ee) > 0, -cdt, 1.0);
+                    jm.stage, -cdt, 1.0);
             }));
             CKR(pf.run(PF_LU, s, P * lu_flops(N), 0, 1, [&] {
                 le = bte_lu_factor_t<double>(P, N, N, (double*)w->J, ld, js, w->piv, w->info, s, 0);
