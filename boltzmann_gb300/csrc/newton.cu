@@ -250,6 +250,10 @@ k_ref_merit(GridView g, int P, const int* __restrict__ list, const double* __res
     if (tid == 0) out[pt] = sqrt(nn);
 }
 
+// Per Jacobian row (p, q): K1 at the band columns (dk, s), e = (dk + 3) nsh + s, then
+// K2a[s][dr] and K2b[s][dr] (the e-e bilinear form's two linearizations), in FP64.
+__host__ __device__ inline int kc_row(int nsh) { return 3 * BTE_NB * nsh; }
+
 // ---------------------------------------------------------------------------------
 // FP64 iterative refinement of the mixed-precision Newton step: r = b - J x with the
 // bordered Jacobian applied matrix-free in FP64 (the same terms k_jacobian writes):
@@ -264,7 +268,7 @@ k_refine_residual(GridView g, PointParams pp, int ee, const int* __restrict__ ac
                   const double* __restrict__ h, const double* __restrict__ F, const double* __restrict__ aux,
                   const double* __restrict__ scal, const double* __restrict__ x, int ldd, double beta_scale,
                   const double* __restrict__ rowscale, float* __restrict__ rs, double* __restrict__ sigma,
-                  const int* __restrict__ done) {
+                  const int* __restrict__ done, const double* __restrict__ kc) {
     extern __shared__ double sm[];
     const int slot = blockIdx.x;
     if (slot >= nact) return;
@@ -305,25 +309,29 @@ k_refine_residual(GridView g, PointParams pp, int ee, const int* __restrict__ ac
     ux = block_sum(ux, red);
     uh = block_sum(uh, red);
     if (ee) {
-        for (int r = tid; r < n; r += nt) {
-            int p = r / nsh, l = r % nsh;
-            const double* HLr = g.HL + ((size_t)l * nsp + p) * nsp;
-            const double* GLr = g.GL + ((size_t)l * nsp + p) * nsp;
+        // HL x and GL x; rows taken mode-major so that a warp shares the mode
+        for (int rm = tid; rm < n; rm += nt) {
+            const int l = rm / nsp, p = rm % nsp;
+            const double* HLr = g.HL + (size_t)rm * nsp;
+            const double* GLr = g.GL + (size_t)rm * nsp;
             double s1 = 0, s2 = 0;
             for (int c = 0; c < nsp; ++c) {
                 double v = sx[c * nsh + l];
                 s1 += HLr[c] * v;
                 s2 += GLr[c] * v;
             }
-            sxh[r] = s1;
-            sxg[r] = s2;
+            sxh[p * nsh + l] = s1;
+            sxg[p * nsh + l] = s2;
         }
         __syncthreads();
     }
     const double cadv = E * g.c_adv;
+    const int kcn = kc_row(nsh);
     double amax = 0.0;
-    for (int r = tid; r < n; r += nt) {
-        const int p = r / nsh, q = r % nsh;
+    // rows mode-major: the lanes of a warp take the same branch (dense l = 0 row or band)
+    for (int rm = tid; rm < n; rm += nt) {
+        const int q = rm / nsp, p = rm % nsp;
+        const int r = p * nsh + q;
         double y = 0.0;
         for (int s = 0; s < g.nspecies; ++s) {
             double ns = n0 * pp.ns[(size_t)s * pp.P + pt];
@@ -353,26 +361,20 @@ k_refine_residual(GridView g, PointParams pp, int ee, const int* __restrict__ ac
             mx += g.Mr[bi] * sx[k * nsh + q];
         }
         y += n0 * Tg * gt + cadv * adv - mu * mx - ax[3 * n + r] * wx;
-        if (ee) {
+        if (ee && kc) {
+            // C(x; HL h, GL h) + C(h; HL x, GL x) through the row's coefficients, which the
+            // Jacobian of this Newton step wrote: K1 . x over the band, K2a . (HL x) + K2b . (GL x)
+            const double* kr = kc + ((size_t)slot * n + r) * kcn;
             double c1 = 0.0;
-            for (int t = 0; t < g.ntri; ++t) {
-                if (g.tri[3 * t] != q) continue;
-                const int l = g.tri[3 * t + 1], s = g.tri[3 * t + 2];
-                const double* ca = g.CA + ((size_t)t * nsp + p) * BTE_NB * BTE_NB;
-                const double* cb = g.CB + ((size_t)t * nsp + p) * BTE_NB * BTE_NB;
-                for (int dk = -BTE_BAND; dk <= BTE_BAND; ++dk) {
-                    int k = p + dk;
-                    if (k < 0 || k >= nsp) continue;
-                    double in_h = 0.0, in_x = 0.0;
-                    for (int dr = -BTE_BAND; dr <= BTE_BAND; ++dr) {
-                        int rr = p + dr;
-                        if (rr < 0 || rr >= nsp) continue;
-                        int o = (dk + BTE_BAND) * BTE_NB + dr + BTE_BAND;
-                        in_h += ca[o] * ax[rr * nsh + s] + cb[o] * ax[n + rr * nsh + s];
-                        in_x += ca[o] * sxh[rr * nsh + s] + cb[o] * sxg[rr * nsh + s];
-                    }
-                    c1 += in_h * sx[k * nsh + l] + in_x * sh[k * nsh + l];
-                }
+            for (int e = 0; e < BTE_NB * nsh; ++e) {
+                const int k = p + e / nsh - BTE_BAND;
+                if (k >= 0 && k < nsp) c1 += kr[e] * sx[k * nsh + e % nsh];
+            }
+            for (int e = 0; e < BTE_NB * nsh; ++e) {
+                const int rr = p + e % BTE_NB - BTE_BAND;
+                if (rr < 0 || rr >= nsp) continue;
+                const int o = rr * nsh + e / BTE_NB;
+                c1 += kr[BTE_NB * nsh + e] * sxh[o] + kr[2 * BTE_NB * nsh + e] * sxg[o];
             }
             y += ne * gam * c1 + ne * ax[2 * n + r] * dgx;
         }
@@ -532,7 +534,7 @@ __global__ void __launch_bounds__(JAC_WARPS * 32)
 k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int nact, const double* __restrict__ h,
            const double* __restrict__ F, const double* __restrict__ aux, const double* __restrict__ scal,
            T* __restrict__ J, int ld, long long stride, double beta_scale, double* __restrict__ rowscale,
-           int stage_hl, double jscale, double jshift) {
+           int stage_hl, double jscale, double jshift, double* __restrict__ kc) {
     extern __shared__ __align__(16) unsigned char jsm[];
     const int slot = blockIdx.y;
     if (slot >= nact) return;
@@ -612,6 +614,7 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
     __shared__ T k2s[JAC_WARPS][2][BTE_NB * 5];
     T* k2a = k2s[wid][0];
     T* k2b = k2s[wid][1];
+    double* kcr = (ee && kc) ? kc + ((size_t)slot * n + a) * kc_row(nsh) : nullptr;
     if (ee) {
         for (int e = lane; e < nsh * BTE_NB; e += 32) {
             const int s = e / BTE_NB, dr = e % BTE_NB;
@@ -631,6 +634,10 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
             }
             k2a[e] = (T)acc_a;
             k2b[e] = (T)acc_b;
+            if (kcr) {
+                kcr[BTE_NB * nsh + e] = acc_a;
+                kcr[2 * BTE_NB * nsh + e] = acc_b;
+            }
         }
         __syncwarp();
     }
@@ -689,7 +696,10 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
     for (int e = lane; e < BTE_NB * nsh; e += 32) {
         const int dk = e / nsh - BTE_BAND, s = e % nsh;
         const int c = p + dk;
-        if (c < 0 || c >= nsp) continue;
+        if (c < 0 || c >= nsp) {
+            if (kcr) kcr[e] = 0.0;
+            continue;
+        }
         const int j = c * nsh + s;
         const int bi = p * BTE_NB + dk + BTE_BAND;
         double v = 0.0;
@@ -725,6 +735,7 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
                 }
             }
             v += negam * k1;
+            if (kcr) kcr[e] = k1;
         }
         if (be) {  // backward-Euler form only: the steady kernel spends no FP64 op here
             v *= jscale;
@@ -783,11 +794,18 @@ __global__ void k_store_solution(int P_act, const T* __restrict__ xs, int N, con
 // (or a residual already below stagnate_rtol * ||r0|| that the full step cannot reduce)
 // means the state is converged to the arithmetic's floor: for the worst-conditioned
 // points of the batched workloads (cond ~ 5e10 after equilibration) the FP64 Newton steps
-// at the floor are ~1e-9 of ||h||, so step_rtol = 1e-8 stops there.
+// at the floor are ~1e-9 of ||h||, so step_rtol = 1e-8 stops there. Where the floor's noise
+// steps are larger than that, the search stalls instead: a merit already below
+// STALL_RTOL * ||r0|| whose search has backtracked below STALL_ALPHA is at the floor (in the
+// quadratic basin a Newton step is taken whole), and the point ends with stall_status
+// (ROUNDOFF in FP64; the mixed form hands it to FP64) rather than halving on until a
+// noise-level decrease passes the test at a vanishing step.
+constexpr double STALL_ALPHA = 1.0 / 64.0;
+constexpr double STALL_RTOL = 1e-6;
 __global__ void k_armijo(int nact, const int* __restrict__ act, int* searching, double* alpha,
                          const double* __restrict__ r, const double* __restrict__ rt, double c, double rho,
                          double amin, int* status, int* nsearch, int* accepted, const double* __restrict__ r0,
-                         double stagnate_rtol, const double* __restrict__ srel, double step_rtol) {
+                         double stagnate_rtol, const double* __restrict__ srel, double step_rtol, int stall_status) {
     int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= nact) return;
     int pt = act[slot];
@@ -811,6 +829,12 @@ __global__ void k_armijo(int nact, const int* __restrict__ act, int* searching, 
         return;
     }
     al *= rho;
+    if (al < STALL_ALPHA && rr <= STALL_RTOL * r0[pt]) {
+        searching[pt] = 0;
+        accepted[pt] = 0;
+        status[pt] = stall_status;
+        return;
+    }
     if (al < amin) {
         searching[pt] = 0;
         accepted[pt] = 0;
@@ -908,13 +932,17 @@ struct BteWork {
     int32_t* refdone = nullptr;                  // refinement finished for the point in this Newton step
     int32_t* nit = nullptr;                      // Newton iterations of each point in its current solve
     void* J = nullptr;
+    // e-e coefficients of the Jacobian rows in FP64 by slot (mixed form with e-e only):
+    // P x n x kc_row(nsh), written by k_jacobian and applied by the refinement
+    double* kc = nullptr;
+    size_t kcbytes = 0;
     int32_t *piv = nullptr, *info = nullptr, *act = nullptr, *act2 = nullptr, *cnt = nullptr;
     int32_t *searching = nullptr, *accepted = nullptr;
 };
 
 static void free_work(BteWork* w) {
     void* ptrs[] = {w->nit, w->refdone, w->reason, w->corr0, w->corr1, w->ref_r, w->ref_r0, w->rowscale, w->h0, w->srel, w->sigma, w->xs, w->h, w->ht, w->F, w->Ft, w->aux, w->auxt, w->scal, w->scalt, w->dh, w->r, w->rt, w->r0,
-                    w->alpha, w->J, w->piv, w->info, w->act, w->act2, w->cnt, w->searching, w->accepted};
+                    w->alpha, w->J, w->kc, w->piv, w->info, w->act, w->act2, w->cnt, w->searching, w->accepted};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     *w = BteWork();
@@ -940,7 +968,8 @@ static int ensure_work(BteWork* w, const BteGrid* g, int P, int prec) {
     const int n = g->n, N = n + 1;
     const int ld = (N + 1 + 3) & ~3;  // row length of the augmented matrix, padded
     size_t jb = (size_t)P * N * ld * (prec == BTE_PREC_MIXED ? sizeof(float) : sizeof(double));
-    if (w->cap >= P && w->n == n && w->jbytes >= jb) return BTE_OK;
+    const size_t kb = (prec == BTE_PREC_MIXED && g->ee) ? (size_t)P * n * kc_row(g->nsh) * sizeof(double) : 0;
+    if (w->cap >= P && w->n == n && w->jbytes >= jb && w->kcbytes >= kb) return BTE_OK;
     free_work(w);
     auto A = [&](void** p, size_t bytes) -> bool { return cudaMalloc(p, std::max<size_t>(bytes, 8)) == cudaSuccess; };
     size_t pn = (size_t)P * n * sizeof(double);
@@ -957,19 +986,18 @@ static int ensure_work(BteWork* w, const BteGrid* g, int P, int prec) {
               A((void**)&w->reason, (size_t)P * sizeof(int32_t)) && A((void**)&w->refdone, (size_t)P * sizeof(int32_t)) &&
               A((void**)&w->nit, (size_t)P * sizeof(int32_t)) && A((void**)&w->r, P * sizeof(double)) &&
               A((void**)&w->rt, P * sizeof(double)) && A((void**)&w->r0, P * sizeof(double)) &&
-              A((void**)&w->alpha, P * sizeof(double)) && A(&w->J, jb) &&
+              A((void**)&w->alpha, P * sizeof(double)) && A(&w->J, jb) && (kb == 0 || A((void**)&w->kc, kb)) &&
               A((void**)&w->piv, (size_t)P * N * sizeof(int32_t)) && A((void**)&w->info, P * sizeof(int32_t)) &&
               A((void**)&w->act, P * sizeof(int32_t)) && A((void**)&w->act2, P * sizeof(int32_t)) &&
               A((void**)&w->cnt, 4 * sizeof(int32_t)) && A((void**)&w->searching, P * sizeof(int32_t)) &&
               A((void**)&w->accepted, P * sizeof(int32_t));
     if (!ok) { free_work(w); return BTE_ERR_ALLOC; }
-    w->cap = P; w->n = n; w->jbytes = jb; w->prec = prec;
+    w->cap = P; w->n = n; w->jbytes = jb; w->kcbytes = kb; w->prec = prec;
     return BTE_OK;
 }
 
 static inline unsigned nblk(int n, int b) { return (unsigned)((n + b - 1) / b); }
 
-// shared memory of a Jacobian CTA when its HL / GL rows are staged (0: read from global)
 // Dynamic shared memory of k_jacobian: the per-point column vectors, and (with e-e on) the
 // HL / GL rows of the CTA's splines when they fit in 96 KB (else they are read from HBM).
 struct JacSmem {
@@ -1175,6 +1203,7 @@ struct Lane {
     void* J;
     int32_t *piv, *info;
     double *xs, *rowscale, *sigma;
+    double* kc;  // e-e row coefficients by slot (refined lanes), else null
 };
 
 // One Newton iteration (Jacobian, factorization, step, refinement, line search, acceptance,
@@ -1213,7 +1242,7 @@ static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
                 const JacSmem jm = jac_smem<float>(g, ee);
                 k_jacobian<float><<<gj, JAC_WARPS * 32, jm.bytes, s>>>(gv, pp, ee, L.act, nact, w->h, w->F, w->aux, w->scal,
                                                                  (float*)L.J, ld, jstride, beta_scale, L.rowscale,
-                                                                 jm.stage, 1.0, 0.0);
+                                                                 jm.stage, 1.0, 0.0, L.kc);
             }));
             CKR(pf.run(PF_LU, s, nact * lu_flops(N), lub, 1, [&] {
                 le = bte_lu_factor_t<float>(nact, N, N + 1, (float*)L.J, ld, jstride, L.piv, L.info, s, 0);
@@ -1234,7 +1263,7 @@ static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
                            nact * (res_bytes_pt(g, true) + 0.5 * N * (N + 1) * wsz), 3, [&] {
                     k_refine_residual<<<nact, 256, ref_smem, s>>>(gv, pp, ee, L.act, nact, w->h, w->F, w->aux,
                                                                   w->scal, w->dh, ldd, beta_scale, L.rowscale, xs,
-                                                                  L.sigma, w->refdone);
+                                                                  L.sigma, w->refdone, L.kc);
                     le = bte_lu_solve_t<float>(nact, N, (const float*)L.J, ld, jstride, L.piv, xs, 0, s);
                     k_refine_update<<<nact, 128, 0, s>>>(nact, L.act, N, xs, L.sigma, w->dh, ldd, ccur,
                                                          w->refdone);
@@ -1254,7 +1283,7 @@ static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
                 const JacSmem jm = jac_smem<double>(g, ee);
                 k_jacobian<double><<<gj, JAC_WARPS * 32, jm.bytes, s>>>(gv, pp, ee, L.act, nact, w->h, w->F, w->aux, w->scal,
                                                                   (double*)L.J, ld, jstride, beta_scale, L.rowscale,
-                                                                  jm.stage, 1.0, 0.0);
+                                                                  jm.stage, 1.0, 0.0, nullptr);
             }));
             CKR(pf.run(PF_LU, s, nact * lu_flops(N), lub, 1, [&] {
                 le = bte_lu_factor_t<double>(nact, N, N + 1, (double*)L.J, ld, jstride, L.piv, L.info, s, 0);
@@ -1280,7 +1309,8 @@ static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
             CKR(other([&] {
                 k_armijo<<<nblk(nact, 256), 256, 0, s>>>(nact, L.act, w->searching, w->alpha, w->r, w->rt,
                                                         o->line_search_c, o->alpha_rho, amin, status, w->cnt,
-                                                        w->accepted, w->r0, 1e-9, w->srel, 1e-8);
+                                                        w->accepted, w->r0, 1e-9, w->srel, 1e-8,
+                                                        prec == BTE_PREC_MIXED ? BTE_ST_NEED_FP64 : BTE_ST_ROUNDOFF);
             }));
             int hc = 0;
             CKR(cudaMemcpyAsync(&hc, w->cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
@@ -1325,13 +1355,13 @@ int bte_solve_impl(BteGrid* g, int P, const double* n0, const double* ne, const 
     // border scale: typical magnitude of the raw collision operator per unit n0
     c.beta_scale = g->q0max / (g->umax > 0 ? g->umax : 1.0);
     c.res_smem = (size_t)5 * c.n * sizeof(double);
-    c.ref_smem = (size_t)(5 * c.n + 1) * sizeof(double);
+    c.ref_smem = (size_t)(5 * c.n + 2) * sizeof(double);  // x, r: n + 1 each; h, HL x, GL x: n each
     c.o = o; c.status = status; c.iters = iters; c.s = s;
     const int n = c.n;
     if (c.res_smem > 48 * 1024) CKR(cudaFuncSetAttribute(k_residual, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.res_smem));
     if (c.ref_smem > 48 * 1024) CKR(cudaFuncSetAttribute(k_refine_residual, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.ref_smem));
     Profiler& pf = g_prof;
-    Lane L{w->act, w->act2, w->J, w->piv, w->info, w->xs, w->rowscale, w->sigma};
+    Lane L{w->act, w->act2, w->J, w->piv, w->info, w->xs, w->rowscale, w->sigma, w->kc};
     auto other = [&](auto&& fn) { return pf.run(PF_OTHER, s, 0, 0, 1, fn); };
     auto residual_all = [&](int nact) {
         return pf.run(PF_RESIDUAL, s, nact * res_flops_pt(g, c.ee), nact * res_bytes_pt(g, false), 1, [&] {
@@ -1555,7 +1585,7 @@ static SolveCtx engine_ctx(BteEngine* e, cudaStream_t s) {
     c.jstride = (long long)c.N * c.ld;
     c.beta_scale = g->q0max / (g->umax > 0 ? g->umax : 1.0);
     c.res_smem = (size_t)5 * c.n * sizeof(double);
-    c.ref_smem = (size_t)(5 * c.n + 1) * sizeof(double);
+    c.ref_smem = (size_t)(5 * c.n + 2) * sizeof(double);  // x, r: n + 1 each; h, HL x, GL x: n each
     c.o = &e->opts; c.status = e->status; c.iters = e->iters; c.s = s;
     return c;
 }
@@ -1567,7 +1597,7 @@ int bte_engine_create_impl(BteGrid* g, int cap, int fcap, const bte_solve_opts* 
     const int n = g->n, N = n + 1, ld = (N + 1 + 3) & ~3;
     int rc = ensure_work(&e->w, g, cap, e->prec);
     if (rc) { delete e; return rc; }
-    e->bytes = e->w.jbytes + (size_t)cap * (size_t)(n * 12 + (N + 1) * 3 + 24) * sizeof(double);  // J + per-slot vectors
+    e->bytes = e->w.jbytes + e->w.kcbytes + (size_t)cap * (size_t)(n * 12 + (N + 1) * 3 + 24) * sizeof(double);  // J + per-slot vectors
     bool ok = true;
     auto A = [&](void** p, size_t bytes) {
         if (!ok) return;
@@ -1591,8 +1621,8 @@ int bte_engine_create_impl(BteGrid* g, int cap, int fcap, const bte_solve_opts* 
         A((void**)&e->sg64, (size_t)f * sizeof(double));
     }
     if (!ok) { engine_free(e); delete e; return BTE_ERR_ALLOC; }
-    e->main = Lane{e->w.act, e->w.act2, e->w.J, e->w.piv, e->w.info, e->w.xs, e->w.rowscale, e->w.sigma};
-    e->f64 = Lane{e->act64a, e->act64b, e->J64, e->piv64, e->info64, e->xs64, e->rs64, e->sg64};
+    e->main = Lane{e->w.act, e->w.act2, e->w.J, e->w.piv, e->w.info, e->w.xs, e->w.rowscale, e->w.sigma, e->w.kc};
+    e->f64 = Lane{e->act64a, e->act64b, e->J64, e->piv64, e->info64, e->xs64, e->rs64, e->sg64, nullptr};
     e->free_slots.resize(cap);
     for (int i = 0; i < cap; ++i) e->free_slots[i] = cap - 1 - i;  // pop_back hands out 0, 1, 2, ...
     SolveCtx c = engine_ctx(e, 0);
@@ -1940,7 +1970,7 @@ int bte_transient_impl(BteGrid* g, int P, const double* n0, const double* ne, co
                 const JacSmem jm = jac_smem<float>(g, c.ee);
                 k_jacobian<float><<<gj, JAC_WARPS * 32, jm.bytes, s>>>(
                     c.gv, c.pp, c.ee, all, P, w->h, w->F, w->aux, w->scal, (float*)w->J, ld, js, beta, w->rowscale,
-                    jm.stage, -cdt, 1.0);
+                    jm.stage, -cdt, 1.0, nullptr);
             }));
             CKR(pf.run(PF_LU, s, P * lu_flops(N), 0, 1, [&] {
                 le = bte_lu_factor_t<float>(P, N, N, (float*)w->J, ld, js, w->piv, w->info, s, 0);
@@ -1950,7 +1980,7 @@ int bte_transient_impl(BteGrid* g, int P, const double* n0, const double* ne, co
                 const JacSmem jm = jac_smem<double>(g, c.ee);
                 k_jacobian<double><<<gj, JAC_WARPS * 32, jm.bytes, s>>>(
                     c.gv, c.pp, c.ee, all, P, w->h, w->F, w->aux, w->scal, (double*)w->J, ld, js, beta, w->rowscale,
-                    jm.stage, -cdt, 1.0);
+                    jm.stage, -cdt, 1.0, nullptr);
             }));
             CKR(pf.run(PF_LU, s, P * lu_flops(N), 0, 1, [&] {
                 le = bte_lu_factor_t<double>(P, N, N, (double*)w->J, ld, js, w->piv, w->info, s, 0);
