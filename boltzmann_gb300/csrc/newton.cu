@@ -33,6 +33,7 @@ cudaError_t bte_lu_solve_t(int P, int N, const T* A, int ld, long long stride, c
 // device view of a grid (passed by value to kernels)
 struct GridView {
     int nsp, nsh, n, lmax, nspecies, ntri;
+    int tqmax;  // largest number of e-e triples (q, l, s) sharing one q
     double vth, mw0, c_adv, gam_c, k1ev;
     const double *Mr, *Minv, *mm1, *mm2, *q0, *q1, *cgT, *adv_coef;
     const double *mass, *temp, *u, *p, *Mp, *W;
@@ -131,8 +132,11 @@ k_residual(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
         __syncthreads();
     }
     const double cadv = E * g.c_adv;
-    for (int r = tid; r < n; r += nt) {
-        const int p = r / nsh, q = r % nsh;
+    // rows mode-major: the lanes of a warp share the mode, so the dense l = 0 row and the
+    // e-e triples of that mode run without divergence
+    for (int rm = tid; rm < n; rm += nt) {
+        const int q = rm / nsp, p = rm % nsp;
+        const int r = p * nsh + q;
         double y = 0.0;
         // electron-heavy collisions
         for (int s = 0; s < g.nspecies; ++s) {
@@ -521,6 +525,12 @@ template <typename T>
 __host__ __device__ inline size_t jac_col_bytes(int nsp, int nspecies) {
     return (((size_t)nsp + nspecies) * sizeof(double) + (size_t)3 * nsp * sizeof(T) + 15) & ~(size_t)15;
 }
+// then the per-warp partial sums of the e-e coefficients: tqmax triples x 7 offsets x
+// (K2a, K2b, K1) in FP64
+constexpr int JAC_TRI_MAX = 48;  // e-e triples of one mode (42 in all at l_max = 4)
+__host__ __device__ inline size_t jac_part_bytes(int tqmax) {
+    return (size_t)JAC_WARPS * tqmax * BTE_NB * 3 * sizeof(double);
+}
 
 // One bordered Jacobian row per warp. The row's entries fall in three groups, each
 // handled by its own pass so that the lanes of a warp do the same work (an FP64
@@ -564,7 +574,8 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
     const int prow0 = max(0, min(a0, n - 1) / nsh - BTE_BAND);
     const int prow1 = min(nsp - 1, min(a0 + JAC_WARPS - 1, n - 1) / nsh + BTE_BAND);
     const int nr = prow1 - prow0 + 1;
-    T* sHL = reinterpret_cast<T*>(jsm + jac_col_bytes<T>(nsp, nspc));
+    double* part = reinterpret_cast<double*>(jsm + jac_col_bytes<T>(nsp, nspc)) + (size_t)wid * g.tqmax * BTE_NB * 3;
+    T* sHL = reinterpret_cast<T*>(jsm + jac_col_bytes<T>(nsp, nspc) + jac_part_bytes(g.tqmax));
     T* sGL = sHL + (size_t)nr * nsh * nsp;
     if (stage_hl && ee) {
         const T* HLg = OpsT<T>::HL(g);
@@ -609,32 +620,76 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
     // dgamma/dh = gam_c * 1.5 * (Top / (Top.h) - Mop / (Mop.h)), Top = temp * K_1eV
     const double dg_t = ee ? ne * Ua * g.gam_c * 1.5 / t0 : 0.0;
     const double dg_m = ee ? ne * Ua * g.gam_c * 1.5 / m0 : 0.0;
-    // K2a[dr][s], K2b[dr][s] for this row: sum over triples (q, l, s) and dk of C[t][p][dk][dr] h[(p+dk, l)],
-    // accumulated in FP64 by the warp (lane = (s, dr) pair) and kept in shared memory as T
+    // e-e coefficients of this row, in FP64 (the linearization of C(h; HL h, GL h)):
+    //   K2a[s][dr] = sum_{t = (q, l, s)} sum_dk CA[t][p][dk][dr] h[(p + dk, l)]   (K2b: CB)
+    //   K1[dk][s]  = sum_{t = (q, s, s')} sum_dr (CA[t][p][dk][dr] HLh[(p + dr, s')] + CB .. GLh)
+    // One lane per (triple of mode q, offset) computes both partial sums, so that every lane
+    // is busy; the partials are then summed over the triples in triple order. K2 is kept in
+    // shared memory as T for the dense Coulomb product, K1 in FP64 for the band.
     __shared__ T k2s[JAC_WARPS][2][BTE_NB * 5];
+    __shared__ double k1s[JAC_WARPS][BTE_NB * 5];
+    __shared__ int tqs[JAC_WARPS][JAC_TRI_MAX];
     T* k2a = k2s[wid][0];
     T* k2b = k2s[wid][1];
+    double* k1r = k1s[wid];
+    int* tq = tqs[wid];
     double* kcr = (ee && kc) ? kc + ((size_t)slot * n + a) * kc_row(nsh) : nullptr;
     if (ee) {
-        for (int e = lane; e < nsh * BTE_NB; e += 32) {
-            const int s = e / BTE_NB, dr = e % BTE_NB;
-            double acc_a = 0.0, acc_b = 0.0;
-            for (int t = 0; t < g.ntri; ++t) {
-                if (g.tri[3 * t] != q || g.tri[3 * t + 2] != s) continue;
-                const int l = g.tri[3 * t + 1];
-                const double* ca = g.CA + ((size_t)t * nsp + p) * BTE_NB * BTE_NB + dr;
-                const double* cb = g.CB + ((size_t)t * nsp + p) * BTE_NB * BTE_NB + dr;
-                for (int dk = -BTE_BAND; dk <= BTE_BAND; ++dk) {
-                    int k = p + dk;
-                    if (k < 0 || k >= nsp) continue;
-                    double hv = hp[k * nsh + l];
-                    acc_a += ca[(dk + BTE_BAND) * BTE_NB] * hv;
-                    acc_b += cb[(dk + BTE_BAND) * BTE_NB] * hv;
+        int ntq = 0;
+        for (int t0 = 0; t0 < g.ntri; t0 += 32) {
+            const int t = t0 + lane;
+            const bool m = t < g.ntri && g.tri[3 * t] == q;
+            const unsigned bal = __ballot_sync(0xffffffffu, m);
+            const int at = ntq + __popc(bal & ((1u << lane) - 1u));
+            if (m && at < JAC_TRI_MAX) tq[at] = t;
+            ntq += __popc(bal);
+        }
+        ntq = min(ntq, g.tqmax);
+        __syncwarp();
+        for (int e = lane; e < ntq * BTE_NB; e += 32) {
+            const int t = tq[e / BTE_NB], o = e % BTE_NB;
+            const int l = g.tri[3 * t + 1], s2 = g.tri[3 * t + 2];
+            const double* ca = g.CA + ((size_t)t * nsp + p) * BTE_NB * BTE_NB;
+            const double* cb = g.CB + ((size_t)t * nsp + p) * BTE_NB * BTE_NB;
+            double pa = 0.0, pb = 0.0, p1 = 0.0;
+            for (int dk = -BTE_BAND; dk <= BTE_BAND; ++dk) {  // K2 partial, o = dr
+                const int k = p + dk;
+                if (k < 0 || k >= nsp) continue;
+                const double hv = hp[k * nsh + l];
+                pa += ca[(dk + BTE_BAND) * BTE_NB + o] * hv;
+                pb += cb[(dk + BTE_BAND) * BTE_NB + o] * hv;
+            }
+            const int c = p + o - BTE_BAND;  // K1 partial, o = dk + 3
+            if (c >= 0 && c < nsp) {
+                for (int dr = -BTE_BAND; dr <= BTE_BAND; ++dr) {
+                    const int rr = p + dr;
+                    if (rr < 0 || rr >= nsp) continue;
+                    p1 += ca[o * BTE_NB + dr + BTE_BAND] * ax[rr * nsh + s2] +
+                          cb[o * BTE_NB + dr + BTE_BAND] * ax[n + rr * nsh + s2];
                 }
+            }
+            part[3 * e + 0] = pa;
+            part[3 * e + 1] = pb;
+            part[3 * e + 2] = p1;
+        }
+        __syncwarp();
+        for (int e = lane; e < nsh * BTE_NB; e += 32) {
+            const int s = e / BTE_NB, dr = e % BTE_NB;     // K2[s][dr]
+            const int dk3 = e / nsh, s1 = e % nsh;          // K1 at e = (dk + 3) nsh + s1
+            double acc_a = 0.0, acc_b = 0.0, k1 = 0.0;
+            for (int i = 0; i < ntq; ++i) {
+                const int t = tq[i];
+                if (g.tri[3 * t + 2] == s) {
+                    acc_a += part[3 * (i * BTE_NB + dr) + 0];
+                    acc_b += part[3 * (i * BTE_NB + dr) + 1];
+                }
+                if (g.tri[3 * t + 1] == s1) k1 += part[3 * (i * BTE_NB + dk3) + 2];
             }
             k2a[e] = (T)acc_a;
             k2b[e] = (T)acc_b;
+            k1r[e] = k1;
             if (kcr) {
+                kcr[e] = k1;
                 kcr[BTE_NB * nsh + e] = acc_a;
                 kcr[2 * BTE_NB * nsh + e] = acc_b;
             }
@@ -696,10 +751,7 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
     for (int e = lane; e < BTE_NB * nsh; e += 32) {
         const int dk = e / nsh - BTE_BAND, s = e % nsh;
         const int c = p + dk;
-        if (c < 0 || c >= nsp) {
-            if (kcr) kcr[e] = 0.0;
-            continue;
-        }
+        if (c < 0 || c >= nsp) continue;
         const int j = c * nsh + s;
         const int bi = p * BTE_NB + dk + BTE_BAND;
         double v = 0.0;
@@ -720,23 +772,7 @@ k_jacobian(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
         }
         if (s == q + 1) v += cadv * (g.mm1[bi] * g.adv_coef[q * 4 + 0] + g.adv_coef[q * 4 + 1] * g.mm2[bi]);
         if (s == q - 1) v += cadv * (g.mm1[bi] * g.adv_coef[q * 4 + 2] + g.adv_coef[q * 4 + 3] * g.mm2[bi]);
-        if (ee) {
-            // K1[(p,q)][(c,s)] = sum_{t=(q,s,s')} sum_dr C[t][p][dk][dr] pot[(p+dr, s')]
-            double k1 = 0.0;
-            for (int t = 0; t < g.ntri; ++t) {
-                if (g.tri[3 * t] != q || g.tri[3 * t + 1] != s) continue;
-                const int s2 = g.tri[3 * t + 2];
-                const double* ca = g.CA + ((size_t)t * nsp + p) * BTE_NB * BTE_NB + (dk + BTE_BAND) * BTE_NB;
-                const double* cb = g.CB + ((size_t)t * nsp + p) * BTE_NB * BTE_NB + (dk + BTE_BAND) * BTE_NB;
-                for (int dr = -BTE_BAND; dr <= BTE_BAND; ++dr) {
-                    int rr = p + dr;
-                    if (rr < 0 || rr >= nsp) continue;
-                    k1 += ca[dr + BTE_BAND] * ax[rr * nsh + s2] + cb[dr + BTE_BAND] * ax[n + rr * nsh + s2];
-                }
-            }
-            v += negam * k1;
-            if (kcr) kcr[e] = k1;
-        }
+        if (ee) v += negam * k1r[e];
         if (be) {  // backward-Euler form only: the steady kernel spends no FP64 op here
             v *= jscale;
             if (s == q) v += jshift * g.Mr[bi];
@@ -951,6 +987,12 @@ static void free_work(BteWork* w) {
 static GridView view_of(const BteGrid* g) {
     GridView v;
     v.nsp = g->nsp; v.nsh = g->nsh; v.n = g->n; v.lmax = g->lmax; v.nspecies = g->nspecies; v.ntri = g->ntri;
+    v.tqmax = 0;
+    for (int q = 0; q < g->nsh; ++q) {
+        int c = 0;
+        for (int t = 0; t < g->ntri; ++t) c += (g->tri[3 * t] == q);
+        v.tqmax = std::max(v.tqmax, c);
+    }
     v.vth = g->vth; v.mw0 = g->mw0; v.c_adv = g->c_adv;
     v.gam_c = (BTE_QE * BTE_QE * BTE_QE * BTE_QE) / (4.0 * BTE_PI * (BTE_EPS0 * BTE_ME) * (BTE_EPS0 * BTE_ME)) / (g->vth * g->vth * g->vth);
     v.k1ev = BTE_QE / BTE_KB;
@@ -1006,7 +1048,13 @@ struct JacSmem {
 };
 template <typename T>
 static JacSmem jac_smem(const BteGrid* g, int ee) {
-    JacSmem r{jac_col_bytes<T>(g->nsp, g->nspecies), 0};
+    int tqmax = 0;
+    for (int q = 0; q < g->nsh; ++q) {
+        int c = 0;
+        for (int t = 0; t < g->ntri; ++t) c += (g->tri[3 * t] == q);
+        tqmax = std::max(tqmax, c);
+    }
+    JacSmem r{jac_col_bytes<T>(g->nsp, g->nspecies) + jac_part_bytes(tqmax), 0};
     const int rows = (JAC_WARPS + g->nsh - 1) / g->nsh + 1 + 2 * BTE_BAND;
     const size_t hl = (size_t)2 * rows * g->nsh * g->nsp * sizeof(T);
     if (ee && r.bytes + hl <= 96 * 1024) {
