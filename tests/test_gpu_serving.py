@@ -89,3 +89,40 @@ def test_result_same_alone_and_in_a_mix(synthetic_xs):
         ok = r.qoi["status"] <= 1
         assert np.all(np.isfinite(r.ff[:, ok]))
     assert summ["p99_ms"] >= summ["p50_ms"] > 0
+
+
+def test_tps_csv_requests_through_the_server(synthetic_xs, tmp_path):
+    """Points read from a TPS CSV (the reference driver's `-input` file) and split into
+    requests give, through the server, the plain solve path's results on the same points."""
+    from boltzmann_gb300.lxcat import read_available_species
+    from boltzmann_gb300.serving import BteServer, wait_all
+    from boltzmann_gb300.tps_input import read_tps_csv, requests_from_tps
+    import torch
+    species = read_available_species(synthetic_xs)
+    P, n_sp, l_max = 10, 32, 1
+    p = batch_parameters(P, 23)
+    path = tmp_path / "tps.csv"
+    with open(path, "w") as f:
+        f.write(",".join(["Tg", "n0", "ne/n0", "E"] + ["(%s)/n0" % s for s in species]) + "\n")
+        for i in range(P):
+            vals = [p["Tg"][i], p["n0"][i], p["ne"][i] / p["n0"][i], p["E"][i]] + [1.0] * len(species)
+            f.write(",".join(repr(float(v)) for v in vals) + "\n")
+    prm = read_tps_csv(str(path), species)
+    reqs = requests_from_tps(prm, n_sp, l_max, max_points=4)
+    assert [r.P for r in reqs] == [4, 4, 2]
+    with BteServer(synthetic_xs, [(n_sp, l_max)], precision="fp64", capacity=8, fp64_capacity=4) as srv:
+        for r in reqs:
+            srv.submit(r)
+        wait_all(reqs, timeout=300)
+    s, args = gpu_solver(synthetic_xs, n_sp, l_max, True, P, precision="fp64")
+    for k in ["n0", "ne", "ns_by_n0", "Tg", "E"]:
+        s.set_boltzmann_parameter(0, k, prm[k])
+    f0 = torch.as_tensor(s.initialize(0, P), device="cuda")
+    args.ee_collisions = 0
+    ffw, _ = s.solve(0, f0, 1e-20, 1e-14, 100, "steady-state", 1e-16, 0.5, 1e-4)
+    args.ee_collisions = 1
+    ff, _ = s.solve(0, ffw, 1e-20, 1e-14, 100, "steady-state", 1e-16, 0.5, 1e-4)
+    ff = ff.cpu().numpy()
+    got = np.concatenate([r.ff for r in reqs], axis=1)
+    assert all(np.all(r.qoi["status"] <= 1) for r in reqs)
+    assert float(np.max(rel_l2_cols(got, ff))) < TOL_SAME
