@@ -1009,7 +1009,10 @@ static GridView view_of(const BteGrid* g) {
 static int ensure_work(BteWork* w, const BteGrid* g, int P, int prec) {
     const int n = g->n, N = n + 1;
     const int ld = (N + 1 + 3) & ~3;  // row length of the augmented matrix, padded
-    size_t jb = (size_t)P * N * ld * (prec == BTE_PREC_MIXED ? sizeof(float) : sizeof(double));
+    // the mixed form's FP64 pass reuses this buffer for FP64 matrices, half as many: it holds
+    // at least two FP32 matrices so that one FP64 matrix fits whatever P is
+    size_t jb = (prec == BTE_PREC_MIXED) ? (size_t)std::max(P, 2) * N * ld * sizeof(float)
+                                         : (size_t)P * N * ld * sizeof(double);
     const size_t kb = (prec == BTE_PREC_MIXED && g->ee) ? (size_t)P * n * kc_row(g->nsh) * sizeof(double) : 0;
     if (w->cap >= P && w->n == n && w->jbytes >= jb && w->kcbytes >= kb) return BTE_OK;
     free_work(w);
@@ -1216,15 +1219,24 @@ __global__ void k_collect_failed(int P, int* status, int* act_out, int* nout, in
     }
 }
 
-// a point handed to the FP64 form keeps its last accepted iterate (every iterate the mixed
-// form accepted decreased the FP64 merit) and its iteration count; only a point whose
-// residual became non-finite restarts from h0
+// A point handed to the FP64 form keeps its iteration count, and by default its last
+// accepted iterate (every iterate the mixed form accepted decreased the FP64 merit): a
+// refinement that stalled in the first iterations leaves a sound iterate to continue from.
+// It restarts from h0 when its residual became non-finite, or when its mixed-form
+// trajectory went astray: its line search failed, or it was still running after
+// MIXED_HANDOVER_ITER iterations (points converge in about 15). FP64 Newton can stall from
+// such an iterate as well, even where the lumped merit is small (it weighs the components
+// unlike the reference's merit), while from h0 it converges in the iterations it always
+// takes.
+__device__ inline bool handover_restarts(int reason, int nit) {
+    return reason == BTE_ST_NONFINITE || reason == BTE_ST_LINESEARCH || nit >= MIXED_HANDOVER_ITER;
+}
 __global__ void k_restore(int n, int nact, const int* __restrict__ act, const int* __restrict__ reason,
                           const double* __restrict__ h0, double* h, int* nit) {
     int slot = blockIdx.x;
     if (slot >= nact) return;
     int pt = act[slot];
-    if (reason[pt] != BTE_ST_NONFINITE) return;
+    if (!handover_restarts(reason[pt], nit[pt])) return;
     for (int i = threadIdx.x; i < n; i += blockDim.x) h[(size_t)pt * n + i] = h0[(size_t)pt * n + i];
 }
 
@@ -1440,8 +1452,9 @@ int bte_solve_impl(BteGrid* g, int P, const double* n0, const double* ne, const 
         int nf = 0;
         CKR(cudaMemcpyAsync(&nf, w->cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         CKR(cudaStreamSynchronize(s));
-        // the J buffer holds FP32 matrices for P points: FP64 chunks of at most P / 2
-        const int chunk = std::max(1, P / 2);
+        // FP64 chunks of as many matrices as the J buffer holds in FP64 (at least one)
+        const int chunk = (int)std::min<size_t>((size_t)P, w->jbytes / ((size_t)c.N * c.ld * sizeof(double)));
+        if (chunk < 1) return BTE_ERR_STATE;
         std::vector<int32_t> failed(nf);
         if (nf) CKR(cudaMemcpyAsync(failed.data(), L.act2, nf * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         CKR(cudaStreamSynchronize(s));
@@ -1569,7 +1582,7 @@ __global__ void k_engine_to_fp64(int m, const int* __restrict__ list, int n, int
     const int st = status[pt];
     __syncthreads();
     if (threadIdx.x == 0) { reason[pt] = st; status[pt] = -1; }
-    if (st != BTE_ST_NONFINITE) return;
+    if (!handover_restarts(st, nit[pt])) return;
     for (int k = threadIdx.x; k < n; k += blockDim.x) h[(size_t)pt * n + k] = h0[(size_t)pt * n + k];
 }
 

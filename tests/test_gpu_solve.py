@@ -85,3 +85,24 @@ def test_mixed_matches_fp64(synthetic_xs):
     f1, q1 = gpu_solution(s1, a1, prm, True, P)
     f2, q2 = gpu_solution(s2, a2, prm, True, P)
     assert np.max(rel_l2_cols(f2, f1)) < 1e-8
+
+
+@pytest.mark.parametrize("n_pts", [1, 3])
+def test_mixed_handover_small_batches(synthetic_xs, n_pts):
+    """Points the mixed form hands to FP64 run in FP64 chunks inside the mixed form's
+    Jacobian buffer; with one point that buffer must still hold one FP64 matrix. A line
+    search floor of 0.9 makes the damped first steps fail, so every point is handed over
+    (reason: line search, which restarts it from its initial state) and ends as the plain
+    FP64 form ends it."""
+    from boltzmann_gb300.workloads import batch_parameters
+    prm = batch_parameters(n_pts, 31, ee=False)
+    out = {}
+    for precision in ("mixed", "fp64"):
+        s, args = gpu_solver(synthetic_xs, 32, 1, False, n_pts, precision=precision)
+        for k in ["n0", "ne", "ns_by_n0", "Tg", "E"]:
+            s.set_boltzmann_parameter(0, k, prm[k])
+        f0 = s.initialize(0, n_pts)
+        ff, qoi = s.solve(0, f0, ATOL, RTOL, 100, "steady-state", 0.9, 0.5, 1e-4)
+        out[precision] = (np.asarray(ff), np.asarray(qoi["status"]))
+    np.testing.assert_array_equal(out["mixed"][1], out["fp64"][1])
+    assert float(np.max(rel_l2_cols(out["mixed"][0], out["fp64"][0]))) < 1e-8
