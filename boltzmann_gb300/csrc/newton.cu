@@ -1219,24 +1219,26 @@ __global__ void k_collect_failed(int P, int* status, int* act_out, int* nout, in
     }
 }
 
-// A point handed to the FP64 form keeps its iteration count, and by default its last
-// accepted iterate (every iterate the mixed form accepted decreased the FP64 merit): a
-// refinement that stalled in the first iterations leaves a sound iterate to continue from.
-// It restarts from h0 when its residual became non-finite, or when its mixed-form
-// trajectory went astray: its line search failed, or it was still running after
-// MIXED_HANDOVER_ITER iterations (points converge in about 15). FP64 Newton can stall from
-// such an iterate as well, even where the lumped merit is small (it weighs the components
-// unlike the reference's merit), while from h0 it converges in the iterations it always
-// takes.
-__device__ inline bool handover_restarts(int reason, int nit) {
-    return reason == BTE_ST_NONFINITE || reason == BTE_ST_LINESEARCH || nit >= MIXED_HANDOVER_ITER;
+// A point handed to the FP64 form keeps its iteration count. It keeps its last accepted
+// iterate when that iterate is already close to the root (merit below
+// HANDOVER_KEEP_RTOL of the initial one): FP64 Newton finishes from there in a step or
+// two. It restarts from h0 when its residual became non-finite, when its mixed-form
+// trajectory went astray (its line search failed, or it was still running after
+// MIXED_HANDOVER_ITER iterations; points converge in about 15), or when it is still far
+// from the root. FP64 Newton was seen to stall for 90 iterations from a mixed iterate at 5%
+// of the initial merit, while from h0 it converges in the iterations it always takes.
+constexpr double HANDOVER_KEEP_RTOL = 1e-3;
+__device__ inline bool handover_restarts(int reason, int nit, double r, double r0) {
+    if (reason == BTE_ST_NONFINITE || reason == BTE_ST_LINESEARCH || nit >= MIXED_HANDOVER_ITER) return true;
+    return !(r <= HANDOVER_KEEP_RTOL * r0);
 }
 __global__ void k_restore(int n, int nact, const int* __restrict__ act, const int* __restrict__ reason,
-                          const double* __restrict__ h0, double* h, int* nit) {
+                          const double* __restrict__ h0, double* h, int* nit, const double* __restrict__ r,
+                          const double* __restrict__ r0) {
     int slot = blockIdx.x;
     if (slot >= nact) return;
     int pt = act[slot];
-    if (!handover_restarts(reason[pt], nit[pt])) return;
+    if (!handover_restarts(reason[pt], nit[pt], r[pt], r0[pt])) return;
     for (int i = threadIdx.x; i < n; i += blockDim.x) h[(size_t)pt * n + i] = h0[(size_t)pt * n + i];
 }
 
@@ -1471,7 +1473,7 @@ int bte_solve_impl(BteGrid* g, int P, const double* n0, const double* ne, const 
         for (int c0 = 0; c0 < nf; c0 += chunk) {
             int m = std::min(chunk, nf - c0);
             CKR(cudaMemcpyAsync(L.act, failed.data() + c0, m * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-            CKR(other([&] { k_restore<<<m, 256, 0, s>>>(n, m, L.act, w->reason, w->h0, w->h, w->nit); }));
+            CKR(other([&] { k_restore<<<m, 256, 0, s>>>(n, m, L.act, w->reason, w->h0, w->h, w->nit, w->r, w->r0); }));
             CKR(residual_all(m));
             for (int it = 0, nact = m; it < o->max_iter && nact > 0; ++it) {
                 nact = newton_iteration(c, L, nact, BTE_PREC_FP64);
@@ -1575,14 +1577,15 @@ __global__ void k_engine_sort(int nold, const int* __restrict__ old, const int* 
 
 // a point entering the FP64 lane: as k_collect_failed + k_restore do in bte_solve_steady
 __global__ void k_engine_to_fp64(int m, const int* __restrict__ list, int n, int* status, int* reason, int* nit,
-                                 const double* __restrict__ h0, double* h) {
+                                 const double* __restrict__ h0, double* h, const double* __restrict__ r,
+                                 const double* __restrict__ r0) {
     const int i = blockIdx.x;
     if (i >= m) return;
     const int pt = list[i];
     const int st = status[pt];
     __syncthreads();
     if (threadIdx.x == 0) { reason[pt] = st; status[pt] = -1; }
-    if (!handover_restarts(st, nit[pt])) return;
+    if (!handover_restarts(st, nit[pt], r[pt], r0[pt])) return;
     for (int k = threadIdx.x; k < n; k += blockDim.x) h[(size_t)pt * n + k] = h0[(size_t)pt * n + k];
 }
 
@@ -1768,7 +1771,7 @@ int bte_engine_step_impl(BteEngine* e, int* n_done, int32_t* done_out, cudaStrea
         for (int i = 0; i < k; ++i) { mv[i] = e->f64_wait.front(); e->f64_wait.pop_front(); }
         CKR(cudaMemcpyAsync(e->l_in, mv.data(), k * sizeof(int32_t), cudaMemcpyHostToDevice, s));
         CKR(pf.run(PF_OTHER, s, 0, 0, 1, [&] {
-            k_engine_to_fp64<<<k, 256, 0, s>>>(k, e->l_in, n, e->status, w->reason, w->nit, w->h0, w->h);
+            k_engine_to_fp64<<<k, 256, 0, s>>>(k, e->l_in, n, e->status, w->reason, w->nit, w->h0, w->h, w->r, w->r0);
         }));
         CKR(pf.run(PF_RESIDUAL, s, k * res_flops_pt(g, c.ee), k * res_bytes_pt(g, false), 1, [&] {
             k_residual<<<k, 256, c.res_smem, s>>>(c.gv, c.pp, c.ee, e->l_in, k, w->h, nullptr, 0, nullptr, nullptr,
