@@ -36,7 +36,7 @@ cudaError_t bte_lu_factor_t(int P, int N, int NC, T* A, int ld, long long stride
                             cudaStream_t s, int kernel);
 template <typename T>
 cudaError_t bte_lu_solve_t(int P, int N, const T* A, int ld, long long stride, const int32_t* piv, T* b, int mode,
-                           cudaStream_t s);
+                           cudaStream_t s, const int32_t* mats = nullptr);
 
 namespace {
 
@@ -389,7 +389,7 @@ int bte1d_step_x(Bte1d* h, double hstep, double* V, void* stream) {
         h->launches += 2 + 3 * (long long)Nx;
     }
     const size_t smem = (size_t)Nr * Nr * 8;
-    if (smem > 48 * 1024) CK1(cudaFuncSetAttribute(k_radial_mix, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK1(bte_raise_smem_limit((const void*)k_radial_mix, smem));
     k_radial_mix<<<dim3(nb(C, 128), Nr), 128, smem, s>>>(Nr, C, h->Qinv, V, h->Vt);
     k_zero_inflow<<<nb((size_t)Nr * Nvt, 256), 256, 0, s>>>(Nr, Nvt, Nx, h->right, h->Vt);
     CK1(cudaGetLastError());

@@ -4,6 +4,10 @@
 #include <stdint.h>
 #include <math.h>
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 #define BTE_SP_ORDER 3          // cubic B-splines only (the reference's driver default)
 #define BTE_BAND 3              // |p - k| <= 3 for overlapping cubic supports
 #define BTE_NB (2 * BTE_BAND + 1)
@@ -21,6 +25,32 @@
 #define BTE_ERR_CUDA -2
 #define BTE_ERR_ALLOC -3
 #define BTE_ERR_STATE -4
+
+// Raise a kernel's dynamic shared-memory limit on the current device to at least `bytes`;
+// it is never lowered. The limit starts at 48 KB minus the kernel's static shared memory
+// (queried once per kernel and device), so a request below 48 KB can need it too. The limit
+// belongs to the kernel, not to the calling thread: serving engines launch the same kernels
+// from several host threads for grids of different sizes, and a smaller limit set by one of
+// them between another's set and launch made that launch fail.
+inline cudaError_t bte_raise_smem_limit(const void* kernel, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, size_t> cur;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    const auto key = std::make_pair(kernel, dev);
+    auto it = cur.find(key);
+    if (it == cur.end()) {
+        cudaFuncAttributes fa;
+        if ((e = cudaFuncGetAttributes(&fa, kernel)) != cudaSuccess) return e;
+        it = cur.emplace(key, (size_t)fa.maxDynamicSharedSizeBytes).first;
+    }
+    if (bytes <= it->second) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) it->second = bytes;
+    return e;
+}
 
 // Status codes written per point by the solver.
 #define BTE_ST_CONVERGED 0      // ||r|| <= atol + rtol * ||r0||

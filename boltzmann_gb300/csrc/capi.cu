@@ -14,7 +14,7 @@ cudaError_t bte_lu_factor_t(int P, int N, int NC, T* A, int ld, long long stride
                             cudaStream_t s, int kernel);
 template <typename T>
 cudaError_t bte_lu_solve_t(int P, int N, const T* A, int ld, long long stride, const int32_t* piv, T* b, int mode,
-                           cudaStream_t s);
+                           cudaStream_t s, const int32_t* mats = nullptr);
 void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w);
 
 static thread_local std::string g_last_error = "";

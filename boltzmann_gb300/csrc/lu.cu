@@ -415,16 +415,17 @@ k_lu_right(int N, int NC, T* __restrict__ A, int ld, long long stride, int32_t* 
 // Substitution for one right-hand side per matrix. mode 0: full solve (gather b by perm,
 // unit-lower forward, upper backward); mode 1: backward only (the RHS was eliminated as
 // column N during the factorization). Rows of position r are read from stored row perm[r].
+// With a list, CTA i solves with matrix mats[i] and right-hand side i.
 template <typename T>
 __global__ void __launch_bounds__(LU_THREADS)
 k_lu_solve(int N, const T* __restrict__ A, int ld, long long stride, const int32_t* __restrict__ perm,
-           T* __restrict__ b, int mode) {
+           T* __restrict__ b, int mode, const int32_t* __restrict__ mats) {
     extern __shared__ __align__(16) unsigned char smraw[];
     T* x = reinterpret_cast<T*>(smraw);
-    const int mat = blockIdx.x;
+    const int mat = mats ? mats[blockIdx.x] : (int)blockIdx.x;
     const T* a = A + (size_t)mat * stride;
     const int32_t* pm = perm + (size_t)mat * N;
-    T* bb = b + (size_t)mat * N;
+    T* bb = b + (size_t)blockIdx.x * N;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
     if (mode == 1) {
@@ -486,7 +487,7 @@ template <typename T, int RPT>
 cudaError_t launch_left(int P, int N, int NC, T* A, int ld, long long stride, int32_t* piv, int32_t* info,
                         cudaStream_t s) {
     size_t sm = left_smem_bytes(N, sizeof(T));
-    cudaError_t e = cudaFuncSetAttribute(k_lu_left<T, RPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = bte_raise_smem_limit((const void*)k_lu_left<T, RPT>, sm);
     if (e != cudaSuccess) return e;
     k_lu_left<T, RPT><<<P, LU_THREADS, sm, s>>>(N, NC, A, ld, stride, piv, info);
     return cudaGetLastError();
@@ -496,7 +497,7 @@ template <typename T, int NB, int ROWS>
 cudaError_t launch_right_r(int P, int N, int NC, T* A, int ld, long long stride, int32_t* piv, int32_t* info,
                            cudaStream_t s) {
     size_t sm = lu_smem_bytes(N, NC, NB, sizeof(T));
-    cudaError_t e = cudaFuncSetAttribute(k_lu_right<T, NB, ROWS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = bte_raise_smem_limit((const void*)k_lu_right<T, NB, ROWS>, sm);
     if (e != cudaSuccess) return e;
     k_lu_right<T, NB, ROWS><<<P, LU_THREADS, sm, s>>>(N, NC, A, ld, stride, piv, info);
     return cudaGetLastError();
@@ -549,18 +550,18 @@ cudaError_t bte_lu_factor_t(int P, int N, int NC, T* A, int ld, long long stride
 
 template <typename T>
 cudaError_t bte_lu_solve_t(int P, int N, const T* A, int ld, long long stride, const int32_t* piv, T* b, int mode,
-                           cudaStream_t s) {
+                           cudaStream_t s, const int32_t* mats) {
     if (P <= 0) return cudaSuccess;
     size_t sm = (size_t)N * sizeof(T);
-    if (sm > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_lu_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        if (e != cudaSuccess) return e;
-    }
-    k_lu_solve<T><<<P, LU_THREADS, sm, s>>>(N, A, ld, stride, piv, b, mode);
+    cudaError_t e = bte_raise_smem_limit((const void*)k_lu_solve<T>, sm);
+    if (e != cudaSuccess) return e;
+    k_lu_solve<T><<<P, LU_THREADS, sm, s>>>(N, A, ld, stride, piv, b, mode, mats);
     return cudaGetLastError();
 }
 
 template cudaError_t bte_lu_factor_t<double>(int, int, int, double*, int, long long, int32_t*, int32_t*, cudaStream_t, int);
 template cudaError_t bte_lu_factor_t<float>(int, int, int, float*, int, long long, int32_t*, int32_t*, cudaStream_t, int);
-template cudaError_t bte_lu_solve_t<double>(int, int, const double*, int, long long, const int32_t*, double*, int, cudaStream_t);
-template cudaError_t bte_lu_solve_t<float>(int, int, const float*, int, long long, const int32_t*, float*, int, cudaStream_t);
+template cudaError_t bte_lu_solve_t<double>(int, int, const double*, int, long long, const int32_t*, double*, int,
+                                            cudaStream_t, const int32_t*);
+template cudaError_t bte_lu_solve_t<float>(int, int, const float*, int, long long, const int32_t*, float*, int,
+                                           cudaStream_t, const int32_t*);

@@ -28,7 +28,7 @@ cudaError_t bte_lu_factor_t(int P, int N, int NC, T* A, int ld, long long stride
                             cudaStream_t s, int kernel);
 template <typename T>
 cudaError_t bte_lu_solve_t(int P, int N, const T* A, int ld, long long stride, const int32_t* piv, T* b, int mode,
-                           cudaStream_t s);
+                           cudaStream_t s, const int32_t* mats = nullptr);
 
 // device view of a grid (passed by value to kernels)
 struct GridView {
@@ -272,14 +272,18 @@ k_refine_residual(GridView g, PointParams pp, int ee, const int* __restrict__ ac
                   const double* __restrict__ h, const double* __restrict__ F, const double* __restrict__ aux,
                   const double* __restrict__ scal, const double* __restrict__ x, int ldd, double beta_scale,
                   const double* __restrict__ rowscale, float* __restrict__ rs, double* __restrict__ sigma,
-                  const int* __restrict__ done, const double* __restrict__ kc) {
+                  const int* __restrict__ done, const double* __restrict__ kc, const int* __restrict__ slots,
+                  int matvec, const double* __restrict__ xlist, int ldx, double* __restrict__ out64) {
+    // slots (optional): CTA i works on slot slots[i]; xlist (optional): x of CTA i at
+    // xlist + i * ldx instead of x[pt * ldd]; matvec: D (J x) instead of D (b - J x);
+    // out64 (optional): the FP64 result of CTA i at out64 + i * (n + 1), and no FP32 output
     extern __shared__ double sm[];
-    const int slot = blockIdx.x;
-    if (slot >= nact) return;
+    if ((int)blockIdx.x >= nact) return;
+    const int slot = slots ? slots[blockIdx.x] : (int)blockIdx.x;
     const int pt = act[slot];
     if (pp.eept) ee = pp.eept[pt];
     const int n = g.n, nsh = g.nsh, nsp = g.nsp, N = n + 1, tid = threadIdx.x, nt = blockDim.x;
-    if (done[pt]) {  // refinement finished for this point: a zero correction
+    if (done && done[pt]) {  // refinement finished for this point: a zero correction
         for (int i = tid; i < N; i += nt) rs[(size_t)slot * N + i] = 0.0f;
         if (tid == 0) sigma[slot] = 0.0;
         return;
@@ -293,7 +297,7 @@ k_refine_residual(GridView g, PointParams pp, int ee, const int* __restrict__ ac
     const double* hp = h + (size_t)pt * n;
     const double* ax = aux + (size_t)pt * 4 * n;
     const double* sc = scal + (size_t)pt * SC_COUNT;
-    for (int i = tid; i < N; i += nt) sx[i] = x[(size_t)pt * ldd + i];
+    for (int i = tid; i < N; i += nt) sx[i] = xlist ? xlist[(size_t)blockIdx.x * ldx + i] : x[(size_t)pt * ldd + i];
     for (int i = tid; i < n; i += nt) sh[i] = hp[i];
     __syncthreads();
     const double n0 = pp.n0[pt], Tg = pp.Tg[pt], E = pp.E[pt], ne = sc[SC_NE];
@@ -383,14 +387,19 @@ k_refine_residual(GridView g, PointParams pp, int ee, const int* __restrict__ ac
             y += ne * gam * c1 + ne * ax[2 * n + r] * dgx;
         }
         y += -beta * g.Mp[r] * sx[n];
-        double rv = (-F[(size_t)pt * n + r] - y) * rowscale[(size_t)slot * N + r];
+        double rv = (matvec ? y : (-F[(size_t)pt * n + r] - y)) * rowscale[(size_t)slot * N + r];
         sr[r] = rv;
         amax = fmax(amax, fabs(rv));
     }
     if (tid == 0) {
-        double rv = (beta * (1.0 - uh) - beta * ux) * rowscale[(size_t)slot * N + n];
+        double rv = (matvec ? beta * ux : (beta * (1.0 - uh) - beta * ux)) * rowscale[(size_t)slot * N + n];
         sr[n] = rv;
         amax = fmax(amax, fabs(rv));
+    }
+    if (out64) {
+        __syncthreads();
+        for (int i = tid; i < N; i += nt) out64[(size_t)blockIdx.x * N + i] = sr[i];
+        return;
     }
     // max-norm for the FP32 scaling
     for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
@@ -461,6 +470,199 @@ __global__ void k_refine_first(int nact, const int* __restrict__ act, const doub
     if (slot >= nact) return;
     int pt = act[slot];
     if (!done[pt] && c_cur[pt] <= first_tol) done[pt] = 1;
+}
+
+// ---------------------------------------------------------------------------------
+// GMRES refinement of the mixed-form Newton step for the points whose plain refinement
+// stalled (the FP32 factors are then too inaccurate for a stationary iteration, but they
+// still cluster the spectrum of the preconditioned operator): right-preconditioned
+// GMRES(GM_M) on D J d = D b from d = 0, the preconditioner the FP32 LU substitution, the
+// operator the matrix-free FP64 Jacobian (k_refine_residual in matvec mode), Arnoldi by
+// classical Gram-Schmidt applied twice in FP64. The preconditioned vectors Z_k are kept, so
+// the step is d = Z y (flexible form: the FP32 substitution need not be an exact linear
+// map). A point whose residual falls below GM_TOL of ||D b|| ends; one above GM_ACCEPT of
+// it after GM_M iterations is handed to the FP64 form. Lists: point i works on slot list[i].
+// ---------------------------------------------------------------------------------
+constexpr int GM_M = 20;
+constexpr int GM_CAP = 512;  // points per GMRES batch
+// GMRES refinement runs for bordered sizes above this. At c2's N = 385 it resolved all but
+// 12 of the ~200 stalled points per step but cost more than their FP64 factorizations
+// (7,580 against 8,210 solves/s: the refined points kept the Newton tail longer); an FP64
+// factorization costs N^3 and a GMRES iteration N^2, so above N = 512 it pays.
+constexpr int GM_MIN_N = 513;
+// status of a point GMRES did not resolve, until all batches are done (k_gm_finalize makes it
+// NEED_FP64); not negative, so the point is not running, and not NEED_FP64, so that a later
+// batch does not collect it again
+constexpr int GM_FAILED_MARK = 1000;
+constexpr double GM_TOL = 1e-8;
+constexpr double GM_ACCEPT = 1e-8;
+
+__global__ void k_gm_collect(int nact, const int* __restrict__ act, int* status, int* list, int* cnt, int cap) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= nact) return;
+    const int pt = act[slot];
+    if (status[pt] != BTE_ST_NEED_FP64) return;
+    const int i = atomicAdd(cnt, 1);
+    if (i < cap) {
+        list[i] = slot;
+        status[pt] = -1;
+    }
+}
+
+// v_0 = r_0 / ||r_0||, g = (||r_0||, 0, ...)
+__global__ void k_gm_start(int ng, int N, const double* __restrict__ W, double* V, double* g, double* bn, int* on) {
+    __shared__ double red[32];
+    const int i = blockIdx.x;
+    if (i >= ng) return;
+    const double* w = W + (size_t)i * N;
+    double ss = 0.0;
+    for (int j = threadIdx.x; j < N; j += blockDim.x) ss += w[j] * w[j];
+    const double b = sqrt(block_sum(ss, red));
+    const double inv = (b > 0.0) ? 1.0 / b : 0.0;
+    double* v = V + (size_t)i * (GM_M + 1) * N;
+    for (int j = threadIdx.x; j < N; j += blockDim.x) v[j] = w[j] * inv;
+    if (threadIdx.x == 0) {
+        bn[i] = b;
+        g[(size_t)i * (GM_M + 1)] = b;
+        on[i] = (b > 0.0) ? 1 : 0;
+    }
+}
+
+// FP32 right-hand side of the substitution: v_k scaled by its max-norm
+__global__ void k_gm_pre(int ng, int N, int k, const double* __restrict__ V, const int* __restrict__ on, float* xf,
+                         double* sig) {
+    __shared__ double red[32];
+    const int i = blockIdx.x;
+    if (i >= ng) return;
+    const double* v = V + ((size_t)i * (GM_M + 1) + k) * N;
+    float* x = xf + (size_t)i * N;
+    if (!on[i]) {
+        for (int j = threadIdx.x; j < N; j += blockDim.x) x[j] = 0.0f;
+        return;
+    }
+    double m = 0.0;
+    for (int j = threadIdx.x; j < N; j += blockDim.x) m = fmax(m, fabs(v[j]));
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double mm = 0.0;
+        for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) mm = fmax(mm, red[w]);
+        red[0] = (mm > 0.0) ? mm : 1.0;
+        sig[i] = red[0];
+    }
+    __syncthreads();
+    const double inv = 1.0 / red[0];
+    for (int j = threadIdx.x; j < N; j += blockDim.x) x[j] = (float)(v[j] * inv);
+}
+
+// z_k = sigma * (FP32 substitution result), kept in FP64
+__global__ void k_gm_post(int ng, int N, int k, const float* __restrict__ xf, const double* __restrict__ sig,
+                          const int* __restrict__ on, double* Z) {
+    const int i = blockIdx.x;
+    if (i >= ng) return;
+    double* z = Z + ((size_t)i * GM_M + k) * N;
+    const double sg = on[i] ? sig[i] : 0.0;
+    for (int j = threadIdx.x; j < N; j += blockDim.x) z[j] = sg * (double)xf[(size_t)i * N + j];
+}
+
+__global__ void k_gm_finalize(int nact, const int* __restrict__ act, int* status) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= nact) return;
+    const int pt = act[slot];
+    if (status[pt] == GM_FAILED_MARK) status[pt] = BTE_ST_NEED_FP64;
+}
+
+// One Arnoldi step on w = D J z_k, the Givens update of the least-squares problem, and for
+// a point that ends, the step d = Z y written to dh (its status set when not accepted).
+__global__ void __launch_bounds__(256)
+k_gm_arnoldi(int ng, int N, int k, const double* __restrict__ W, double* V, double* H, double* cs, double* sn,
+             double* g, const double* __restrict__ bn, int* on, const double* __restrict__ Z,
+             const int* __restrict__ list, const int* __restrict__ act, double* dh, int ldd, int* status, int* active) {
+    extern __shared__ double gw[];  // w (N)
+    __shared__ double red[32];
+    __shared__ double hc[GM_M + 2];
+    __shared__ double yv[GM_M + 1];
+    __shared__ int fin;
+    const int i = blockIdx.x;
+    if (i >= ng || !on[i]) return;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int j = tid; j < N; j += nt) gw[j] = W[(size_t)i * N + j];
+    if (tid < GM_M + 2) hc[tid] = 0.0;
+    __syncthreads();
+    const double* Vi = V + (size_t)i * (GM_M + 1) * N;
+    // classical Gram-Schmidt applied twice: all projections on the same w, then one update
+    __shared__ double pc[GM_M + 1];
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int j = 0; j <= k; ++j) {
+            double d = 0.0;
+            for (int t = tid; t < N; t += nt) d += Vi[(size_t)j * N + t] * gw[t];
+            d = block_sum(d, red);
+            if (tid == 0) pc[j] = d;
+        }
+        __syncthreads();
+        for (int t = tid; t < N; t += nt) {
+            double wt = gw[t];
+            for (int j = 0; j <= k; ++j) wt -= pc[j] * Vi[(size_t)j * N + t];
+            gw[t] = wt;
+        }
+        if (tid == 0)
+            for (int j = 0; j <= k; ++j) hc[j] += pc[j];
+        __syncthreads();
+    }
+    double ss = 0.0;
+    for (int t = tid; t < N; t += nt) ss += gw[t] * gw[t];
+    const double hk1 = sqrt(block_sum(ss, red));
+    double* vk1 = V + ((size_t)i * (GM_M + 1) + k + 1) * N;
+    const double inv = (hk1 > 0.0) ? 1.0 / hk1 : 0.0;
+    for (int t = tid; t < N; t += nt) vk1[t] = gw[t] * inv;
+    if (tid == 0) {
+        double* csi = cs + (size_t)i * GM_M;
+        double* sni = sn + (size_t)i * GM_M;
+        double* gi = g + (size_t)i * (GM_M + 1);
+        hc[k + 1] = hk1;
+        for (int j = 0; j < k; ++j) {
+            const double a = csi[j] * hc[j] + sni[j] * hc[j + 1];
+            hc[j + 1] = -sni[j] * hc[j] + csi[j] * hc[j + 1];
+            hc[j] = a;
+        }
+        const double den = hypot(hc[k], hc[k + 1]);
+        const double c = (den > 0.0) ? hc[k] / den : 1.0, sv = (den > 0.0) ? hc[k + 1] / den : 0.0;
+        csi[k] = c;
+        sni[k] = sv;
+        hc[k] = den;
+        hc[k + 1] = 0.0;
+        gi[k + 1] = -sv * gi[k];
+        gi[k] = c * gi[k];
+        double* Hi = H + ((size_t)i * GM_M + k) * (GM_M + 1);  // column k of R
+        for (int j = 0; j <= k; ++j) Hi[j] = hc[j];
+        const double res = fabs(gi[k + 1]);
+        const bool ok = res <= GM_TOL * bn[i];
+        fin = (ok || k == GM_M - 1 || !(hk1 > 0.0) || !isfinite(res)) ? 1 : 0;
+        if (fin) {
+            // back substitution R y = g over the k + 1 columns
+            for (int j = k; j >= 0; --j) {
+                double sacc = gi[j];
+                for (int l = j + 1; l <= k; ++l) sacc -= H[((size_t)i * GM_M + l) * (GM_M + 1) + j] * yv[l];
+                const double d = H[((size_t)i * GM_M + j) * (GM_M + 1) + j];
+                yv[j] = (d != 0.0) ? sacc / d : 0.0;
+            }
+            const int pt = act[list[i]];
+            if (!(res <= GM_ACCEPT * bn[i])) status[pt] = GM_FAILED_MARK;
+            on[i] = 0;
+        } else {
+            atomicAdd(active, 1);
+        }
+    }
+    __syncthreads();
+    if (!fin) return;
+    const int pt = act[list[i]];
+    const double* Zi = Z + (size_t)i * GM_M * N;
+    for (int t = tid; t < N; t += nt) {
+        double x = 0.0;
+        for (int j = 0; j <= k; ++j) x += yv[j] * Zi[(size_t)j * N + t];
+        dh[(size_t)pt * ldd + t] = x;
+    }
 }
 
 // ---------------------------------------------------------------------------------
@@ -972,13 +1174,21 @@ struct BteWork {
     // P x n x kc_row(nsh), written by k_jacobian and applied by the refinement
     double* kc = nullptr;
     size_t kcbytes = 0;
+    // GMRES refinement of stalled points (mixed form), gm_cap points at a time
+    int gm_cap = 0;
+    size_t gmbytes = 0;
+    double *gm_V = nullptr, *gm_Z = nullptr, *gm_W = nullptr, *gm_H = nullptr, *gm_cs = nullptr, *gm_sn = nullptr;
+    double *gm_g = nullptr, *gm_bn = nullptr, *gm_sig = nullptr;
+    float* gm_xf = nullptr;
+    int32_t *gm_list = nullptr, *gm_on = nullptr, *gm_cnt = nullptr;
     int32_t *piv = nullptr, *info = nullptr, *act = nullptr, *act2 = nullptr, *cnt = nullptr;
     int32_t *searching = nullptr, *accepted = nullptr;
 };
 
 static void free_work(BteWork* w) {
     void* ptrs[] = {w->nit, w->refdone, w->reason, w->corr0, w->corr1, w->ref_r, w->ref_r0, w->rowscale, w->h0, w->srel, w->sigma, w->xs, w->h, w->ht, w->F, w->Ft, w->aux, w->auxt, w->scal, w->scalt, w->dh, w->r, w->rt, w->r0,
-                    w->alpha, w->J, w->kc, w->piv, w->info, w->act, w->act2, w->cnt, w->searching, w->accepted};
+                    w->alpha, w->J, w->kc, w->gm_V, w->gm_Z, w->gm_W, w->gm_H, w->gm_cs, w->gm_sn, w->gm_g, w->gm_bn,
+                    w->gm_sig, w->gm_xf, w->gm_list, w->gm_on, w->gm_cnt, w->piv, w->info, w->act, w->act2, w->cnt, w->searching, w->accepted};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     *w = BteWork();
@@ -1014,7 +1224,10 @@ static int ensure_work(BteWork* w, const BteGrid* g, int P, int prec) {
     size_t jb = (prec == BTE_PREC_MIXED) ? (size_t)std::max(P, 2) * N * ld * sizeof(float)
                                          : (size_t)P * N * ld * sizeof(double);
     const size_t kb = (prec == BTE_PREC_MIXED && g->ee) ? (size_t)P * n * kc_row(g->nsh) * sizeof(double) : 0;
-    if (w->cap >= P && w->n == n && w->jbytes >= jb && w->kcbytes >= kb) return BTE_OK;
+    const int gc = (prec == BTE_PREC_MIXED && N >= GM_MIN_N) ? std::min(P, GM_CAP) : 0;
+    const size_t gmb = (size_t)gc * (((size_t)(2 * GM_M + 2) * N + GM_M * (GM_M + 1) + 3 * GM_M + 4) * sizeof(double) +
+                                     (size_t)N * sizeof(float) + 2 * sizeof(int32_t));
+    if (w->cap >= P && w->n == n && w->jbytes >= jb && w->kcbytes >= kb && w->gm_cap >= gc) return BTE_OK;
     free_work(w);
     auto A = [&](void** p, size_t bytes) -> bool { return cudaMalloc(p, std::max<size_t>(bytes, 8)) == cudaSuccess; };
     size_t pn = (size_t)P * n * sizeof(double);
@@ -1032,12 +1245,26 @@ static int ensure_work(BteWork* w, const BteGrid* g, int P, int prec) {
               A((void**)&w->nit, (size_t)P * sizeof(int32_t)) && A((void**)&w->r, P * sizeof(double)) &&
               A((void**)&w->rt, P * sizeof(double)) && A((void**)&w->r0, P * sizeof(double)) &&
               A((void**)&w->alpha, P * sizeof(double)) && A(&w->J, jb) && (kb == 0 || A((void**)&w->kc, kb)) &&
+              (gc == 0 || (A((void**)&w->gm_V, (size_t)gc * (GM_M + 1) * N * sizeof(double)) &&
+                           A((void**)&w->gm_Z, (size_t)gc * GM_M * N * sizeof(double)) &&
+                           A((void**)&w->gm_W, (size_t)gc * N * sizeof(double)) &&
+                           A((void**)&w->gm_H, (size_t)gc * GM_M * (GM_M + 1) * sizeof(double)) &&
+                           A((void**)&w->gm_cs, (size_t)gc * GM_M * sizeof(double)) &&
+                           A((void**)&w->gm_sn, (size_t)gc * GM_M * sizeof(double)) &&
+                           A((void**)&w->gm_g, (size_t)gc * (GM_M + 1) * sizeof(double)) &&
+                           A((void**)&w->gm_bn, (size_t)gc * sizeof(double)) &&
+                           A((void**)&w->gm_sig, (size_t)gc * sizeof(double)) &&
+                           A((void**)&w->gm_xf, (size_t)gc * N * sizeof(float)) &&
+                           A((void**)&w->gm_list, (size_t)gc * sizeof(int32_t)) &&
+                           A((void**)&w->gm_on, (size_t)gc * sizeof(int32_t)) &&
+                           A((void**)&w->gm_cnt, 4 * sizeof(int32_t)))) &&
               A((void**)&w->piv, (size_t)P * N * sizeof(int32_t)) && A((void**)&w->info, P * sizeof(int32_t)) &&
               A((void**)&w->act, P * sizeof(int32_t)) && A((void**)&w->act2, P * sizeof(int32_t)) &&
               A((void**)&w->cnt, 4 * sizeof(int32_t)) && A((void**)&w->searching, P * sizeof(int32_t)) &&
               A((void**)&w->accepted, P * sizeof(int32_t));
     if (!ok) { free_work(w); return BTE_ERR_ALLOC; }
     w->cap = P; w->n = n; w->jbytes = jb; w->kcbytes = kb; w->prec = prec;
+    w->gm_cap = gc; w->gmbytes = gmb;
     return BTE_OK;
 }
 
@@ -1064,12 +1291,9 @@ static JacSmem jac_smem(const BteGrid* g, int ee) {
         r.bytes += hl;
         r.stage = 1;
     }
-    // opt in above the default 48 KB once per device (the launch fails loudly past the limit)
-    static unsigned set_mask = 0;
-    if (r.bytes > 48 * 1024 && g->device < 32 && !(set_mask & (1u << g->device))) {
-        cudaFuncSetAttribute(k_jacobian<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        set_mask |= 1u << g->device;
-    }
+    // above the default 48 KB the kernel's limit is raised (never lowered); a failure shows
+    // at the launch
+    bte_raise_smem_limit((const void*)k_jacobian<T>, r.bytes);
     return r;
 }
 
@@ -1268,6 +1492,73 @@ struct Lane {
     double* kc;  // e-e row coefficients by slot (refined lanes), else null
 };
 
+// GMRES refinement (k_gm_*) of the points of lane L whose plain refinement stalled in this
+// Newton iteration (status NEED_FP64 after the refinement passes), gm_cap points at a time.
+// Each such point gets the step d = Z y from d = 0, or keeps NEED_FP64 when GMRES does not
+// reach GM_ACCEPT. The Jacobian factors, row scales and e-e coefficients of the iteration
+// are those the plain refinement used.
+static cudaError_t gmres_refine(SolveCtx& c, Lane& L, int nact) {
+    BteWork* w = c.w;
+    const int N = c.N, ld = c.ld, ldd = c.ldd, ee = c.ee;
+    cudaStream_t s = c.s;
+    Profiler& pf = g_prof;
+    cudaError_t e = cudaSuccess;
+#define GMCK(x, what)                                                                            \
+    do {                                                                                         \
+        cudaError_t _e = (x);                                                                    \
+        if (_e != cudaSuccess) {                                                                 \
+            fprintf(stderr, "bte: GMRES refinement, %s: %s\n", what, cudaGetErrorString(_e));    \
+            return _e;                                                                           \
+        }                                                                                        \
+    } while (0)
+    for (int round = 0; round < 64; ++round) {
+        GMCK(cudaMemsetAsync(w->gm_cnt, 0, 2 * sizeof(int32_t), s), "clear counters");
+        k_gm_collect<<<nblk(nact, 256), 256, 0, s>>>(nact, L.act, c.status, w->gm_list, w->gm_cnt, w->gm_cap);
+        GMCK(cudaGetLastError(), "collect");
+        int hc[2] = {0, 0};
+        GMCK(cudaMemcpyAsync(hc, w->gm_cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, s), "read count");
+        GMCK(cudaStreamSynchronize(s), "sync after collect");
+        const int ng = std::min(hc[0], w->gm_cap);
+        if (ng <= 0) break;
+        const size_t zb = (size_t)ng * GM_M * N * sizeof(double);
+        GMCK(pf.run(PF_REFINE, s, 0, 0, 2, [&] {
+            // r0 = D b (d = 0): the first preconditioned vector is still zero
+            cudaMemsetAsync(w->gm_Z, 0, zb, s);
+            k_refine_residual<<<ng, 256, c.ref_smem, s>>>(c.gv, c.pp, ee, L.act, ng, w->h, w->F, w->aux, w->scal, w->dh,
+                                                          ldd, c.beta_scale, L.rowscale, nullptr, nullptr, nullptr,
+                                                          L.kc, w->gm_list, 0, w->gm_Z, GM_M * N, w->gm_W);
+            k_gm_start<<<ng, 256, 0, s>>>(ng, N, w->gm_W, w->gm_V, w->gm_g, w->gm_bn, w->gm_on);
+        }), "start");
+        const size_t arn_smem = (size_t)N * sizeof(double);
+        GMCK(bte_raise_smem_limit((const void*)k_gm_arnoldi, arn_smem), "shared memory limit");
+        for (int k = 0; k < GM_M; ++k) {
+            cudaError_t le = cudaSuccess;
+            GMCK(pf.run(PF_REFINE, s, 0, 0, 5, [&] {
+                k_gm_pre<<<ng, 256, 0, s>>>(ng, N, k, w->gm_V, w->gm_on, w->gm_xf, w->gm_sig);
+                le = bte_lu_solve_t<float>(ng, N, (const float*)L.J, ld, c.jstride, L.piv, w->gm_xf, 0, s, w->gm_list);
+                k_gm_post<<<ng, 256, 0, s>>>(ng, N, k, w->gm_xf, w->gm_sig, w->gm_on, w->gm_Z);
+                k_refine_residual<<<ng, 256, c.ref_smem, s>>>(c.gv, c.pp, ee, L.act, ng, w->h, w->F, w->aux, w->scal,
+                                                              w->dh, ldd, c.beta_scale, L.rowscale, nullptr, nullptr,
+                                                              nullptr, L.kc, w->gm_list, 1, w->gm_Z + (size_t)k * N,
+                                                              GM_M * N, w->gm_W);
+                cudaMemsetAsync(w->gm_cnt + 1, 0, sizeof(int32_t), s);
+                k_gm_arnoldi<<<ng, 256, arn_smem, s>>>(ng, N, k, w->gm_W, w->gm_V, w->gm_H, w->gm_cs, w->gm_sn, w->gm_g,
+                                                       w->gm_bn, w->gm_on, w->gm_Z, w->gm_list, L.act, w->dh, ldd,
+                                                       c.status, w->gm_cnt + 1);
+            }), "iteration");
+            GMCK(le, "substitution");
+            int left = 0;
+            GMCK(cudaMemcpyAsync(&left, w->gm_cnt + 1, sizeof(int32_t), cudaMemcpyDeviceToHost, s), "read active");
+            GMCK(cudaStreamSynchronize(s), "sync after iteration");
+            if (left == 0) break;
+        }
+        if (hc[0] <= w->gm_cap) break;  // every stalled point had a place in this batch
+    }
+#undef GMCK
+    k_gm_finalize<<<nblk(nact, 256), 256, 0, s>>>(nact, L.act, c.status);
+    return cudaGetLastError();
+}
+
 // One Newton iteration (Jacobian, factorization, step, refinement, line search, acceptance,
 // convergence test) for the `nact` points of lane L whose F, aux, scal and r are current;
 // returns the points still running, whose list is then L.act (the list before the
@@ -1325,7 +1616,8 @@ static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
                            nact * (res_bytes_pt(g, true) + 0.5 * N * (N + 1) * wsz), 3, [&] {
                     k_refine_residual<<<nact, 256, ref_smem, s>>>(gv, pp, ee, L.act, nact, w->h, w->F, w->aux,
                                                                   w->scal, w->dh, ldd, beta_scale, L.rowscale, xs,
-                                                                  L.sigma, w->refdone, L.kc);
+                                                                  L.sigma, w->refdone, L.kc, nullptr, 0, nullptr, 0,
+                                                                  nullptr);
                     le = bte_lu_solve_t<float>(nact, N, (const float*)L.J, ld, jstride, L.piv, xs, 0, s);
                     k_refine_update<<<nact, 128, 0, s>>>(nact, L.act, N, xs, L.sigma, w->dh, ldd, ccur,
                                                          w->refdone);
@@ -1339,6 +1631,8 @@ static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
                                                                        rf + 1 == nrefine);
                     }));
             }
+            // points whose refinement stalled: GMRES on the same FP32 factors before any FP64 hand-over
+            if (nrefine > 0 && w->gm_cap > 0) CKR(gmres_refine(c, L, nact));
         } else {
             double* xs = L.xs;
             CKR(pf.run(PF_JACOBIAN, s, nact * jac_flops_pt(g, ee), jb, 1, [&] {
@@ -1420,8 +1714,8 @@ int bte_solve_impl(BteGrid* g, int P, const double* n0, const double* ne, const 
     c.ref_smem = (size_t)(5 * c.n + 2) * sizeof(double);  // x, r: n + 1 each; h, HL x, GL x: n each
     c.o = o; c.status = status; c.iters = iters; c.s = s;
     const int n = c.n;
-    if (c.res_smem > 48 * 1024) CKR(cudaFuncSetAttribute(k_residual, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.res_smem));
-    if (c.ref_smem > 48 * 1024) CKR(cudaFuncSetAttribute(k_refine_residual, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.ref_smem));
+    CKR(bte_raise_smem_limit((const void*)k_residual, c.res_smem));
+    CKR(bte_raise_smem_limit((const void*)k_refine_residual, c.ref_smem));
     Profiler& pf = g_prof;
     Lane L{w->act, w->act2, w->J, w->piv, w->info, w->xs, w->rowscale, w->sigma, w->kc};
     auto other = [&](auto&& fn) { return pf.run(PF_OTHER, s, 0, 0, 1, fn); };
@@ -1441,7 +1735,7 @@ int bte_solve_impl(BteGrid* g, int P, const double* n0, const double* ne, const 
     CKR(residual_all(P));
     CKR(cudaMemcpyAsync(w->r0, w->r, P * sizeof(double), cudaMemcpyDeviceToDevice, s));
     const size_t rm_smem = (size_t)2 * n * sizeof(double);
-    if (rm_smem > 48 * 1024) CKR(cudaFuncSetAttribute(k_ref_merit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rm_smem));
+    CKR(bte_raise_smem_limit((const void*)k_ref_merit, rm_smem));
     CKR(other([&] { k_ref_merit<<<P, 256, rm_smem, s>>>(c.gv, P, nullptr, w->F, w->ref_r0); }));
     for (int it = 0, nact = P; it < o->max_iter && nact > 0; ++it) {
         nact = newton_iteration(c, L, nact, prec);
@@ -1661,7 +1955,7 @@ int bte_engine_create_impl(BteGrid* g, int cap, int fcap, const bte_solve_opts* 
     const int n = g->n, N = n + 1, ld = (N + 1 + 3) & ~3;
     int rc = ensure_work(&e->w, g, cap, e->prec);
     if (rc) { delete e; return rc; }
-    e->bytes = e->w.jbytes + e->w.kcbytes + (size_t)cap * (size_t)(n * 12 + (N + 1) * 3 + 24) * sizeof(double);  // J + per-slot vectors
+    e->bytes = e->w.jbytes + e->w.kcbytes + e->w.gmbytes + (size_t)cap * (size_t)(n * 12 + (N + 1) * 3 + 24) * sizeof(double);  // J + per-slot vectors
     bool ok = true;
     auto A = [&](void** p, size_t bytes) {
         if (!ok) return;
@@ -1690,10 +1984,10 @@ int bte_engine_create_impl(BteGrid* g, int cap, int fcap, const bte_solve_opts* 
     e->free_slots.resize(cap);
     for (int i = 0; i < cap; ++i) e->free_slots[i] = cap - 1 - i;  // pop_back hands out 0, 1, 2, ...
     SolveCtx c = engine_ctx(e, 0);
-    if (c.res_smem > 48 * 1024) cudaFuncSetAttribute(k_residual, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.res_smem);
-    if (c.ref_smem > 48 * 1024) cudaFuncSetAttribute(k_refine_residual, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.ref_smem);
+    if (bte_raise_smem_limit((const void*)k_residual, c.res_smem) != cudaSuccess) { engine_free(e); delete e; return BTE_ERR_CUDA; }
+    if (bte_raise_smem_limit((const void*)k_refine_residual, c.ref_smem) != cudaSuccess) { engine_free(e); delete e; return BTE_ERR_CUDA; }
     const size_t rm_smem = (size_t)2 * n * sizeof(double);
-    if (rm_smem > 48 * 1024) cudaFuncSetAttribute(k_ref_merit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rm_smem);
+    if (bte_raise_smem_limit((const void*)k_ref_merit, rm_smem) != cudaSuccess) { engine_free(e); delete e; return BTE_ERR_CUDA; }
     *out = e;
     return BTE_OK;
 }
@@ -1986,9 +2280,9 @@ int bte_transient_impl(BteGrid* g, int P, const double* n0, const double* ne, co
     c.beta_scale = g->q0max / (g->umax > 0 ? g->umax : 1.0);
     c.res_smem = (size_t)5 * n * sizeof(double);
     c.o = &so; c.status = status; c.iters = iters; c.s = s;
-    if (c.res_smem > 48 * 1024) CKR(cudaFuncSetAttribute(k_residual, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.res_smem));
+    CKR(bte_raise_smem_limit((const void*)k_residual, c.res_smem));
     const size_t rm_smem = (size_t)2 * n * sizeof(double);
-    if (rm_smem > 48 * 1024) CKR(cudaFuncSetAttribute(k_ref_merit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rm_smem));
+    CKR(bte_raise_smem_limit((const void*)k_ref_merit, rm_smem));
     Profiler& pf = g_prof;
     auto other = [&](auto&& fn) { return pf.run(PF_OTHER, s, 0, 0, 1, fn); };
     const int harmonic = o->efreq > 0 ? 1 : 0;
