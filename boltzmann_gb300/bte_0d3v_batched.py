@@ -14,6 +14,9 @@ Differences a caller can observe:
     `qoi["status"]` / `qoi["iters"]` report each point's outcome instead of printing;
   * `args.precision` selects "fp64" (plain, default) or "mixed" (FP32 Jacobian
     factorizations against the FP64 residual);
+  * `args.krylov` (mixed form) chooses when a point whose FP64 refinement stalls gets
+    GMRES on its FP32 factors before it goes to FP64: 0 for bordered sizes above 512
+    (default), 1 always, 2 for every point (diagnostics), -1 never;
   * failures raise RuntimeError instead of calling sys.exit.
 """
 from __future__ import annotations
@@ -300,7 +303,8 @@ class bte_0d3v_batched:
         opts = _lib.SolveOpts(atol=float(atol), rtol=float(rtol), max_iter=int(max_iter), alpha_min=float(alpha_min),
                               alpha_rho=float(alpha_rho), line_search_c=float(line_search_c),
                               ee=int(getattr(self._args, "ee_collisions", 0)), precision=self._precision(),
-                              refine=int(getattr(self._args, "refine", 4)))
+                              refine=int(getattr(self._args, "refine", 4)),
+                              krylov=int(getattr(self._args, "krylov", 0)))
         stream = torch.cuda.current_stream().cuda_stream
         _lib.check(_lib.load().bte_solve_steady(self._grid[grid_idx], n_pts, _ptr(n0), _ptr(ne), _ptr(ns), _ptr(Tg),
                                                 _ptr(E), _ptr(f), _ptr(status), _ptr(iters), C.byref(opts),

@@ -497,11 +497,13 @@ constexpr int GM_FAILED_MARK = 1000;
 constexpr double GM_TOL = 1e-8;
 constexpr double GM_ACCEPT = 1e-8;
 
-__global__ void k_gm_collect(int nact, const int* __restrict__ act, int* status, int* list, int* cnt, int cap) {
+// all: every running point as well (the diagnostic mode krylov = 2), first batch only
+__global__ void k_gm_collect(int nact, const int* __restrict__ act, int* status, int* list, int* cnt, int cap,
+                             bool all) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= nact) return;
     const int pt = act[slot];
-    if (status[pt] != BTE_ST_NEED_FP64) return;
+    if (status[pt] != BTE_ST_NEED_FP64 && !(all && status[pt] < 0)) return;
     const int i = atomicAdd(cnt, 1);
     if (i < cap) {
         list[i] = slot;
@@ -1216,7 +1218,7 @@ static GridView view_of(const BteGrid* g) {
 
 #define CKR(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) { fprintf(stderr, "bte: %s at %s:%d\n", cudaGetErrorString(_e), __FILE__, __LINE__); return BTE_ERR_CUDA; } } while (0)
 
-static int ensure_work(BteWork* w, const BteGrid* g, int P, int prec) {
+static int ensure_work(BteWork* w, const BteGrid* g, int P, int prec, int krylov = 0) {
     const int n = g->n, N = n + 1;
     const int ld = (N + 1 + 3) & ~3;  // row length of the augmented matrix, padded
     // the mixed form's FP64 pass reuses this buffer for FP64 matrices, half as many: it holds
@@ -1224,7 +1226,8 @@ static int ensure_work(BteWork* w, const BteGrid* g, int P, int prec) {
     size_t jb = (prec == BTE_PREC_MIXED) ? (size_t)std::max(P, 2) * N * ld * sizeof(float)
                                          : (size_t)P * N * ld * sizeof(double);
     const size_t kb = (prec == BTE_PREC_MIXED && g->ee) ? (size_t)P * n * kc_row(g->nsh) * sizeof(double) : 0;
-    const int gc = (prec == BTE_PREC_MIXED && N >= GM_MIN_N) ? std::min(P, GM_CAP) : 0;
+    const bool gm = prec == BTE_PREC_MIXED && (krylov > 0 || (krylov == 0 && N >= GM_MIN_N));
+    const int gc = gm ? std::min(P, GM_CAP) : 0;
     const size_t gmb = (size_t)gc * (((size_t)(2 * GM_M + 2) * N + GM_M * (GM_M + 1) + 3 * GM_M + 4) * sizeof(double) +
                                      (size_t)N * sizeof(float) + 2 * sizeof(int32_t));
     if (w->cap >= P && w->n == n && w->jbytes >= jb && w->kcbytes >= kb && w->gm_cap >= gc) return BTE_OK;
@@ -1497,7 +1500,7 @@ struct Lane {
 // Each such point gets the step d = Z y from d = 0, or keeps NEED_FP64 when GMRES does not
 // reach GM_ACCEPT. The Jacobian factors, row scales and e-e coefficients of the iteration
 // are those the plain refinement used.
-static cudaError_t gmres_refine(SolveCtx& c, Lane& L, int nact) {
+static cudaError_t gmres_refine(SolveCtx& c, Lane& L, int nact, bool all) {
     BteWork* w = c.w;
     const int N = c.N, ld = c.ld, ldd = c.ldd, ee = c.ee;
     cudaStream_t s = c.s;
@@ -1513,7 +1516,8 @@ static cudaError_t gmres_refine(SolveCtx& c, Lane& L, int nact) {
     } while (0)
     for (int round = 0; round < 64; ++round) {
         GMCK(cudaMemsetAsync(w->gm_cnt, 0, 2 * sizeof(int32_t), s), "clear counters");
-        k_gm_collect<<<nblk(nact, 256), 256, 0, s>>>(nact, L.act, c.status, w->gm_list, w->gm_cnt, w->gm_cap);
+        k_gm_collect<<<nblk(nact, 256), 256, 0, s>>>(nact, L.act, c.status, w->gm_list, w->gm_cnt, w->gm_cap,
+                                                     all && round == 0);
         GMCK(cudaGetLastError(), "collect");
         int hc[2] = {0, 0};
         GMCK(cudaMemcpyAsync(hc, w->gm_cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, s), "read count");
@@ -1632,7 +1636,8 @@ static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
                     }));
             }
             // points whose refinement stalled: GMRES on the same FP32 factors before any FP64 hand-over
-            if (nrefine > 0 && w->gm_cap > 0) CKR(gmres_refine(c, L, nact));
+            if (nrefine > 0 && w->gm_cap > 0 && o->krylov >= 0 && (o->krylov > 0 || N >= GM_MIN_N))
+                CKR(gmres_refine(c, L, nact, o->krylov == 2));
         } else {
             double* xs = L.xs;
             CKR(pf.run(PF_JACOBIAN, s, nact * jac_flops_pt(g, ee), jb, 1, [&] {
@@ -1701,7 +1706,7 @@ int bte_solve_impl(BteGrid* g, int P, const double* n0, const double* ne, const 
     if (P <= 0) return BTE_OK;
     BteWork* w = bte_work_get(g);
     const int prec = o->precision;
-    int rc = ensure_work(w, g, P, prec);
+    int rc = ensure_work(w, g, P, prec, o->krylov);
     if (rc) return rc;
     SolveCtx c{};
     c.g = g; c.w = w; c.gv = view_of(g); c.pp = PointParams{n0, ne, Tg, E, ns_by_n0, P};
@@ -1953,7 +1958,7 @@ int bte_engine_create_impl(BteGrid* g, int cap, int fcap, const bte_solve_opts* 
     e->g = g; e->cap = cap; e->prec = o->precision; e->opts = *o;
     e->fcap = (o->precision == BTE_PREC_MIXED) ? std::max(1, std::min(fcap, cap)) : 0;
     const int n = g->n, N = n + 1, ld = (N + 1 + 3) & ~3;
-    int rc = ensure_work(&e->w, g, cap, e->prec);
+    int rc = ensure_work(&e->w, g, cap, e->prec, o->krylov);
     if (rc) { delete e; return rc; }
     e->bytes = e->w.jbytes + e->w.kcbytes + e->w.gmbytes + (size_t)cap * (size_t)(n * 12 + (N + 1) * 3 + 24) * sizeof(double);  // J + per-slot vectors
     bool ok = true;

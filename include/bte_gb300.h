@@ -70,7 +70,13 @@ typedef struct {
                                      Newton step (0-8); a point stops once its correction
                                      contracts 4x, and goes to the FP64 path if it does not
                                      contract at all                                          */
-    int reserved[5];
+    int krylov;                   /* mixed form: GMRES on the FP32 factors for a point whose
+                                     refinement does not contract, before it goes to the FP64
+                                     path. 0: for bordered sizes n + 1 > 512 (default);
+                                     1: for every size; 2: for every point of every Newton
+                                     step (diagnostics); -1: never. No counterpart in the
+                                     reference, which inverts in FP64                         */
+    int reserved[4];
 } bte_solve_opts;
 
 /* Options of the transient solve (the reference's args.dt / cycles / Efreq). */

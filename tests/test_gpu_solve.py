@@ -106,3 +106,31 @@ def test_mixed_handover_small_batches(synthetic_xs, n_pts):
         out[precision] = (np.asarray(ff), np.asarray(qoi["status"]))
     np.testing.assert_array_equal(out["mixed"][1], out["fp64"][1])
     assert float(np.max(rel_l2_cols(out["mixed"][0], out["fp64"][0]))) < 1e-8
+
+
+def test_fp64_ee_jacobian_near_default_shared_limit(synthetic_xs):
+    """64 B-splines x l_max 3 with e-e on: the FP64 Jacobian kernel asks for 48,336 bytes of
+    dynamic shared memory, between its default limit (48 KB minus its static shared memory)
+    and 48 KB; the launch needs the raised limit."""
+    from boltzmann_gb300.workloads import batch_parameters
+    prm = batch_parameters(2, 41)
+    s, args = gpu_solver(synthetic_xs, 64, 3, True, 2, precision="fp64")
+    ff, qoi = gpu_solution(s, args, prm, True, 2)
+    assert np.all(np.asarray(qoi["status"]) <= 1)
+    assert np.all(np.isfinite(np.asarray(ff)))
+
+
+def test_mixed_gmres_refinement_matches_fp64(synthetic_xs):
+    """The mixed form with every Newton step solved by GMRES on the FP32 factors (krylov = 2)
+    converges to the plain FP64 solution."""
+    from boltzmann_gb300.workloads import batch_parameters
+    n_pts = 6
+    prm = batch_parameters(n_pts, 43)
+    out = {}
+    for precision in ("mixed", "fp64"):
+        s, args = gpu_solver(synthetic_xs, 40, 2, True, n_pts, precision=precision)
+        args.krylov = 2
+        ff, qoi = gpu_solution(s, args, prm, True, n_pts)
+        out[precision] = (np.asarray(ff), np.asarray(qoi["status"]))
+    assert np.all(out["mixed"][1] <= 1) and np.all(out["fp64"][1] <= 1)
+    assert float(np.max(rel_l2_cols(out["mixed"][0], out["fp64"][0]))) < 1e-8
