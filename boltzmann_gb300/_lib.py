@@ -25,7 +25,9 @@ EXPORTED = ["bte_grid_create", "bte_grid_destroy", "bte_grid_info", "bte_grid_ex
             "bte_radial_components", "bte_stats_reset", "bte_stats", "bte_solve_info", "bte_lu_factor_ex",
             "bte_engine_create", "bte_engine_destroy", "bte_engine_admit", "bte_engine_step", "bte_engine_collect",
             "bte_engine_info", "bte_solve_transient", "bte1d_create", "bte1d_destroy", "bte1d_step_x", "bte1d_step_v", "bte1d_lmat", "bte1d_block_solve",
-            "bte1d_ords_to_lm", "bte1d_lm_to_ords", "bte1d_launches", "bte1d_last_error"]
+            "bte1d_ords_to_lm", "bte1d_lm_to_ords", "bte1d_launches", "bte1d_last_error",
+            "bte_bidiag_solve", "bte_banded_tri_solve", "bte_banded_tri_mv", "bte_adv_be_sweep",
+            "bte_bsr_upper_unit_solve", "bte_sweep_last_error"]
 
 STAT_FAMILIES = ["residual", "jacobian", "lu_factor", "lu_solve", "refine", "other"]
 
@@ -109,6 +111,13 @@ def load() -> C.CDLL:
     if hasattr(lib, "bte_radial_components"):
         lib.bte_radial_components.argtypes = [vp, C.c_int, vp, C.c_int, vp, vp, vp]
     lib.bte_solve_transient.argtypes = [vp, C.c_int] + [vp] * 11 + [C.POINTER(TransientOpts), vp]
+    ci = C.c_int
+    lib.bte_bidiag_solve.argtypes = [ci, ci, vp, vp, vp, vp, ci, vp]
+    lib.bte_banded_tri_solve.argtypes = [ci, ci, ci, vp, vp, vp, ci, vp]
+    lib.bte_banded_tri_mv.argtypes = [ci, ci, ci, vp, vp, vp, ci, vp]
+    lib.bte_adv_be_sweep.argtypes = [ci, vp, vp, vp, vp, C.c_double, vp, vp, ci, ci, ci, ci, vp]
+    lib.bte_bsr_upper_unit_solve.argtypes = [ci, ci, ci, vp, vp, vp, vp, vp, vp]
+    lib.bte_sweep_last_error.restype = C.c_char_p
     _lib = lib
     return lib
 
