@@ -90,6 +90,11 @@ def _adv(kind, D_LtoR, D_RtoL, c1, c2, dt, b, out, ndiags, Nr, Nvt, Nx, name):
         raise ValueError("out must be a contiguous float64 CUDA tensor of b's size")
     if b.numel() != Nr * Nvt * Nx:
         raise ValueError("b must hold Nr * Nvt * Nx values")
+    N = (Nr, Nvt, Nx)[kind]
+    if D_LtoR.numel() != ndiags * N or D_RtoL.numel() != ndiags * N:
+        raise ValueError("D_LtoR and D_RtoL must be (ndiags, %d)" % N)
+    if c1.numel() != (Nx, Nx, Nr)[kind] or c2.numel() != (Nvt, Nr, Nvt)[kind]:
+        raise ValueError("coefficient vectors of the wrong length")
     _check(_lib.load().bte_adv_be_sweep(kind, _ptr(D_LtoR), _ptr(D_RtoL), _ptr(c1), _ptr(c2), float(dt), _ptr(b),
                                         _ptr(out), int(ndiags), int(Nr), int(Nvt), int(Nx), _stream()), name)
 
