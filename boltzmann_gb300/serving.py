@@ -168,12 +168,14 @@ class BteServer:
     grids: list of (n_sp, l_max); every grid is assembled once (with e-e operators) from
     `lxcat_file` and stays resident. hbm_budget_bytes bounds the device memory of the points
     admitted at any time (a request larger than the whole budget is admitted alone).
-    `backend_factory(key)` may replace the CUDA engine (used by host-only tests).
+    `backend_factory(key)` may replace the CUDA engine (used by host-only tests). refine and
+    krylov are the mixed form's refinement options (bte_solve_opts: FP64 refinement passes;
+    GMRES on the FP32 factors for stalled points, 0 = bordered sizes above 512, -1 = never).
     """
 
     def __init__(self, lxcat_file, grids, precision="mixed", hbm_budget_bytes=8 << 30, capacity=1024,
                  fp64_capacity=64, atol=1e-20, rtol=1e-14, max_iter=100, alpha_min=1e-16, alpha_rho=0.5,
-                 line_search_c=1e-4, refine=4, ev_max=80.0, Te=4.0, device=0, backend_factory=None):
+                 line_search_c=1e-4, refine=4, ev_max=80.0, Te=4.0, device=0, backend_factory=None, krylov=0):
         self.budget = int(hbm_budget_bytes)
         self.used = 0
         self.peak_used = 0
@@ -205,7 +207,7 @@ class BteServer:
                                   alpha_min=float(alpha_min), alpha_rho=float(alpha_rho),
                                   line_search_c=float(line_search_c), ee=1,
                                   precision=_lib.PREC_MIXED if precision == "mixed" else _lib.PREC_FP64,
-                                  refine=int(refine))
+                                  refine=int(refine), krylov=int(krylov))
             for i, k in enumerate(keys):
                 be = EngineBackend(s._grid[i], s._grid_info[i], capacity, fp64_capacity, opts, device)
                 self._workers[k] = _Worker(k, be)
