@@ -53,8 +53,9 @@ def parse():
     ap.add_argument("--serve-budget-gb", type=float, default=16.0, help="HBM budget of admitted points")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-1d", action="store_true", help="skip the 1D3V (config 4) leg")
-    ap.add_argument("--c5-points", type=int, default=64, help="points of the config-5 sample (0: skip)")
-    ap.add_argument("--c5-plain-points", type=int, default=8)
+    ap.add_argument("--c5-points", type=int, default=256, help="points of the config-5 sample (0: skip)")
+    ap.add_argument("--c5-plain-points", type=int, default=256,
+                    help="points of the plain FP64 run of the config-5 sample (the same points, for a fair ratio)")
     ap.add_argument("--steps-1d", type=int, default=20)
     return ap.parse_args()
 
