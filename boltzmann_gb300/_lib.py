@@ -27,7 +27,8 @@ EXPORTED = ["bte_grid_create", "bte_grid_destroy", "bte_grid_info", "bte_grid_ex
             "bte_engine_info", "bte_solve_transient", "bte1d_create", "bte1d_destroy", "bte1d_step_x", "bte1d_step_v", "bte1d_lmat", "bte1d_block_solve",
             "bte1d_ords_to_lm", "bte1d_lm_to_ords", "bte1d_launches", "bte1d_last_error",
             "bte_bidiag_solve", "bte_banded_tri_solve", "bte_banded_tri_mv", "bte_adv_be_sweep",
-            "bte_bsr_upper_unit_solve", "bte_sweep_last_error"]
+            "bte_bsr_upper_unit_solve", "bte_sweep_last_error", "bte_dgemm_nn", "bte_permute3",
+            "bte_fvm_inflow_zero"]
 
 STAT_FAMILIES = ["residual", "jacobian", "lu_factor", "lu_solve", "refine", "other"]
 
@@ -118,6 +119,9 @@ def load() -> C.CDLL:
     lib.bte_adv_be_sweep.argtypes = [ci, vp, vp, vp, vp, C.c_double, vp, vp, ci, ci, ci, ci, vp]
     lib.bte_bsr_upper_unit_solve.argtypes = [ci, ci, ci, vp, vp, vp, vp, vp, vp]
     lib.bte_sweep_last_error.restype = C.c_char_p
+    lib.bte_dgemm_nn.argtypes = [ci, ci, ci, vp, ci, vp, ci, vp, ci, vp]
+    lib.bte_permute3.argtypes = [ci, ci, ci, ci, ci, ci, vp, vp, vp]
+    lib.bte_fvm_inflow_zero.argtypes = [ci, ci, ci, vp, vp, vp]
     _lib = lib
     return lib
 

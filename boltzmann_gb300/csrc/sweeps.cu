@@ -181,6 +181,67 @@ __global__ void k_bsr_upper_unit(int nbr, int bs, int nrhs, const double* __rest
     }
 }
 
+// C = A B (row-major; A M x K, B K x N), FP64, 32 x 32 output tiles through shared memory:
+// the op-split step's collision solve PmatC v (bte_1d3v_solver.py:1797).
+constexpr int GT = 32;
+__global__ void __launch_bounds__(GT * 8)
+k_dgemm_nn(int M, int N, int K, const double* __restrict__ A, int lda, const double* __restrict__ B, int ldb,
+           double* __restrict__ C, int ldc) {
+    __shared__ double As[GT][GT + 1];
+    __shared__ double Bs[GT][GT + 1];
+    const int tx = threadIdx.x % GT, ty = threadIdx.x / GT;  // 32 x 8 threads, 4 rows each
+    const int row0 = blockIdx.y * GT, col = blockIdx.x * GT + tx;
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int k0 = 0; k0 < K; k0 += GT) {
+        for (int r = ty; r < GT; r += 8) {
+            const int ar = row0 + r, ak = k0 + tx;
+            As[r][tx] = (ar < M && ak < K) ? A[(size_t)ar * lda + ak] : 0.0;
+            const int bk = k0 + r;
+            Bs[r][tx] = (bk < K && col < N) ? B[(size_t)bk * ldb + col] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int kk = 0; kk < GT; ++kk) {
+            const double b = Bs[kk][tx];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) acc[i] += As[ty + 8 * i][kk] * b;
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int r = row0 + ty + 8 * i;
+        if (r < M && col < N) C[(size_t)r * ldc + col] = acc[i];
+    }
+}
+
+// out = in with its three axes reordered: in has dims (d0, d1, d2); output axis a is input
+// axis perm[a] (the op-split step's layout swaps, bte_1d3v_solver.py:1813,1831,1848).
+__global__ void k_permute3(int d0, int d1, int d2, int p0, int p1, int p2, const double* __restrict__ in,
+                           double* __restrict__ out) {
+    const long long n = (long long)d0 * d1 * d2;
+    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= n) return;
+    const int dims[3] = {d0, d1, d2};
+    const int od1 = dims[p1], od2 = dims[p2];
+    const int c = (int)(o % od2), b = (int)((o / od2) % od1), a = (int)(o / ((long long)od1 * od2));
+    int idx[3];
+    idx[p0] = a;
+    idx[p1] = b;
+    idx[p2] = c;
+    out[o] = in[((long long)idx[0] * d1 + idx[1]) * d2 + idx[2]];
+}
+
+// Inflow boundary of the x sweep on v (Nr, Nvt, Nx): zero at the first x point for
+// theta_j <= pi/2, at the last for theta_j > pi/2 (bte_1d3v_solver.py:1839-1840).
+__global__ void k_fvm_inflow_zero(int Nr, int Nvt, int Nx, const double* __restrict__ vt, double* v) {
+    const int line = blockIdx.x * blockDim.x + threadIdx.x;
+    if (line >= Nr * Nvt) return;
+    const int j = line % Nvt;
+    const double half_pi = 0.5 * 3.14159265358979323846;
+    v[(size_t)line * Nx + ((vt[j] <= half_pi) ? 0 : Nx - 1)] = 0.0;
+}
+
 thread_local std::string g_sw_err;
 int sw_fail(const char* msg) {
     g_sw_err = msg;
@@ -252,6 +313,35 @@ int bte_bsr_upper_unit_solve(int nbr, int bs, int nrhs, const double* data, cons
     if (e != cudaSuccess) return sw_fail("bte_bsr_upper_unit_solve: block too large for shared memory");
     k_bsr_upper_unit<<<nrhs, 256, smem, (cudaStream_t)stream>>>(nbr, bs, nrhs, data, indptr, indices, b, out);
     return sw_launched("bte_bsr_upper_unit_solve");
+}
+
+int bte_dgemm_nn(int M, int N, int K, const double* A, int lda, const double* B, int ldb, double* C, int ldc,
+                 void* stream) {
+    if (M < 0 || N < 0 || K < 0 || lda < K || ldb < N || ldc < N) return sw_fail("bte_dgemm_nn: bad sizes");
+    if (M == 0 || N == 0) return 0;
+    if (!A || !B || !C) return sw_fail("bte_dgemm_nn: null pointer");
+    if (C == A || C == B) return sw_fail("bte_dgemm_nn: C must not alias A or B");
+    dim3 grid((unsigned)((N + GT - 1) / GT), (unsigned)((M + GT - 1) / GT));
+    k_dgemm_nn<<<grid, GT * 8, 0, (cudaStream_t)stream>>>(M, N, K, A, lda, B, ldb, C, ldc);
+    return sw_launched("bte_dgemm_nn");
+}
+
+int bte_permute3(int d0, int d1, int d2, int p0, int p1, int p2, const double* in, double* out, void* stream) {
+    if (d0 < 0 || d1 < 0 || d2 < 0) return sw_fail("bte_permute3: bad sizes");
+    const int s = (1 << p0) | (1 << p1) | (1 << p2);
+    if (p0 < 0 || p1 < 0 || p2 < 0 || p0 > 2 || p1 > 2 || p2 > 2 || s != 7) return sw_fail("bte_permute3: perm must reorder 0, 1, 2");
+    const long long n = (long long)d0 * d1 * d2;
+    if (n == 0) return 0;
+    if (!in || !out || in == out) return sw_fail("bte_permute3: null or aliased buffers");
+    k_permute3<<<sw_blocks(n), SW_THREADS, 0, (cudaStream_t)stream>>>(d0, d1, d2, p0, p1, p2, in, out);
+    return sw_launched("bte_permute3");
+}
+
+int bte_fvm_inflow_zero(int Nr, int Nvt, int Nx, const double* vt, double* v, void* stream) {
+    if (Nr < 1 || Nvt < 1 || Nx < 1) return sw_fail("bte_fvm_inflow_zero: bad sizes");
+    if (!vt || !v) return sw_fail("bte_fvm_inflow_zero: null pointer");
+    k_fvm_inflow_zero<<<sw_blocks((long long)Nr * Nvt), SW_THREADS, 0, (cudaStream_t)stream>>>(Nr, Nvt, Nx, vt, v);
+    return sw_launched("bte_fvm_inflow_zero");
 }
 
 }  // extern "C"

@@ -48,6 +48,20 @@ int bte_adv_be_sweep(int kind, const double* D_LtoR, const double* D_RtoL, const
 int bte_bsr_upper_unit_solve(int nbr, int bs, int nrhs, const double* data, const int* indptr, const int* indices,
                              const double* b, double* out, void* stream);
 
+/* C = A B, row-major FP64 (A M x K with row stride lda, B K x N, C M x N); C aliases neither.
+ * The op-split step's dense collision solve PmatC v (bte_1d3v_solver.py:1797). */
+int bte_dgemm_nn(int M, int N, int K, const double* A, int lda, const double* B, int ldb, double* C, int ldc,
+                 void* stream);
+
+/* out = in with its axes reordered: in (d0, d1, d2) contiguous; output axis a is input axis
+ * p_a (a permutation of 0, 1, 2). The op-split step's xp.swapaxes layout changes
+ * (bte_1d3v_solver.py:1813,1831,1848). */
+int bte_permute3(int d0, int d1, int d2, int p0, int p1, int p2, const double* in, double* out, void* stream);
+
+/* Inflow boundary of the x sweep on v (Nr, Nvt, Nx): v[r][j][0] = 0 where vt[j] <= pi/2 and
+ * v[r][j][Nx-1] = 0 where vt[j] > pi/2 (bte_1d3v_solver.py:1839-1840). */
+int bte_fvm_inflow_zero(int Nr, int Nvt, int Nx, const double* vt, double* v, void* stream);
+
 const char* bte_sweep_last_error(void);
 
 #ifdef __cplusplus

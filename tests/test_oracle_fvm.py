@@ -1,0 +1,46 @@
+"""The FVM 1D3V op-split oracle and the sweeps' band storage against the reference's own
+set-up and step (tests/golden/fvm_reference.npz, made by tests/golden/make_golden_fvm.py)."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import bte1d_fvm_oracle as F
+from oracle import sweeps_oracle as S
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "fvm_reference.npz")
+
+
+@pytest.fixture(scope="module")
+def g():
+    return dict(np.load(GOLDEN))
+
+
+def _band_part(D, nd, lower):
+    """D restricted to its first nd diagonals below (lower) or above the main one."""
+    N = D.shape[0]
+    i, j = np.indices((N, N))
+    k = (i - j) if lower else (j - i)
+    return np.where((k >= 0) & (k < nd), D, 0.0)
+
+
+def test_band_storage_is_the_reference_upwind_operators(g):
+    """The sweeps read D[i][i-k] at band[k][i-k] (lower) and D[i][i+k] at band[k][i+k] (upper):
+    the reference's band arrays, read that way, are its dense upwind matrices (v_theta's after
+    the diag(sin theta) factor init() applies, bte_1d3v_solver.py:1449-1450)."""
+    sin_vt = np.diag(np.sin(g["vt"]))
+    for band_l, band_r, DL, DR, nd in (
+            (g["vr_diag_l2r"], g["vr_diag_r2l"], g["Dvr_LtoR"], g["Dvr_RtoL"], int(g["pvr"]) + 1),
+            (g["vt_diag_l2r"], g["vt_diag_r2l"], sin_vt @ g["Dvt_LtoR"], sin_vt @ g["Dvt_RtoL"], int(g["pvt"]) + 1),
+            (g["x_diag_l2r"], g["x_diag_r2l"], g["Dx_LtoR"], g["Dx_RtoL"], int(g["px"]) + 1)):
+        np.testing.assert_allclose(S.band_by_column_to_dense(band_l, True), _band_part(DL, nd, True), rtol=0, atol=1e-12 * np.abs(DL).max())
+        np.testing.assert_allclose(S.band_by_column_to_dense(band_r, False), _band_part(DR, nd, False), rtol=0, atol=1e-12 * np.abs(DR).max())
+        # the upwind stencils fit in the stored band
+        assert np.abs(DL - _band_part(DL, nd, True)).max() <= 1e-12 * np.abs(DL).max()
+        assert np.abs(DR - _band_part(DR, nd, False)).max() <= 1e-12 * np.abs(DR).max()
+
+
+def test_op_split_step_matches_the_reference(g):
+    y = F.op_split_step(g, g["E"], g["v0"], float(g["dt"]))
+    ref = g["step"]
+    assert np.max(np.abs(y - ref)) <= 1e-13 * np.max(np.abs(ref))
