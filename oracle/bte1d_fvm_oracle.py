@@ -17,6 +17,8 @@ pins this composition to the reference's own step.
 """
 from __future__ import annotations
 
+import math
+
 import numpy as np
 
 from . import sweeps_oracle as SO
@@ -44,3 +46,65 @@ def op_split_step(g, E, v, dt, alpha=1.0):
     nd = int(g["px"]) + 1
     y = SO.adv_x_BE(g["x_diag_l2r"][:nd], g["x_diag_r2l"][:nd], ax * vr, cos_vt, h, y.reshape(-1), Nr, Nvt, Nx)
     return y.reshape(Nr * Nvt, Nx)
+
+
+# ----------------------------------------------------------------------------------
+# Set-up: the FVM v-grid and the electron-heavy collision operator on it
+# ----------------------------------------------------------------------------------
+def fvm_vr_grid(basis, spline_qpts):
+    """Radial FVM cells: the B-spline basis's per-interval Gauss-Legendre points and weights
+    (spec_spherical.gl_vr with use_bspline_qgrid, spec_spherical.py:1010-1012)."""
+    return basis.gauss_pn(spline_qpts * basis.num_intervals)
+
+
+def _linear_weights(xs, grid):
+    """Rows: the linear-interpolation weights of the grid values at xs, zero outside
+    [grid[0], grid[-1]] (scipy interp1d, kind linear, fill 0)."""
+    W = np.zeros((len(xs), len(grid)))
+    for k in range(len(grid)):
+        e = np.zeros(len(grid))
+        e[k] = 1.0
+        W[:, k] = np.interp(xs, grid, e, left=0.0, right=0.0)
+    return W
+
+
+def collision_op_fvm(processes, vr, vr_qw, vt, vt_qw, vth, rmax, c_gamma):
+    """Sum over processes of the strong-form binary collision operator on the (v_r, theta) FVM
+    grid, index r * Nvt + j (collision_operator_spherical.py:1334-1437):
+      C f = (gain) - (loss),  loss_r = 4 pi s(v_r), s(v) = v vth sigma(eps(v)) / (4 pi),
+      gain_r = s(v_pre) J(v_r) * [f interpolated at v_pre(v_r)] averaged over theta,
+    with v_pre and J per process: elastic v / sqrt(1 - 2 m/M), J = (1 - 2 m/M)^(-3/2);
+    excitation sqrt(v^2 + (c_gamma/vth)^2 eps_th), J = v_pre / v; ionization
+    sqrt(2 v^2 + (c_gamma/vth)^2 eps_th), J = 4 v_pre / v. Interpolation is linear on the
+    v_r cells, zero below the first cell, and falls linearly from the last cell to 0 at
+    rmax."""
+    nr, nt = len(vr), len(vt)
+    eps = lambda v: (v * vth / c_gamma) ** 2
+    avg = np.tile(2.0 * np.pi * np.asarray(vt_qw), (nt, 1))   # each row: the theta average
+    F = np.zeros((nr * nt, nr * nt))
+    for g in processes:
+        if g.gtype == 0:
+            scale = math.sqrt(1.0 - 2.0 * g.mByM)
+            vpre = vr / scale
+            J = np.full(nr, scale ** -3)
+        elif g.gtype == 1:
+            vpre = np.sqrt(vr ** 2 + (c_gamma / vth) ** 2 * g.threshold)
+            J = vpre / vr
+        elif g.gtype == 2:
+            vpre = np.sqrt(2.0 * vr ** 2 + (c_gamma / vth) ** 2 * g.threshold)
+            J = 4.0 * vpre / vr
+        else:
+            raise NotImplementedError("attachment has no strong-form FVM operator in the reference")
+        s = vr * vth * g.total_cross_section(eps(vr)) / (4.0 * np.pi)
+        s_pre = vpre * vth * g.total_cross_section(eps(vpre)) / (4.0 * np.pi)
+        Lw = _linear_weights(vpre, vr)
+        tail = (vpre > vr[-1]) & (vpre <= rmax)
+        Lw[tail, -1] = (rmax - vpre[tail]) / (rmax - vr[-1])
+        F += np.kron(np.diag(s_pre * J) @ Lw, avg) - 4.0 * np.pi * np.kron(np.diag(s), np.eye(nt))
+    return F
+
+
+def collision_inverse(F, dt, tau, n0, np0):
+    """PmatC = (I - dt tau n0 np0 F)^-1, the op-split step's collision solve
+    (bte_1d3v_solver.py:1346-1375; no gas-temperature term on the FVM grid)."""
+    return np.linalg.inv(np.eye(F.shape[0]) - dt * tau * n0 * np0 * F)

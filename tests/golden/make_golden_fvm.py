@@ -21,6 +21,10 @@ Harness steps, as the reference's own CPU use would need:
   composition: collision solve, layout swaps, inflow zeroing, coefficients and order
   (bte_1d3v_solver.py:1745-1870, type XVTVRC).
 
+The fixture also keeps the collision operator on the FVM grid (op_col_en, from the reference's
+`_Lop_eulerian_strong_form`, collision_operator_spherical.py:1334-1437) with the grid weights,
+n0, np0 and the v-domain, from which the step's PmatC is built.
+
 Writes `fvm_reference.npz`. Usage:  python tests/golden/make_golden_fvm.py
 """
 import os
@@ -98,7 +102,10 @@ def main():
             Dvr_LtoR=dense("upwinded_dx", Nr, "L"), Dvr_RtoL=dense("upwinded_dx", Nr, "R"),
             Dx_LtoR=dense("upwinded_dx", Nx, "L"), Dx_RtoL=dense("upwinded_dx", Nx, "R"),
             Dvt_LtoR=dense("upwinded_dvt", Nvt, "L"), Dvt_RtoL=dense("upwinded_dvt", Nvt, "R"),
-            PmatC=np.asarray(b.PmatC), v0=v0, E=E, step=y)
+            PmatC=np.asarray(b.PmatC), v0=v0, E=E, step=y,
+            op_col_en=np.asarray(b.op_col_en.toarray() if hasattr(b.op_col_en, "toarray") else b.op_col_en),
+            vr_qw=np.asarray(b.grid_info["vr_qw"]), vt_qw=np.asarray(b.grid_info["vt_qw"]), n0=p.n0, np0=p.np0,
+            domain=np.asarray(b.op_spec_sp._basis_p._domain, dtype=np.float64), spline_qpts=p.spline_qpts)
         assert Nr != Nx and Nr != Nvt and Nx != Nvt  # grids told apart by size
         np.savez_compressed(os.path.join(HERE, "fvm_reference.npz"), **{k: v for k, v in out.items()})
         print("wrote fvm_reference.npz: dof_v %d, Nx %d, |step| %.6e" % (Nr * Nvt, Nx, np.linalg.norm(y)))

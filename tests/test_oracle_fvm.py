@@ -44,3 +44,24 @@ def test_op_split_step_matches_the_reference(g):
     y = F.op_split_step(g, g["E"], g["v0"], float(g["dt"]))
     ref = g["step"]
     assert np.max(np.abs(y - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
+def test_collision_operator_and_inverse_on_the_fvm_grid(g, synthetic_xs):
+    """The oracle's FVM grid, strong-form collision operator and PmatC against the reference's
+    (same cross sections: the synthetic LXCat file the fixture was made from)."""
+    from oracle import bte_oracle as O
+    from oracle import bte1d_oracle as O1
+    Nr = int(g["Nr"])
+    ops = O.Operators(O.processes_from_lxcat(synthetic_xs), 80.0, 4.0, 8, 0, ee=False, snap=False)
+    vr, vr_qw = F.fvm_vr_grid(ops.basis, int(g["spline_qpts"]))
+    np.testing.assert_allclose(vr, g["vr"], rtol=1e-14, atol=0)
+    np.testing.assert_allclose(vr_qw, g["vr_qw"], rtol=1e-13, atol=0)
+    vt, vt_qw = O1.gl_vt(int(g["Nvt"]))
+    np.testing.assert_allclose(vt, g["vt"], rtol=1e-14, atol=0)
+    C = F.collision_op_fvm(O.processes_from_lxcat(synthetic_xs), vr, vr_qw, vt, vt_qw, float(g["vth"]),
+                           float(g["domain"][1]), O.C_GAMMA)
+    ref = g["op_col_en"]
+    assert np.max(np.abs(C - ref)) <= 1e-12 * np.max(np.abs(ref))
+    P = F.collision_inverse(ref, float(g["dt"]), float(g["tau"]), float(g["n0"]), float(g["np0"]))
+    assert np.max(np.abs(P - g["PmatC"])) <= 1e-10 * np.max(np.abs(g["PmatC"]))
+    assert len(vr) == Nr
