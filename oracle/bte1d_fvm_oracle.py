@@ -108,3 +108,95 @@ def collision_inverse(F, dt, tau, n0, np0):
     """PmatC = (I - dt tau n0 np0 F)^-1, the op-split step's collision solve
     (bte_1d3v_solver.py:1346-1375; no gas-temperature term on the FVM grid)."""
     return np.linalg.inv(np.eye(F.shape[0]) - dt * tau * n0 * np0 * F)
+
+
+# ----------------------------------------------------------------------------------
+# Set-up: upwind first-derivative operators and their band arrays
+# ----------------------------------------------------------------------------------
+def _lagrange_d1(xs, t):
+    """Weights w_k with sum_k w_k f(xs_k) = p'(t), p the interpolating polynomial of f on the
+    stencil xs: w_k = l_k'(t) = sum_{m != k} 1/(x_k - x_m) prod_{j != k, m} (t - x_j)/(x_k - x_j)."""
+    n = len(xs)
+    w = np.zeros(n)
+    for k in range(n):
+        acc = 0.0
+        for m in range(n):
+            if m == k:
+                continue
+            term = 1.0 / (xs[k] - xs[m])
+            for j in range(n):
+                if j != k and j != m:
+                    term *= (t - xs[j]) / (xs[k] - xs[j])
+            acc += term
+        w[k] = acc
+    return w
+
+
+def upwind_d1(x, sw, direction):
+    """One-sided first derivative on the points x with stencils of sw points (mesh.py:20-55):
+    "L" uses x[i-sw+1 .. i] (shorter near the start, row 0 empty), "R" uses x[i .. i+sw-1]
+    (shorter near the end, row N-1 from the single last point: empty)."""
+    N = len(x)
+    D = np.zeros((N, N))
+    for i in range(N):
+        if direction == "L":
+            lo = max(0, i - (sw - 1))
+            if i > lo:
+                D[i, lo:i + 1] = _lagrange_d1(x[lo:i + 1], x[i])
+        else:
+            hi = min(N, i + sw)
+            if hi - 1 > i:
+                D[i, i:hi] = _lagrange_d1(x[i:hi], x[i])
+    return D
+
+
+def upwind_d1_theta(x, sw, direction):
+    """mesh.py:80-112 without central differences: upwind_d1 within each hemisphere of the
+    ordinates, bridged by a two-point stencil across the equator (row mp for "L", row mp-1
+    for "R", mp = N/2)."""
+    N = len(x)
+    mp = N // 2
+    D = np.zeros((N, N))
+    D[:mp, :mp] = upwind_d1(x[:mp], sw, direction)
+    D[mp:, mp:] = upwind_d1(x[mp:], sw, direction)
+    if direction == "L":
+        D[mp] = 0.0
+        D[mp, mp - 1:mp + 1] = _lagrange_d1(x[mp - 1:mp + 1], x[mp])
+    else:
+        D[mp - 1] = 0.0
+        D[mp - 1, mp - 1:mp + 1] = _lagrange_d1(x[mp - 1:mp + 1], x[mp - 1])
+    return D
+
+
+def bands_by_column(D, nd, lower):
+    """The first nd diagonals of D stored by column, as the sweeps read them: lower
+    band[k][i-k] = D[i][i-k], upper band[k][i+k] = D[i][i+k] (bte_1d3v_solver.py:1452-1462)."""
+    N = D.shape[0]
+    B = np.zeros((nd, N))
+    for k in range(nd):
+        if lower:
+            B[k, :N - k] = np.diagonal(D, offset=-k)
+        else:
+            B[k, k:] = np.diagonal(D, offset=k)
+    return B
+
+
+def fvm_upwind_bands(vr, vt, x, pvr, pvt, px, rmax):
+    """The six band arrays of the op-split sweeps (bte_1d3v_solver.py:1406-1470): upwind
+    operators of stencil width p+1; inflow rows zeroed (first row of "L", last of "R"); the
+    v_r outflow row set to -1 / (rmax - v_r[-1]); theta operators scaled by sin(theta)."""
+    Dvr_L, Dvr_R = upwind_d1(vr, pvr + 1, "L"), upwind_d1(vr, pvr + 1, "R")
+    Dvt_L, Dvt_R = upwind_d1_theta(vt, pvt + 1, "L"), upwind_d1_theta(vt, pvt + 1, "R")
+    Dx_L, Dx_R = upwind_d1(x, px + 1, "L"), upwind_d1(x, px + 1, "R")
+    Dvr_L[0, :] = 0.0
+    Dvr_R[-1, :] = 0.0
+    Dvr_R[-1, -1] = -1.0 / (rmax - vr[-1])
+    Dvt_L[0, :] = 0.0
+    Dvt_R[-1, :] = 0.0
+    Dx_L[0, :] = 0.0
+    Dx_R[-1, :] = 0.0
+    s = np.diag(np.sin(vt))
+    Dvt_L, Dvt_R = s @ Dvt_L, s @ Dvt_R
+    return dict(vr_diag_l2r=bands_by_column(Dvr_L, pvr + 1, True), vr_diag_r2l=bands_by_column(Dvr_R, pvr + 1, False),
+                vt_diag_l2r=bands_by_column(Dvt_L, pvt + 1, True), vt_diag_r2l=bands_by_column(Dvt_R, pvt + 1, False),
+                x_diag_l2r=bands_by_column(Dx_L, px + 1, True), x_diag_r2l=bands_by_column(Dx_R, px + 1, False))

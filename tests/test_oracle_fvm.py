@@ -65,3 +65,24 @@ def test_collision_operator_and_inverse_on_the_fvm_grid(g, synthetic_xs):
     P = F.collision_inverse(ref, float(g["dt"]), float(g["tau"]), float(g["n0"]), float(g["np0"]))
     assert np.max(np.abs(P - g["PmatC"])) <= 1e-10 * np.max(np.abs(g["PmatC"]))
     assert len(vr) == Nr
+
+
+def test_upwind_operators_and_bands(g):
+    """The oracle's upwind derivative operators (own Lagrange weights) and the six band arrays
+    against the reference's (mesh.upwinded_dx / upwinded_dvt through init())."""
+    p = {k: int(g[k]) for k in ("pvr", "pvt", "px")}
+    for D, x, sw, dirn, theta in ((g["Dx_LtoR"], g["x"], p["px"] + 1, "L", False),
+                                  (g["Dx_RtoL"], g["x"], p["px"] + 1, "R", False),
+                                  (g["Dvt_LtoR"], g["vt"], p["pvt"] + 1, "L", True),
+                                  (g["Dvt_RtoL"], g["vt"], p["pvt"] + 1, "R", True)):
+        mine = (F.upwind_d1_theta if theta else F.upwind_d1)(np.asarray(x), sw, dirn)
+        # the captured arrays carry init()'s inflow-row zeroing
+        if dirn == "L":
+            mine[0, :] = 0.0
+        else:
+            mine[-1, :] = 0.0
+        assert np.max(np.abs(mine - D)) <= 1e-9 * np.max(np.abs(D))
+    bands = F.fvm_upwind_bands(g["vr"], g["vt"], g["x"], p["pvr"], p["pvt"], p["px"], float(g["domain"][1]))
+    for k, b in bands.items():
+        ref = g[k]
+        assert np.max(np.abs(b - ref)) <= 1e-9 * np.max(np.abs(ref)), k
