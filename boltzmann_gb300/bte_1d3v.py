@@ -70,9 +70,10 @@ def chebyshev(Np):
     return xp, V1 @ V0inv
 
 
-def load_params(par):
+def load_params(par, fvm=False):
     """The reference's [bte] parameter table (bte_1d3v_solver.py:77-216) from a TOML file path or
-    a dict; returns a namespace with the derived quantities the step uses."""
+    a dict; returns a namespace with the derived quantities the step uses. `fvm`: the table is
+    for the finite-volume v-space (`vspace_type = 0`), with either x-space."""
     if isinstance(par, (str, os.PathLike)):
         import tomllib
         with open(par, "rb") as fh:
@@ -91,7 +92,12 @@ def load_params(par):
     p.l_max = tp["lmax"]
     p.gmres_rsrt_iter = tp.get("gmres_rsrt_iter", 10)
     p.gmres_maxiter = p.gmres_rsrt_iter * tp["gmres_rsrt"]
-    if tp.get("xspace_type", 1) != 1 or tp.get("vspace_type", 1) != 1:
+    if fvm:
+        if tp.get("vspace_type", 1) != 0:
+            raise ValueError("the finite-volume solver needs vspace_type = 0")
+        if tp.get("xspace_type", 1) not in (0, 1):
+            raise NotImplementedError("xspace_type must be 0 (upwind FD) or 1 (Chebyshev)")
+    elif tp.get("xspace_type", 1) != 1 or tp.get("vspace_type", 1) != 1:
         raise NotImplementedError("only the BE Chebyshev x-space and the spectral v-space are provided")
     if tp.get("ev_extend", 0) != 0:
         raise NotImplementedError("only ev_extend = 0 (the v-grid ends at ev_max)")

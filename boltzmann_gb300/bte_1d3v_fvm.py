@@ -1,29 +1,273 @@
-"""The finite-volume 1D3V op-split step on the GPU.
+"""The finite-volume 1D3V solver: its operator set-up and the op-split step on the GPU.
 
-Counterpart of the reference's `bte_1d3v.step_op_split` with type XVTVRC
-(BESolver/python/bte_1d3v_solver.py:1745-1870), the preconditioner step of its fully implicit
-FVM solver, composed from the library's kernels (`include/bte_sweeps_gb300.h`):
+Counterpart of the reference's `bte_1d3v` with the FVM v-space (`vspace_type = 0`,
+BESolver/python/bte_1d3v_solver.py): cells in v_r (the B-spline basis's per-interval Gauss
+points) x discrete ordinates in theta x points in x, v laid out (Nr * Nvt, Nx), radial cell
+major.
+
+Set-up (host, once per dt; the reference builds the same on the host, :377-470,1333-1470):
+* `radial_cells`: the v_r cells and their widths (spec_spherical.gl_vr with use_bspline_qgrid);
+* `upwind_operator` / `upwind_operator_theta`: one-sided first-derivative operators
+  (mesh.upwinded_dx / upwinded_dvt), weights by Fornberg's recursion;
+* `FvmCollisions`: the strong-form electron-heavy operator
+  (collision_operator_spherical.py:1334-1419) kept in its factored form
+  C = G (x) (1 w^T) - diag(l) (x) I, G the (Nr x Nr) gain matrix, w = 2 pi (theta weights),
+  l the loss rates. The collision inverse (I - c C)^-1 then has the closed form
+  D^-1 (x) I + (c D^-1 G (D - c |w| G)^-1) (x) (1 w^T), D = I + c diag(l): an Nr x Nr solve,
+  not the (Nr Nvt)^3 dense inverse (:1346-1375);
+* `fvm_bands`: the six column-stored band arrays of the sweeps (:1403-1470).
+
+Step (`FvmOpSplit`, :1745-1870, type XVTVRC) from the library's kernels
+(`include/bte_sweeps_gb300.h`):
 1. collisions: yc = PmatC v (bte_dgemm_nn);
 2. v_r advection sweeps on (Nx, Nvt, Nr) (bte_adv_be_sweep kind 0, aE = tau qe / (me vth) E);
 3. v_theta advection sweeps on (Nx, Nr, Nvt) (kind 1);
 4. inflow zeroing and x advection sweeps on (Nr, Nvt, Nx) (kind 2, a = vth tau / L v_r cos theta).
-The layout swaps between the stages run through bte_permute3. Layouts are the reference's: v is
-(Nr * Nvt, Nx), radial cell major.
-
-The operators come from the reference's FVM set-up (`init()`): the dense collision inverse
-PmatC and the column-stored upwind bands of v_r, v_theta and x (bte_1d3v_solver.py:1346-1470).
-This module does not assemble them; the FVM operator set-up is the path's next item.
+The layout swaps between the stages run through bte_permute3.
 """
 from __future__ import annotations
 
-import ctypes as C
+import math
 
 import numpy as np
 
 from . import _lib
+from .bte_1d3v import KB, ME, QE, chebyshev, load_params, ordinates
 from .native_kernels import _check, _ptr, _stream
 
+C_GAMMA = math.sqrt(2.0 * QE / ME)   # v = C_GAMMA sqrt(eps [eV])
 
+
+def thermal_velocity(Te_eV):
+    """sqrt(2 k_B T / m_e) at T = Te_eV electron volts (collisions.py:20-25)."""
+    return math.sqrt(2.0 * KB * (Te_eV * QE / KB) / ME)
+
+
+# ----------------------------------------------------------------------------------
+# grids
+# ----------------------------------------------------------------------------------
+def radial_cells(ev_max, Te, Nr, sp_order, spline_qpts):
+    """The v_r cells (in units of vth): `spline_qpts` Gauss-Legendre points in each knot
+    interval of the order-`sp_order` B-spline basis with Nr + 1 functions on uniform knots over
+    [0, sqrt(ev_max) C_GAMMA / vth] (basis.py:414-429,640-653). Returns (vr, widths, vmax)."""
+    vmax = math.sqrt(ev_max) * C_GAMMA / thermal_velocity(Te)
+    n_int = Nr + 1 - sp_order
+    if n_int < 1:
+        raise ValueError("Nr + 1 must exceed sp_order")
+    edges = np.linspace(0.0, vmax, n_int + 1)
+    gx, gw = np.polynomial.legendre.leggauss(int(spline_qpts))
+    half = 0.5 * np.diff(edges)
+    mid = 0.5 * (edges[1:] + edges[:-1])
+    vr = (half[:, None] * gx[None, :] + mid[:, None]).reshape(-1)
+    qw = (half[:, None] * gw[None, :]).reshape(-1)
+    return vr, qw, vmax
+
+
+def x_points(Np, adaptive_grid=1):
+    """x in [-1, 1] (bte_1d3v_solver.py:248-266, mesh.py:129-185; either x-space):
+    Chebyshev-Gauss-Lobatto points when `adaptive_grid`, else uniform."""
+    if adaptive_grid:
+        return chebyshev(Np)[0]
+    return np.linspace(-1.0, 1.0, Np)
+
+
+# ----------------------------------------------------------------------------------
+# upwind first derivatives
+# ----------------------------------------------------------------------------------
+def fd_weights(x0, nodes):
+    """First-derivative weights at x0 on arbitrary nodes: the recursion of B. Fornberg,
+    "Generation of finite difference formulas on arbitrarily spaced grids", Math. Comp. 51
+    (1988) 699-706, carried to derivative order 1. Exact for polynomials of degree < len(nodes)."""
+    z = np.asarray(nodes, dtype=np.float64)
+    n = len(z)
+    c = np.zeros((n, 2))
+    c[0, 0] = 1.0
+    prod_prev = 1.0
+    dz_prev = z[0] - x0
+    for i in range(1, n):
+        prod = 1.0
+        dz_i = z[i] - x0
+        for j in range(i):
+            d = z[i] - z[j]
+            prod *= d
+            if j == i - 1:
+                c[i, 1] = prod_prev * (c[i - 1, 0] - dz_prev * c[i - 1, 1]) / prod
+                c[i, 0] = -prod_prev * dz_prev * c[i - 1, 0] / prod
+            c[j, 1] = (dz_i * c[j, 1] - c[j, 0]) / d
+            c[j, 0] = dz_i * c[j, 0] / d
+        prod_prev = prod
+        dz_prev = dz_i
+    return c[:, 1]
+
+
+def upwind_operator(x, sw, direction):
+    """Dense one-sided first-derivative operator on the points x (mesh.py:20-55): row i uses
+    the up-to-sw points ending at i ("L") or starting at i ("R"); a row with a single point in
+    its stencil (the first of "L", the last of "R") is zero."""
+    x = np.asarray(x, dtype=np.float64)
+    N = len(x)
+    D = np.zeros((N, N))
+    for i in range(N):
+        lo, hi = (max(0, i - sw + 1), i + 1) if direction == "L" else (i, min(N, i + sw))
+        if hi - lo > 1:
+            D[i, lo:hi] = fd_weights(x[i], x[lo:hi])
+    return D
+
+
+def upwind_operator_theta(vt, sw, direction):
+    """The ordinates' operator (mesh.py:80-112 without central differences): `upwind_operator`
+    on each half of the ordinates, with the first row past the equator ("L", row N/2) or the
+    last row before it ("R", row N/2 - 1) a two-point difference across it."""
+    vt = np.asarray(vt, dtype=np.float64)
+    N = len(vt)
+    h = N // 2
+    D = np.zeros((N, N))
+    D[:h, :h] = upwind_operator(vt[:h], sw, direction)
+    D[h:, h:] = upwind_operator(vt[h:], sw, direction)
+    r = h if direction == "L" else h - 1
+    D[r] = 0.0
+    D[r, h - 1:h + 1] = fd_weights(vt[r], vt[h - 1:h + 1])
+    return D
+
+
+def band_columns(D, nd, lower):
+    """The first nd diagonals of D stored the way the sweeps read them: lower
+    band[k][i - k] = D[i][i - k], upper band[k][i + k] = D[i][i + k]."""
+    N = D.shape[0]
+    B = np.zeros((nd, N))
+    for k in range(nd):
+        if lower:
+            B[k, :N - k] = np.diagonal(D, offset=-k)
+        else:
+            B[k, k:] = np.diagonal(D, offset=k)
+    return B
+
+
+def fvm_upwind_operators(vr, vt, x, pvr, pvt, px, vmax):
+    """The dense upwind operators of the FVM solver with their boundary rows (:1406-1452,
+    spec_spherical.py:909-926): inflow rows zero, the last v_r row of "R" the outflow
+    -1 / (vmax - v_r[-1]), theta operators premultiplied by diag(sin theta)."""
+    out = {"Dvr_L": upwind_operator(vr, pvr + 1, "L"), "Dvr_R": upwind_operator(vr, pvr + 1, "R"),
+           "Dvt_L": upwind_operator_theta(vt, pvt + 1, "L"), "Dvt_R": upwind_operator_theta(vt, pvt + 1, "R"),
+           "Dx_L": upwind_operator(x, px + 1, "L"), "Dx_R": upwind_operator(x, px + 1, "R")}
+    for k in ("Dvr_L", "Dvt_L", "Dx_L"):
+        out[k][0, :] = 0.0
+    for k in ("Dvr_R", "Dvt_R", "Dx_R"):
+        out[k][-1, :] = 0.0
+    out["Dvr_R"][-1, -1] = -1.0 / (vmax - vr[-1])
+    s = np.sin(np.asarray(vt))[:, None]
+    out["Dvt_L"] = s * out["Dvt_L"]
+    out["Dvt_R"] = s * out["Dvt_R"]
+    return out
+
+
+def fvm_bands(ops, pvr, pvt, px):
+    """The sweeps' six band arrays (p + 1, N) from `fvm_upwind_operators` (:1452-1470)."""
+    return dict(vr_diag_l2r=band_columns(ops["Dvr_L"], pvr + 1, True),
+                vr_diag_r2l=band_columns(ops["Dvr_R"], pvr + 1, False),
+                vt_diag_l2r=band_columns(ops["Dvt_L"], pvt + 1, True),
+                vt_diag_r2l=band_columns(ops["Dvt_R"], pvt + 1, False),
+                x_diag_l2r=band_columns(ops["Dx_L"], px + 1, True),
+                x_diag_r2l=band_columns(ops["Dx_R"], px + 1, False))
+
+
+# ----------------------------------------------------------------------------------
+# collisions
+# ----------------------------------------------------------------------------------
+_KINDS = {"ELASTIC": 0, "EXCITATION": 1, "IONIZATION": 2}
+
+
+def _sigma(proc, eps):
+    """Tabulated total cross section, linear in energy, held at the end values outside the
+    table (collisions.py:79)."""
+    e = np.asarray(proc["energy"], dtype=np.float64)
+    s = np.asarray(proc["cross section"], dtype=np.float64)
+    return np.interp(eps, e, s, left=s[0], right=s[-1])
+
+
+class FvmCollisions:
+    """C = G (x) (1 w^T) - diag(loss) (x) I on the (v_r cell, ordinate) grid, index
+    r * Nvt + j: gain G (Nr x Nr), loss (Nr), w = 2 pi theta weights (Nvt)."""
+
+    def __init__(self, gain, loss, w):
+        self.gain = np.asarray(gain, dtype=np.float64)
+        self.loss = np.asarray(loss, dtype=np.float64)
+        self.w = np.asarray(w, dtype=np.float64)
+        self.Nr, self.Nvt = len(self.loss), len(self.w)
+
+    def dense(self):
+        return np.kron(self.gain, np.outer(np.ones(self.Nvt), self.w)) - np.kron(np.diag(self.loss), np.eye(self.Nvt))
+
+    def apply(self, v):
+        """C v for v (Nr * Nvt, ...) without forming C."""
+        V = np.asarray(v).reshape((self.Nr, self.Nvt, -1))
+        m = np.einsum("j,rjx->rx", self.w, V)
+        out = (self.gain @ m)[:, None, :] - self.loss[:, None, None] * V
+        return out.reshape(np.shape(v))
+
+    def inverse_factors(self, c):
+        """(dinv, H) with (I - c C)^-1 b = dinv (x) b + (H (x) 1) (w^T b): dinv = 1 / (1 + c loss),
+        H = c D^-1 G (D - c |w| G)^-1."""
+        d = 1.0 + c * self.loss
+        A = np.diag(d) - (c * self.w.sum()) * self.gain
+        H = (c / d)[:, None] * np.linalg.solve(A.T, self.gain.T).T
+        return 1.0 / d, H
+
+    def inverse_dense(self, c):
+        """The dense (I - c C)^-1, the op-split step's PmatC."""
+        dinv, H = self.inverse_factors(c)
+        return np.kron(np.diag(dinv), np.eye(self.Nvt)) + np.kron(H, np.outer(np.ones(self.Nvt), self.w))
+
+
+def fvm_collisions(processes, vr, vt_qw, vth, vmax):
+    """The strong-form binary collision operator on the FVM grid
+    (collision_operator_spherical.py:1334-1419), summed over `processes` (the
+    `read_cross_section_data` dicts; each needs "type", "threshold", "energy", "cross section",
+    and the elastic ones "mass_ratio"). Per process, with s(v) = v vth sigma(eps(v)) / (4 pi):
+    loss 4 pi s(v_r); gain s(v_pre) J times f at v_pre, linearly interpolated between cells,
+    zero below the first cell and falling linearly to 0 at vmax past the last, averaged over
+    theta. v_pre, J: elastic v / sqrt(1 - 2 m/M), (1 - 2 m/M)^(-3/2); excitation
+    sqrt(v^2 + (C_GAMMA/vth)^2 eps_th), v_pre / v; ionization sqrt(2 v^2 + (C_GAMMA/vth)^2
+    eps_th), 4 v_pre / v."""
+    vr = np.asarray(vr, dtype=np.float64)
+    Nr = len(vr)
+    gain = np.zeros((Nr, Nr))
+    loss = np.zeros(Nr)
+    k2 = (C_GAMMA / vth) ** 2
+    for proc in processes:
+        kind = str(proc["type"]).upper()
+        if kind not in _KINDS:
+            raise NotImplementedError("no strong-form FVM operator for %s processes" % kind)
+        if _KINDS[kind] == 0:
+            scale = math.sqrt(1.0 - 2.0 * float(proc["mass_ratio"]))
+            vpre = vr / scale
+            J = np.full(Nr, scale ** -3)
+        elif _KINDS[kind] == 1:
+            vpre = np.sqrt(vr ** 2 + k2 * float(proc["threshold"]))
+            J = vpre / vr
+        else:
+            vpre = np.sqrt(2.0 * vr ** 2 + k2 * float(proc["threshold"]))
+            J = 4.0 * vpre / vr
+        s = vr * vth * _sigma(proc, (vr * vth / C_GAMMA) ** 2) / (4.0 * math.pi)
+        s_pre = vpre * vth * _sigma(proc, (vpre * vth / C_GAMMA) ** 2) / (4.0 * math.pi)
+        # linear interpolation weights of the cell values at v_pre
+        k = np.clip(np.searchsorted(vr, vpre, side="right") - 1, 0, Nr - 2)
+        t = (vpre - vr[k]) / (vr[k + 1] - vr[k])
+        inside = (vpre >= vr[0]) & (vpre <= vr[-1])
+        tail = (vpre > vr[-1]) & (vpre <= vmax)
+        rows = np.arange(Nr)
+        W = np.zeros((Nr, Nr))
+        W[rows[inside], k[inside]] += 1.0 - t[inside]
+        W[rows[inside], k[inside] + 1] += t[inside]
+        W[rows[tail], Nr - 1] = (vmax - vpre[tail]) / (vmax - vr[-1])
+        gain += (s_pre * J)[:, None] * W
+        loss += 4.0 * math.pi * s
+    return gain, loss
+
+
+# ----------------------------------------------------------------------------------
+# the op-split step on the GPU
+# ----------------------------------------------------------------------------------
 class FvmOpSplit:
     """PmatC (dof_v x dof_v), band arrays (p+1, N) of the three directions, grids vr (Nr),
     vt (Nvt), and the coefficients tau, qe, me, vth, L of the reference's parameters."""
@@ -61,6 +305,8 @@ class FvmOpSplit:
         if v.numel() != dof * Nx or not v.is_cuda or v.dtype != torch.float64:
             raise ValueError("v must be a (Nr * Nvt, Nx) float64 CUDA tensor")
         aE = torch.as_tensor(np.asarray(E), dtype=torch.float64, device=self.dev) * self.cE
+        if aE.numel() != Nx:
+            raise ValueError("E must have Nx values")
         h = float(alpha) * float(dt)
         a, b = self._a, self._b
         _check(lib.bte_dgemm_nn(dof, Nx, dof, _ptr(self.P), dof, _ptr(v), Nx, _ptr(a), Nx, s), "collision solve")

@@ -200,3 +200,96 @@ def fvm_upwind_bands(vr, vt, x, pvr, pvt, px, rmax):
     return dict(vr_diag_l2r=bands_by_column(Dvr_L, pvr + 1, True), vr_diag_r2l=bands_by_column(Dvr_R, pvr + 1, False),
                 vt_diag_l2r=bands_by_column(Dvt_L, pvt + 1, True), vt_diag_r2l=bands_by_column(Dvt_R, pvt + 1, False),
                 x_diag_l2r=bands_by_column(Dx_L, px + 1, True), x_diag_r2l=bands_by_column(Dx_R, px + 1, False))
+
+
+# ----------------------------------------------------------------------------------
+# The fully implicit step (bte_1d3v_solver.py:1890-2009)
+# ----------------------------------------------------------------------------------
+def adv_v_fvm(vr, vt, pvr, pvt, rmax):
+    """Dense upwind v-space advection operators for E >= 0 and E < 0 (unscaled; the solver
+    multiplies by qe / (me vth)), spec_spherical.py:876-951:
+      A_Ep = [Dvr_RtoL on cos > 0 ordinates, Dvr_LtoR on cos < 0] (x) diag(cos) - diag(1/vr) (x) sin Dvt_RtoL,
+      A_En = [Dvr_LtoR on cos > 0, Dvr_RtoL on cos < 0] (x) diag(cos)          - diag(1/vr) (x) sin Dvt_LtoR."""
+    nr, nt = len(vr), len(vt)
+    DL, DR = upwind_d1(vr, pvr + 1, "L"), upwind_d1(vr, pvr + 1, "R")
+    TL, TR = upwind_d1_theta(vt, pvt + 1, "L"), upwind_d1_theta(vt, pvt + 1, "R")
+    DL[0, :] = 0.0
+    DR[-1, :] = 0.0
+    DR[-1, -1] = -1.0 / (rmax - vr[-1])
+    TL[0, :] = 0.0
+    TR[-1, :] = 0.0
+    c, s = np.cos(vt), np.sin(vt)
+    pos = c > 0
+    out = []
+    for Dpos, Dneg, T in ((DR, DL, TR), (DL, DR, TL)):
+        A = np.zeros((nr * nt, nr * nt))
+        for j in range(nt):
+            D = Dpos if pos[j] else Dneg
+            A[j::nt, j::nt] += c[j] * D
+        A -= np.kron(np.diag(1.0 / vr), np.diag(s) @ T)
+        out.append(A)
+    return out[0], out[1]
+
+
+def x_shift_bands(vr, vt, x, px, ax, dt):
+    """bte_x_shift_diag (:780-860, upwind x-space): per (r, j) the row-stored bands of
+    I + dt ax v_r cos(theta_j) D, D the upwind x operator with its inflow row zeroed ("L" for
+    theta <= pi/2, "R" otherwise); (Nr, Nvt, px + 1, Nx), band[k][i] = M[i][i -/+ k]."""
+    Nx = len(x)
+    DL, DR = upwind_d1(x, px + 1, "L"), upwind_d1(x, px + 1, "R")
+    DL[0, :] = 0.0
+    DR[-1, :] = 0.0
+    out = np.zeros((len(vr), len(vt), px + 1, Nx))
+    for j, th in enumerate(vt):
+        lower = th <= 0.5 * np.pi
+        D = DL if lower else DR
+        for i, v in enumerate(vr):
+            M = np.eye(Nx) + dt * ax * v * np.cos(th) * D
+            for k in range(px + 1):
+                if lower:
+                    out[i, j, k, k:] = np.diagonal(M, offset=-k)
+                else:
+                    out[i, j, k, :Nx - k] = np.diagonal(M, offset=k)
+    return out
+
+
+def implicit_matvec(g, A_Ep, A_En, xshift, E, x, dt):
+    """rhs_mvec (:1915-1955): y = X x - dt tau (n0 np0 C x + E (x) A_sign(E) x), the v-space part's
+    inflow rows (theta <= pi/2 at the first x point, > pi/2 at the last) zeroed, X the x-shift
+    bands of `x_shift_bands`. C is g["op_col_en"] (no gas-temperature term on the FVM grid);
+    A_Ep, A_En already scaled by qe / (me vth)."""
+    Nr, Nvt, Nx = int(g["Nr"]), int(g["Nvt"]), int(g["Nx"])
+    vt = np.asarray(g["vt"])
+    X = x.reshape(Nr * Nvt, Nx)
+    E = np.asarray(E)
+    yE = np.where(E[None, :] >= 0, A_Ep @ X, A_En @ X)
+    yv = dt * float(g["tau"]) * (float(g["n0"]) * float(g["np0"]) * (np.asarray(g["op_col_en"]) @ X) + E[None, :] * yE)
+    yv = yv.reshape(Nr, Nvt, Nx)
+    yv[:, vt <= 0.5 * np.pi, 0] = 0.0
+    yv[:, vt > 0.5 * np.pi, -1] = 0.0
+    Z = X.reshape(Nr, Nvt, Nx)
+    yx = np.zeros_like(Z)
+    for j, th in enumerate(vt):
+        yx[:, j] = SO.banded_tri_mv(xshift[:, j], Z[:, j], lower=bool(th <= 0.5 * np.pi))
+    return (yx - yv).reshape(Nr * Nvt, Nx)
+
+
+def implicit_rhs(g, v):
+    """brhs (:1907-1911): v with the inflow values zeroed."""
+    Nr, Nvt, Nx = int(g["Nr"]), int(g["Nvt"]), int(g["Nx"])
+    vt = np.asarray(g["vt"])
+    b = np.array(v, dtype=np.float64).reshape(Nr, Nvt, Nx)
+    b[:, vt <= 0.5 * np.pi, 0] = 0.0
+    b[:, vt > 0.5 * np.pi, -1] = 0.0
+    return b.reshape(Nr * Nvt, Nx)
+
+
+def implicit_step(g, A_Ep, A_En, xshift, E, v, dt):
+    """The fully implicit step's solution, by a dense solve of rhs_mvec y = brhs (the reference
+    reaches it by preconditioned GMRES to rtol): small cases only."""
+    n = int(g["Nr"]) * int(g["Nvt"]) * int(g["Nx"])
+    M = np.zeros((n, n))
+    I = np.eye(n)
+    for k in range(n):
+        M[:, k] = implicit_matvec(g, A_Ep, A_En, xshift, E, I[:, k], dt).reshape(-1)
+    return np.linalg.solve(M, implicit_rhs(g, v).reshape(-1)).reshape(-1, int(g["Nx"]))

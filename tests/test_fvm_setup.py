@@ -1,0 +1,89 @@
+"""The finite-volume 1D3V set-up on the host (grids, upwind operators and bands, the factored
+collision operator and its closed-form inverse) against the reference's own set-up
+(tests/golden/fvm_reference.npz) and the oracle."""
+import os
+
+import numpy as np
+import pytest
+
+from boltzmann_gb300 import bte_1d3v_fvm as P
+from boltzmann_gb300.bte_1d3v import ordinates
+from boltzmann_gb300.lxcat import read_cross_section_data
+from oracle import bte1d_fvm_oracle as F
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "fvm_reference.npz")
+
+
+@pytest.fixture(scope="module")
+def g():
+    return dict(np.load(GOLDEN))
+
+
+def test_grids_match_the_reference(g):
+    vr, qw, vmax = P.radial_cells(80.0, 4.0, 7, 3, int(g["spline_qpts"]))
+    np.testing.assert_allclose(vr, g["vr"], rtol=1e-15, atol=0)
+    np.testing.assert_allclose(qw, g["vr_qw"], rtol=1e-15, atol=0)
+    assert vmax == pytest.approx(float(g["domain"][1]), rel=1e-15)
+    vt, vt_qw = ordinates(int(g["Nvt"]))
+    np.testing.assert_allclose(vt, g["vt"], rtol=1e-15, atol=0)
+    np.testing.assert_allclose(vt_qw, g["vt_qw"], rtol=1e-15, atol=0)
+    np.testing.assert_allclose(P.x_points(int(g["Nx"])), g["x"], rtol=0, atol=1e-15)
+    assert np.array_equal(P.x_points(5, adaptive_grid=0), np.linspace(-1, 1, 5))
+
+
+def test_fd_weights_are_exact_on_polynomials():
+    rng = np.random.default_rng(3)
+    for n in (2, 3, 4, 5):
+        nodes = np.sort(rng.uniform(-1.0, 2.0, n))
+        x0 = nodes[rng.integers(n)]
+        w = P.fd_weights(x0, nodes)
+        for p in range(n):
+            exact = p * x0 ** (p - 1) if p else 0.0
+            assert abs(w @ nodes ** p - exact) <= 1e-9 * max(1.0, abs(exact))
+
+
+def test_upwind_operators_match_the_reference_and_the_oracle(g):
+    """Fornberg weights against the reference's operators (inflow rows zeroed, as captured) and
+    the oracle's explicit Lagrange-derivative weights."""
+    for D, x, sw, dirn, theta in ((g["Dx_LtoR"], g["x"], int(g["px"]) + 1, "L", False),
+                                  (g["Dx_RtoL"], g["x"], int(g["px"]) + 1, "R", False),
+                                  (g["Dvt_LtoR"], g["vt"], int(g["pvt"]) + 1, "L", True),
+                                  (g["Dvt_RtoL"], g["vt"], int(g["pvt"]) + 1, "R", True)):
+        mine = (P.upwind_operator_theta if theta else P.upwind_operator)(x, sw, dirn)
+        orc = (F.upwind_d1_theta if theta else F.upwind_d1)(np.asarray(x), sw, dirn)
+        assert np.max(np.abs(mine - orc)) <= 1e-12 * np.max(np.abs(orc))
+        mine[0 if dirn == "L" else -1, :] = 0.0
+        assert np.max(np.abs(mine - D)) <= 1e-12 * np.max(np.abs(D))
+
+
+def test_bands_match_the_reference(g):
+    p = [int(g[k]) for k in ("pvr", "pvt", "px")]
+    ops = P.fvm_upwind_operators(g["vr"], g["vt"], g["x"], *p, float(g["domain"][1]))
+    for k, b in P.fvm_bands(ops, *p).items():
+        assert b.shape == g[k].shape
+        assert np.max(np.abs(b - g[k])) <= 1e-13 * np.max(np.abs(g[k])), k
+
+
+def test_collision_operator_and_closed_form_inverse(g, synthetic_xs):
+    """The factored operator reproduces the reference's op_col_en; its closed-form inverse the
+    reference's dense PmatC; `apply` the dense product."""
+    procs = list(read_cross_section_data(synthetic_xs).values())
+    vt, vt_qw = ordinates(int(g["Nvt"]))
+    gain, loss = P.fvm_collisions(procs, g["vr"], vt_qw, float(g["vth"]), float(g["domain"][1]))
+    C = P.FvmCollisions(gain, loss, 2.0 * np.pi * vt_qw)
+    ref = g["op_col_en"]
+    assert np.max(np.abs(C.dense() - ref)) <= 1e-13 * np.max(np.abs(ref))
+    c = float(g["dt"]) * float(g["tau"]) * float(g["n0"]) * float(g["np0"])
+    Pm = C.inverse_dense(c)
+    assert np.max(np.abs(Pm - g["PmatC"])) <= 1e-12 * np.max(np.abs(g["PmatC"]))
+    v = np.random.default_rng(1).standard_normal((C.Nr * C.Nvt, 3))
+    np.testing.assert_allclose(C.apply(v), C.dense() @ v, rtol=0, atol=1e-13 * np.abs(C.dense() @ v).max())
+    # (I - c C) applied to the inverse's output returns the input
+    y = Pm @ v
+    np.testing.assert_allclose(y - c * C.apply(y), v, rtol=0, atol=1e-12 * np.abs(v).max())
+
+
+def test_attachment_has_no_fvm_operator(g):
+    proc = {"type": "ATTACHMENT", "threshold": 0.0, "energy": [0.0, 1.0], "cross section": [1e-20, 1e-20]}
+    with pytest.raises(NotImplementedError):
+        P.fvm_collisions([proc], g["vr"], np.ones(4), float(g["vth"]), float(g["domain"][1]))

@@ -86,3 +86,50 @@ def test_upwind_operators_and_bands(g):
     for k, b in bands.items():
         ref = g[k]
         assert np.max(np.abs(b - ref)) <= 1e-9 * np.max(np.abs(ref)), k
+
+
+GOLDEN_IMPLICIT = os.path.join(os.path.dirname(__file__), "golden", "fvm_implicit_reference.npz")
+
+
+@pytest.fixture(scope="module")
+def gi(g):
+    """The fully implicit fixture (same grid as the op-split one), with the op-split fixture's
+    collision operator."""
+    d = dict(np.load(GOLDEN_IMPLICIT))
+    for k in ("vr", "vt", "x"):
+        assert np.array_equal(d[k], g[k])
+    d["op_col_en"] = g["op_col_en"]
+    return d
+
+
+def _implicit_ops(gi):
+    s = float(gi["qe"]) / float(gi["me"]) / float(gi["vth"])
+    Ep, En = F.adv_v_fvm(gi["vr"], gi["vt"], int(gi["pvr"]), int(gi["pvt"]), float(gi["domain"][1]))
+    ax = float(gi["vth"]) * float(gi["tau"]) / float(gi["L"])
+    xs = F.x_shift_bands(gi["vr"], gi["vt"], gi["x"], int(gi["px"]), ax, float(gi["dt"]))
+    return s * Ep, s * En, xs
+
+
+def test_implicit_operators_match_the_reference(gi):
+    Ep, En, xs = _implicit_ops(gi)
+    for mine, ref in ((Ep, gi["adv_v_Ep"]), (En, gi["adv_v_En"])):
+        assert np.max(np.abs(mine - ref)) <= 1e-13 * np.max(np.abs(ref))
+    assert np.max(np.abs(xs - gi["x_shift_diag"])) <= 1e-13 * np.max(np.abs(gi["x_shift_diag"]))
+
+
+def test_implicit_matvec_rhs_and_step_match_the_reference(gi):
+    """rhs_mvec on a seeded vector, the right-hand side, and the step (a direct solve against
+    the reference's GMRES to rtol 1e-12; the field has both signs)."""
+    Ep, En, xs = _implicit_ops(gi)
+    assert (gi["E"] < 0).any() and (gi["E"] > 0).any()
+    dt = float(gi["dt"])
+    Au = F.implicit_matvec(gi, Ep, En, xs, gi["E"], gi["u"], dt).reshape(-1)
+    assert np.max(np.abs(Au - gi["Au"])) <= 1e-13 * np.max(np.abs(gi["Au"]))
+    assert np.array_equal(F.implicit_rhs(gi, gi["v0"]).reshape(-1), gi["brhs"])
+    y = F.implicit_step(gi, Ep, En, xs, gi["E"], gi["v0"], dt)
+    assert np.max(np.abs(y - gi["step"])) <= 1e-10 * np.max(np.abs(gi["step"]))
+
+
+def test_implicit_preconditioner_is_the_op_split_step(g, gi):
+    Mu = F.op_split_step(g, gi["E"], gi["u"].reshape(-1, int(g["Nx"])), float(g["dt"]))
+    assert np.max(np.abs(Mu.reshape(-1) - gi["Mu"])) <= 1e-13 * np.max(np.abs(gi["Mu"]))
