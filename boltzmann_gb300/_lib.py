@@ -28,7 +28,8 @@ EXPORTED = ["bte_grid_create", "bte_grid_destroy", "bte_grid_info", "bte_grid_ex
             "bte1d_ords_to_lm", "bte1d_lm_to_ords", "bte1d_launches", "bte1d_last_error",
             "bte_bidiag_solve", "bte_banded_tri_solve", "bte_banded_tri_mv", "bte_adv_be_sweep",
             "bte_bsr_upper_unit_solve", "bte_sweep_last_error", "bte_dgemm_nn", "bte_permute3",
-            "bte_fvm_inflow_zero"]
+            "bte_fvm_inflow_zero", "bte_fvm_create", "bte_fvm_destroy", "bte_fvm_set_collision_inverse",
+            "bte_fvm_mvec", "bte_fvm_precond", "bte_fvm_step", "bte_fvm_launches", "bte_fvm_last_error"]
 
 STAT_FAMILIES = ["residual", "jacobian", "lu_factor", "lu_solve", "refine", "other"]
 
@@ -51,6 +52,12 @@ class SolveOpts(C.Structure):
         ("alpha_min", C.c_double), ("alpha_rho", C.c_double), ("line_search_c", C.c_double),
         ("ee", C.c_int), ("precision", C.c_int), ("refine", C.c_int), ("krylov", C.c_int), ("reserved", C.c_int * 4),
     ]
+
+
+class FvmCoef(C.Structure):
+    """bte_fvm_coef (include/bte_fvm_gb300.h)."""
+    _fields_ = [("dt", C.c_double), ("dtx", C.c_double), ("tau", C.c_double), ("kappa", C.c_double),
+                ("cA", C.c_double), ("ax", C.c_double)]
 
 
 class TransientOpts(C.Structure):
@@ -122,6 +129,15 @@ def load() -> C.CDLL:
     lib.bte_dgemm_nn.argtypes = [ci, ci, ci, vp, ci, vp, ci, vp, ci, vp]
     lib.bte_permute3.argtypes = [ci, ci, ci, ci, ci, ci, vp, vp, vp]
     lib.bte_fvm_inflow_zero.argtypes = [ci, ci, ci, vp, vp, vp]
+    lib.bte_fvm_create.argtypes = [ci] * 7 + [dp] * 11 + [C.POINTER(vp)]
+    lib.bte_fvm_destroy.argtypes = [vp]
+    lib.bte_fvm_set_collision_inverse.argtypes = [vp, dp, dp]
+    lib.bte_fvm_mvec.argtypes = [vp, C.POINTER(FvmCoef), vp, vp, vp, vp]
+    lib.bte_fvm_precond.argtypes = [vp, C.c_double, C.c_double, C.c_double, vp, vp, vp, vp]
+    lib.bte_fvm_step.argtypes = [vp, C.POINTER(FvmCoef), C.c_double, vp, vp, C.c_double, C.c_double, ci, ci, dp, vp]
+    lib.bte_fvm_launches.argtypes = [vp]
+    lib.bte_fvm_launches.restype = C.c_longlong
+    lib.bte_fvm_last_error.restype = C.c_char_p
     _lib = lib
     return lib
 

@@ -24,9 +24,15 @@ Step (`FvmOpSplit`, :1745-1870, type XVTVRC) from the library's kernels
 3. v_theta advection sweeps on (Nx, Nr, Nvt) (kind 1);
 4. inflow zeroing and x advection sweeps on (Nr, Nvt, Nx) (kind 2, a = vth tau / L v_r cos theta).
 The layout swaps between the stages run through bte_permute3.
+
+Fully implicit step (`FvmImplicit`, `bte_1d3v_fvm.step`; :1890-2009) from the library's
+`bte_fvm_*` entry points (`include/bte_fvm_gb300.h`): restarted GMRES on the fused operator
+rhs_mvec, right-preconditioned with the op-split step, whose collision solve uses the
+closed-form inverse instead of a dense PmatC.
 """
 from __future__ import annotations
 
+import ctypes as C
 import math
 
 import numpy as np
@@ -328,3 +334,236 @@ class FvmOpSplit:
         _check(lib.bte_adv_be_sweep(2, _ptr(l), _ptr(r), _ptr(self.ax_vr), _ptr(self.cos_vt), h, _ptr(b), _ptr(out),
                                     l.shape[0], Nr, Nvt, Nx, s), "x sweep")
         return out
+
+
+# ----------------------------------------------------------------------------------
+# the fully implicit step on the GPU
+# ----------------------------------------------------------------------------------
+_BAND_KEYS = ("vr_diag_l2r", "vr_diag_r2l", "vt_diag_l2r", "vt_diag_r2l", "x_diag_l2r", "x_diag_r2l")
+
+
+def _host(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class FvmImplicit:
+    """The library's fully implicit FVM step (include/bte_fvm_gb300.h) on one GPU: the fused
+    operator (rhs_mvec), the op-split preconditioner with the closed-form collision inverse,
+    and the GMRES solve. Set-up: grids vr (Nr), vt (Nvt), the ordinate weights vt_qw, Nx,
+    `bands` (the six arrays of `fvm_bands`) and `coll` (an `FvmCollisions`)."""
+
+    def __init__(self, vr, vt, vt_qw, Nx, bands, coll, device=0):
+        import torch
+        self.torch = torch
+        self.device = int(device)
+        self.Nr, self.Nvt, self.Nx = len(vr), len(vt), int(Nx)
+        b = [_host(bands[k]) for k in _BAND_KEYS]
+        for (l, r), n in zip(((b[0], b[1]), (b[2], b[3]), (b[4], b[5])), (self.Nr, self.Nvt, self.Nx)):
+            if l.ndim != 2 or l.shape != r.shape or l.shape[1] != n:
+                raise ValueError("band arrays must be (p + 1, N) for their direction")
+        if coll.Nr != self.Nr or coll.Nvt != self.Nvt:
+            raise ValueError("collision operator and grids disagree in size")
+        self.coll = coll
+        self._keep = [_host(vr), _host(vt), _host(2.0 * np.pi * np.asarray(vt_qw)), _host(coll.loss), _host(coll.gain)] + b
+        h = C.c_void_p()
+        lib = _lib.load()
+        rc = lib.bte_fvm_create(self.device, self.Nr, self.Nvt, self.Nx, b[0].shape[0], b[2].shape[0], b[4].shape[0],
+                                *[_dp(a) for a in self._keep], C.byref(h))
+        self._fail(rc, "bte_fvm_create")
+        self._h = h
+        self.gmres_info = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            _lib.load().bte_fvm_destroy(h)
+            self._h = None
+
+    @staticmethod
+    def _fail(rc, what):
+        if rc != 0:
+            raise RuntimeError("%s failed (%d): %s" % (what, rc, _lib.load().bte_fvm_last_error().decode()))
+
+    def _dev(self, a, n):
+        t = self.torch.as_tensor(a, dtype=self.torch.float64, device="cuda")
+        if t.numel() != n:
+            raise ValueError("expected %d values, got %d" % (n, t.numel()))
+        return t.reshape(-1).contiguous()
+
+    def set_collision_inverse(self, c):
+        """Preconditioner collision solve (I - c C)^-1, c = gmres_pc_cv dt tau n0 np0."""
+        dinv, H = self.coll.inverse_factors(float(c))
+        self._inv = (_host(dinv), _host(H))
+        self._fail(_lib.load().bte_fvm_set_collision_inverse(self._h, _dp(self._inv[0]), _dp(self._inv[1])),
+                   "bte_fvm_set_collision_inverse")
+
+    def mvec(self, coef, E, X):
+        """rhs_mvec(X) with coef an `_lib.FvmCoef`; X (Nr * Nvt, Nx) -> CUDA tensor of its shape."""
+        n = self.Nr * self.Nvt * self.Nx
+        Xd, Ed = self._dev(X, n), self._dev(E, self.Nx)
+        Y = self.torch.empty_like(Xd)
+        self._fail(_lib.load().bte_fvm_mvec(self._h, C.byref(coef), _ptr(Ed), _ptr(Xd), _ptr(Y), _stream()),
+                   "bte_fvm_mvec")
+        return Y.reshape(self.Nr * self.Nvt, self.Nx)
+
+    def precond(self, cE, ax, hstep, E, X):
+        """The op-split step (XVTVRC) of X at aE = cE E, x coefficient ax, step hstep."""
+        n = self.Nr * self.Nvt * self.Nx
+        Xd, Ed = self._dev(X, n), self._dev(E, self.Nx)
+        Y = self.torch.empty_like(Xd)
+        self._fail(_lib.load().bte_fvm_precond(self._h, float(cE), float(ax), float(hstep), _ptr(Ed), _ptr(Xd),
+                                               _ptr(Y), _stream()), "bte_fvm_precond")
+        return Y.reshape(self.Nr * self.Nvt, self.Nx)
+
+    def step(self, coef, E, V, alpha=1.0, rtol=1e-12, atol=1e-14, restart=30, max_iter=600):
+        """Solve rhs_mvec(V') = V (inflow values zeroed); returns V' (Nr * Nvt, Nx)."""
+        n = self.Nr * self.Nvt * self.Nx
+        Vd, Ed = self._dev(V, n).clone(), self._dev(E, self.Nx)
+        info = (C.c_double * 4)()
+        rc = _lib.load().bte_fvm_step(self._h, C.byref(coef), float(alpha), _ptr(Ed), _ptr(Vd), float(rtol),
+                                      float(atol), int(restart), int(max_iter), info, _stream())
+        self._fail(rc, "bte_fvm_step")
+        self.gmres_info = {"iterations": int(info[0]), "residual_abs": info[1], "residual_rel": info[2],
+                           "status": int(info[3])}
+        return Vd.reshape(self.Nr * self.Nvt, self.Nx)
+
+    def launches(self):
+        return int(_lib.load().bte_fvm_launches(self._h))
+
+
+# ----------------------------------------------------------------------------------
+# the reference-facing solver
+# ----------------------------------------------------------------------------------
+XVTVRC = 3          # pc_type.XVTVRC (bte_1d3v_solver.py:58-63), the one op-split order the reference implements
+_SOLVERS = {"fully_implicit": "fully_implicit", "XVTVRC": "op_split"}
+
+
+def fvm_setup(par):
+    """The host set-up of the FVM solver from the reference's parameter table (a TOML path with a
+    [bte] table, or the table as a dict): vspace_type = 0, solver_type "fully_implicit" or
+    "XVTVRC", the op-split (XVTVRC) preconditioner, `collisions` an LXCat file. Returns a
+    namespace: params, vth, vmax, vr, vr_qw, vt, vt_qw, x, grid_info, collisions (an
+    `FvmCollisions`), bands (the six `fvm_bands` arrays). Mirrors bte_1d3v.__init__ / init()
+    (bte_1d3v_solver.py:77-216,245-266,377-470,1403-1470)."""
+    import types
+    from .lxcat import read_cross_section_data
+    tp = par
+    if not isinstance(par, dict):
+        import tomllib
+        with open(par, "rb") as fh:
+            tp = tomllib.load(fh)["bte"]
+    p = load_params(tp, fvm=True)
+    p.pvr, p.pvt, p.px = int(tp.get("pvr", 3)), int(tp.get("pvt", 3)), int(tp.get("px", 1))
+    p.adaptive_grid = bool(tp.get("adaptive_grid", 1))
+    p.pc_type = str(tp.get("pc_type", "xvtvrc_solve"))
+    if p.pc_type != "xvtvrc_solve":
+        raise NotImplementedError("only the op-split XVTVRC preconditioner is provided")
+    if tp.get("solver_type") not in _SOLVERS:
+        raise NotImplementedError("solver_type must be one of %s for the FVM v-space" % sorted(_SOLVERS))
+    p.solver = _SOLVERS[tp["solver_type"]]
+    if tp.get("ic_file", ""):
+        raise NotImplementedError("initial conditions from files are not provided")
+    p.qe, p.me = QE, ME
+    vth = thermal_velocity(p.Te)
+    vr, vr_qw, vmax = radial_cells(p.ev_max, p.Te, p.Nr, p.sp_order, p.spline_qpts)
+    vt, vt_qw = ordinates(p.Nvt)
+    x = x_points(p.Np, p.adaptive_grid)
+    procs = list(read_cross_section_data(p.collisions).values())
+    gain, loss = fvm_collisions(procs, vr, vt_qw, vth, vmax)
+    coll = FvmCollisions(gain, loss, 2.0 * np.pi * vt_qw)
+    bands = fvm_bands(fvm_upwind_operators(vr, vt, x, p.pvr, p.pvt, p.px, vmax), p.pvr, p.pvt, p.px)
+    return types.SimpleNamespace(params=p, vth=vth, vmax=vmax, vr=vr, vr_qw=vr_qw, vt=vt, vt_qw=vt_qw, x=x,
+                                 grid_info={"x": x, "vr": vr, "vr_qw": vr_qw, "vt": vt, "vt_qw": vt_qw},
+                                 collisions=coll, bands=bands)
+
+
+def step_coefficients(p, vth, dt, dtx):
+    """(dt, dtx, tau, kappa, cA, ax) of a step (bte_fvm_coef): kappa = n0 np0, cA = qe / (me vth),
+    ax = vth tau / L (bte_1d3v_solver.py:1775-1776); dtx the x-shift's set-up step."""
+    return (float(dt), float(dtx), p.tau, p.n0 * p.np0, QE / ME / vth, vth * (p.tau / p.L))
+
+
+class bte_1d3v_fvm:
+    """The reference's `bte_1d3v` with the finite-volume v-space on one GPU. `par`: the
+    parameter file (TOML with a [bte] table) or the same table as a dict, with
+    vspace_type = 0 and solver_type "fully_implicit" or "XVTVRC"; `collisions` names an
+    LXCat file (single species)."""
+
+    def __init__(self, par, device=0):
+        import torch
+        self.torch = torch
+        st = fvm_setup(par)
+        self.params = p = st.params
+        self.device = int(device)
+        torch.cuda.set_device(self.device)
+        self.bs_vth, self.vmax, self.xp = st.vth, st.vmax, st.x
+        self.grid_info = st.grid_info
+        self.dof_vr, self.dof_vt, self.dof_x = len(st.vr), len(st.vt), p.Np
+        self.dof_v = self.dof_vr * self.dof_vt
+        self.op_col, self.bands = st.collisions, st.bands
+        self.solver = FvmImplicit(st.vr, st.vt, st.vt_qw, p.Np, self.bands, self.op_col, device=self.device)
+        self.c_gamma = C_GAMMA
+        self.gmres_info = None
+        self._dt_init = None
+
+    def init(self, dt, gmres_pc_cv=1.0, gmres_pc_ax=1.0):
+        """init(dt) (:1333-1470): the collision inverse at gmres_pc_cv dt and the x-shift at
+        gmres_pc_ax dt."""
+        p = self.params
+        self.solver.set_collision_inverse(gmres_pc_cv * dt * p.tau * p.n0 * p.np0)
+        self._dt_init = gmres_pc_ax * dt
+
+    def _coef(self, dt):
+        from ._lib import FvmCoef
+        if self._dt_init is None:
+            raise RuntimeError("init(dt) must be called before stepping")
+        return FvmCoef(*step_coefficients(self.params, self.bs_vth, dt, self._dt_init))
+
+    def rhs_mvec(self, E, x, dt):
+        """The fully implicit step's operator applied to x (Nr * Nvt, Nx) (:1915-1955)."""
+        return self.solver.mvec(self._coef(dt), E, x)
+
+    def step_op_split(self, E, v, dv, time, dt, type=XVTVRC, verbose=0, alpha=1.0):
+        """step_op_split (:1745-1870), type XVTVRC: returns the new (Nr * Nvt, Nx) state."""
+        if type != XVTVRC:
+            raise NotImplementedError("preconditioner type not implemented")
+        c = self._coef(dt)
+        return self.solver.precond(c.tau * c.cA, c.ax, float(alpha) * float(dt), E, v)
+
+    def step(self, E, v, dv, time, dt, verbose=0, gmres_pc_vr=1.0, gmres_pc_vt=1.0, pc_left=False):
+        """step (:1872-2030): the fully implicit solve (GMRES preconditioned by the op-split
+        step at gmres_pc_vr dt) or, with solver_type "XVTVRC", one op-split step."""
+        p = self.params
+        if p.solver == "op_split":
+            return self.step_op_split(E, v, dv, time, dt, XVTVRC, verbose)
+        if pc_left:
+            raise NotImplementedError("only right preconditioning is provided")
+        out = self.solver.step(self._coef(dt), E, v, alpha=gmres_pc_vr, rtol=p.rtol, atol=p.atol,
+                               restart=p.gmres_rsrt, max_iter=p.gmres_maxiter)
+        info = self.solver.gmres_info
+        self.gmres_info = info
+        if info["status"] != 0:
+            raise RuntimeError("%08d GMRES solver failed! iterations =%d  ||res|| = %.4E ||res||/||b|| = %.4E"
+                               % (int(time / dt), info["iterations"], info["residual_abs"], info["residual_rel"]))
+        return out
+
+    def initial_condition(self, type=0):
+        """initial_condition(type=0) for the FVM v-space (:1288-1327): the density profile times a
+        Maxwellian at Te in every ordinate."""
+        if type != 0:
+            raise NotImplementedError
+        p = self.params
+        xx = p.L * (self.xp + 1)
+        ne = 1e6 * (1e7 + 1e9 * (1 - 0.5 * xx / p.L) ** 2 * (0.5 * xx / p.L) ** 2) / p.np0
+        ratio = C_GAMMA * math.sqrt(p.Te) / self.bs_vth
+        vr = self.grid_info["vr"]
+        hv = np.exp(-(vr / ratio) ** 2) / (math.sqrt(math.pi) ** 3 * ratio ** 3)
+        v = np.kron(hv, np.ones(self.dof_vt))[:, None] * ne[None, :]
+        return self.torch.as_tensor(v, dtype=self.torch.float64, device="cuda")
+
+    def launches(self):
+        return self.solver.launches()

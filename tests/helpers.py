@@ -45,3 +45,11 @@ def rel_l2_cols(a, b):
     a = np.asarray(a)
     b = np.asarray(b)
     return np.linalg.norm(a - b, axis=0) / np.linalg.norm(b, axis=0)
+
+
+# the parameter table of the finite-volume fixtures (tests/golden/make_golden_fvm_implicit.py:
+# the 1D3V golden table with the FVM v-space, upwind x, stencil orders 2, fully implicit)
+FVM_IMPLICIT_PARAMS = dict(L=2.54e-2, V0=100.0, freq=13.56e6, Tg=300.0, p0=1.0, gmres_rsrt=30, gmres_rsrt_iter=20,
+                           Np=12, Nr=7, Nvt=8, lmax=1, dt=1e-3, ev_max=80.0, ev_extend=0, sp_order=3, spline_qpts=5,
+                           Te=4.0, xspace_type=0, vspace_type=0, solver_type="fully_implicit", adaptive_grid=1, pvr=2,
+                           pvt=2, px=2, rtol=1e-12, atol=1e-14, ic_file="")

@@ -1,0 +1,113 @@
+"""The shared core of the finite-volume fully implicit step (boltzmann_gb300/csrc/fvm_core.h),
+compiled for the host through tests/host/fvm_harness.cpp: its operator, its op-split
+preconditioner (closed-form collision inverse) and its GMRES against the reference's own
+rhs_mvec, preconditioner and step (tests/golden/fvm_implicit_reference.npz), on the
+product's host set-up and step coefficients (boltzmann_gb300.bte_1d3v_fvm.fvm_setup,
+step_coefficients) from the fixture's parameter table."""
+import ctypes as C
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from boltzmann_gb300 import bte_1d3v_fvm as P
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "..", "boltzmann_gb300", "csrc")
+GOLDEN = os.path.join(HERE, "golden", "fvm_implicit_reference.npz")
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no host C++ compiler")
+    so = str(tmp_path_factory.mktemp("fvm") / "fvm_harness.so")
+    r = subprocess.run([cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-I", CSRC,
+                        os.path.join(HERE, "host", "fvm_harness.cpp"), "-o", so], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return C.CDLL(so)
+
+
+@pytest.fixture(scope="module")
+def case(synthetic_xs):
+    """The product's host set-up and step coefficients from the fixture's parameter table."""
+    from helpers import FVM_IMPLICIT_PARAMS
+    g = dict(np.load(GOLDEN))
+    st = P.fvm_setup(dict(FVM_IMPLICIT_PARAMS, collisions=synthetic_xs))
+    for k in ("vr", "vt", "x"):
+        np.testing.assert_allclose(st.grid_info[k], g[k], rtol=0, atol=1e-14 * np.abs(g[k]).max())
+    p = st.params
+    dt = float(g["dt"])
+    c6 = np.array(P.step_coefficients(p, st.vth, dt, dt))
+    np.testing.assert_allclose(c6, [dt, dt, float(g["tau"]), float(g["n0"]) * float(g["np0"]),
+                                    float(g["qe"]) / float(g["me"]) / float(g["vth"]),
+                                    float(g["vth"]) * float(g["tau"]) / float(g["L"])], rtol=1e-14)
+    dinv, H = st.collisions.inverse_factors(dt * c6[2] * c6[3])
+    return dict(g=g, p=[p.pvr, p.pvt, p.px], bands=st.bands, coll=st.collisions, dinv=dinv, H=H, c6=c6,
+                cE=c6[2] * c6[4], ax=c6[5])
+
+
+def _d(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class _Args:
+    """Keeps the marshalled arrays alive for one call."""
+
+    def __init__(self, case):
+        g = case["g"]
+        self.keep = []
+        self.dims = (C.c_int * 6)(int(g["Nr"]), int(g["Nvt"]), int(g["Nx"]), case["p"][0] + 1, case["p"][1] + 1,
+                                  case["p"][2] + 1)
+        bl = [case["bands"][k] for k in ("vr_diag_l2r", "vr_diag_r2l", "vt_diag_l2r", "vt_diag_r2l", "x_diag_l2r",
+                                         "x_diag_r2l")]
+        self.bands = (C.POINTER(C.c_double) * 6)(*[self.p(b) for b in bl])
+        coll = case["coll"]
+        self.common = [self.dims, self.p(g["vr"]), self.p(g["vt"]), self.p(coll.w), self.p(coll.loss),
+                       self.p(coll.gain), self.bands]
+
+    def p(self, a):
+        arr, ptr = _d(a)
+        self.keep.append(arr)
+        return ptr
+
+
+def test_operator_matches_the_reference(harness, case):
+    g = case["g"]
+    a = _Args(case)
+    Y = np.zeros_like(g["u"])
+    harness.fvm_host_mvec(*a.common, a.p(case["c6"]), a.p(g["E"]), a.p(g["u"]), Y.ctypes.data_as(C.POINTER(C.c_double)))
+    assert np.max(np.abs(Y - g["Au"])) <= 1e-12 * np.max(np.abs(g["Au"]))
+
+
+def test_preconditioner_matches_the_reference_op_split_step(harness, case):
+    g = case["g"]
+    a = _Args(case)
+    Y = np.zeros_like(g["u"])
+    harness.fvm_host_precond(*a.common, a.p(case["dinv"]), a.p(case["H"]), C.c_double(case["cE"]),
+                             C.c_double(case["ax"]), C.c_double(float(g["dt"])), a.p(g["E"]), a.p(g["u"]),
+                             Y.ctypes.data_as(C.POINTER(C.c_double)))
+    assert np.max(np.abs(Y - g["Mu"])) <= 1e-12 * np.max(np.abs(g["Mu"]))
+
+
+@pytest.mark.parametrize("restart", [30, 4])
+def test_gmres_step_matches_the_reference(harness, case, restart):
+    """The step to rtol 1e-12 (also with a short restart, so that restarts happen) against the
+    reference's GMRES result."""
+    g = case["g"]
+    a = _Args(case)
+    V = np.ascontiguousarray(g["v0"], dtype=np.float64).copy()
+    info = (C.c_double * 4)()
+    harness.fvm_host_step.restype = C.c_int
+    rc = harness.fvm_host_step(*a.common, a.p(case["dinv"]), a.p(case["H"]), a.p(case["c6"]), C.c_double(1.0),
+                               a.p(g["E"]), V.ctypes.data_as(C.POINTER(C.c_double)), C.c_double(float(g["rtol"])),
+                               C.c_double(float(g["atol"])), C.c_int(restart), C.c_int(400), info)
+    assert rc == 0
+    assert info[3] == 0.0, list(info)
+    assert 0 < info[0] <= 400
+    ref = g["step"]
+    assert np.max(np.abs(V - ref)) <= 1e-10 * np.max(np.abs(ref))

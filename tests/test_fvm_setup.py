@@ -87,3 +87,26 @@ def test_attachment_has_no_fvm_operator(g):
     proc = {"type": "ATTACHMENT", "threshold": 0.0, "energy": [0.0, 1.0], "cross section": [1e-20, 1e-20]}
     with pytest.raises(NotImplementedError):
         P.fvm_collisions([proc], g["vr"], np.ones(4), float(g["vth"]), float(g["domain"][1]))
+
+
+def test_setup_from_the_parameter_table(synthetic_xs, g):
+    """fvm_setup on the fixtures' parameter table reproduces the reference's grids, bands and
+    collision operator."""
+    from helpers import FVM_IMPLICIT_PARAMS
+    st = P.fvm_setup(dict(FVM_IMPLICIT_PARAMS, collisions=synthetic_xs))
+    for k in ("vr", "vt", "x"):
+        np.testing.assert_allclose(st.grid_info[k], g[k], rtol=0, atol=1e-14 * np.abs(g[k]).max())
+    for k, b in st.bands.items():
+        assert np.max(np.abs(b - g[k])) <= 1e-13 * np.max(np.abs(g[k])), k
+    assert np.max(np.abs(st.collisions.dense() - g["op_col_en"])) <= 1e-13 * np.max(np.abs(g["op_col_en"]))
+    p = st.params
+    assert p.L == pytest.approx(float(g["L"])) and p.tau == pytest.approx(float(g["tau"]))
+    assert p.n0 == pytest.approx(float(g["n0"]), rel=1e-14) and p.solver == "fully_implicit"
+
+
+@pytest.mark.parametrize("change", [dict(vspace_type=1), dict(pc_type="none"), dict(solver_type="xvx_strang_split"),
+                                    dict(ic_file="ic.h5"), dict(xspace_type=2)])
+def test_setup_refuses_what_is_not_provided(synthetic_xs, change):
+    from helpers import FVM_IMPLICIT_PARAMS
+    with pytest.raises((NotImplementedError, ValueError)):
+        P.fvm_setup(dict(FVM_IMPLICIT_PARAMS, collisions=synthetic_xs, **change))

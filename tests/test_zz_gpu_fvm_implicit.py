@@ -1,0 +1,65 @@
+"""The finite-volume 1D3V fully implicit step on the GPU (boltzmann_gb300.bte_1d3v_fvm, the
+library's bte_fvm_* entry points) against the reference's own operator, preconditioner and
+step (tests/golden/fvm_implicit_reference.npz), with the product's own host set-up built from
+the same parameter table. The file is named so that pytest collects it after the solver's
+parity tests."""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import FVM_IMPLICIT_PARAMS as PARAMS
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "fvm_implicit_reference.npz")
+
+
+@pytest.fixture(scope="module")
+def g():
+    return dict(np.load(GOLDEN))
+
+
+@pytest.fixture(scope="module")
+def solver(synthetic_xs, g):
+    from boltzmann_gb300.bte_1d3v_fvm import bte_1d3v_fvm
+    s = bte_1d3v_fvm(dict(PARAMS, collisions=synthetic_xs))
+    assert (s.dof_vr, s.dof_vt, s.dof_x) == (int(g["Nr"]), int(g["Nvt"]), int(g["Nx"]))
+    s.init(float(g["dt"]))
+    return s
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(np.asarray(a) - b)) / np.max(np.abs(b)))
+
+
+def test_grid_and_initial_condition(solver, g):
+    for k in ("vr", "vt", "x"):
+        np.testing.assert_allclose(solver.grid_info[k], g[k], rtol=0, atol=1e-14 * np.abs(g[k]).max())
+    assert _rel(solver.initial_condition(0).cpu().numpy(), g["v0"]) <= 1e-13
+
+
+def test_operator_matches_the_reference(solver, g):
+    Y = solver.rhs_mvec(g["E"], g["u"].reshape(-1, int(g["Nx"])), float(g["dt"])).cpu().numpy().reshape(-1)
+    assert _rel(Y, g["Au"]) <= 1e-12
+
+
+def test_preconditioner_matches_the_reference_op_split_step(solver, g):
+    Y = solver.step_op_split(g["E"], g["u"].reshape(-1, int(g["Nx"])), None, 0.0, float(g["dt"])).cpu().numpy()
+    assert _rel(Y.reshape(-1), g["Mu"]) <= 1e-12
+
+
+def test_step_matches_the_reference(solver, g):
+    n0 = solver.launches()
+    y = solver.step(g["E"], g["v0"], None, 0.0, float(g["dt"])).cpu().numpy()
+    assert solver.gmres_info["status"] == 0
+    assert 0 < solver.gmres_info["iterations"] <= 100
+    assert _rel(y, g["step"]) <= 1e-10
+    assert solver.launches() > n0
+
+
+def test_step_before_init_is_refused(synthetic_xs):
+    from boltzmann_gb300.bte_1d3v_fvm import bte_1d3v_fvm
+    s = bte_1d3v_fvm(dict(PARAMS, collisions=synthetic_xs))
+    with pytest.raises(RuntimeError):
+        s.step(np.ones(s.dof_x), np.ones((s.dof_v, s.dof_x)), None, 0.0, 1e-3)
