@@ -481,6 +481,16 @@ def fvm_setup(par):
                                  collisions=coll, bands=bands)
 
 
+def fvm_initial_condition(p, vth, vr, Nvt, x):
+    """initial_condition(type=0) for the FVM v-space (bte_1d3v_solver.py:1288-1327): the density
+    profile ne(x) times a Maxwellian at Te in every cell and ordinate; (Nr * Nvt, Nx)."""
+    xx = p.L * (np.asarray(x) + 1)
+    ne = 1e6 * (1e7 + 1e9 * (1 - 0.5 * xx / p.L) ** 2 * (0.5 * xx / p.L) ** 2) / p.np0
+    ratio = C_GAMMA * math.sqrt(p.Te) / vth
+    hv = np.exp(-(np.asarray(vr) / ratio) ** 2) / (math.sqrt(math.pi) ** 3 * ratio ** 3)
+    return np.kron(hv, np.ones(Nvt))[:, None] * ne[None, :]
+
+
 def step_coefficients(p, vth, dt, dtx):
     """(dt, dtx, tau, kappa, cA, ax) of a step (bte_fvm_coef): kappa = n0 np0, cA = qe / (me vth),
     ax = vth tau / L (bte_1d3v_solver.py:1775-1776); dtx the x-shift's set-up step."""
@@ -552,17 +562,10 @@ class bte_1d3v_fvm:
         return out
 
     def initial_condition(self, type=0):
-        """initial_condition(type=0) for the FVM v-space (:1288-1327): the density profile times a
-        Maxwellian at Te in every ordinate."""
+        """initial_condition(type=0) (:1288-1327), on the device."""
         if type != 0:
             raise NotImplementedError
-        p = self.params
-        xx = p.L * (self.xp + 1)
-        ne = 1e6 * (1e7 + 1e9 * (1 - 0.5 * xx / p.L) ** 2 * (0.5 * xx / p.L) ** 2) / p.np0
-        ratio = C_GAMMA * math.sqrt(p.Te) / self.bs_vth
-        vr = self.grid_info["vr"]
-        hv = np.exp(-(vr / ratio) ** 2) / (math.sqrt(math.pi) ** 3 * ratio ** 3)
-        v = np.kron(hv, np.ones(self.dof_vt))[:, None] * ne[None, :]
+        v = fvm_initial_condition(self.params, self.bs_vth, self.grid_info["vr"], self.dof_vt, self.xp)
         return self.torch.as_tensor(v, dtype=self.torch.float64, device="cuda")
 
     def launches(self):

@@ -110,3 +110,11 @@ def test_setup_refuses_what_is_not_provided(synthetic_xs, change):
     from helpers import FVM_IMPLICIT_PARAMS
     with pytest.raises((NotImplementedError, ValueError)):
         P.fvm_setup(dict(FVM_IMPLICIT_PARAMS, collisions=synthetic_xs, **change))
+
+
+def test_initial_condition_matches_the_reference(synthetic_xs):
+    from helpers import FVM_IMPLICIT_PARAMS
+    gi = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "fvm_implicit_reference.npz")))
+    st = P.fvm_setup(dict(FVM_IMPLICIT_PARAMS, collisions=synthetic_xs))
+    v = P.fvm_initial_condition(st.params, st.vth, st.vr, len(st.vt), st.x)
+    assert np.max(np.abs(v - gi["v0"])) <= 1e-14 * np.max(np.abs(gi["v0"]))
