@@ -29,7 +29,8 @@ EXPORTED = ["bte_grid_create", "bte_grid_destroy", "bte_grid_info", "bte_grid_ex
             "bte_bidiag_solve", "bte_banded_tri_solve", "bte_banded_tri_mv", "bte_adv_be_sweep",
             "bte_bsr_upper_unit_solve", "bte_sweep_last_error", "bte_dgemm_nn", "bte_permute3",
             "bte_fvm_inflow_zero", "bte_fvm_create", "bte_fvm_destroy", "bte_fvm_set_collision_inverse",
-            "bte_fvm_mvec", "bte_fvm_precond", "bte_fvm_step", "bte_fvm_launches", "bte_fvm_last_error"]
+            "bte_fvm_mvec", "bte_fvm_precond", "bte_fvm_step", "bte_fvm_launches", "bte_fvm_last_error",
+            "bte_fvm_set_sl_grid", "bte_fvm_sl_advect", "bte_fvm_sl_step"]
 
 STAT_FAMILIES = ["residual", "jacobian", "lu_factor", "lu_solve", "refine", "other"]
 
@@ -135,6 +136,9 @@ def load() -> C.CDLL:
     lib.bte_fvm_mvec.argtypes = [vp, C.POINTER(FvmCoef), vp, vp, vp, vp]
     lib.bte_fvm_precond.argtypes = [vp, C.c_double, C.c_double, C.c_double, vp, vp, vp, vp]
     lib.bte_fvm_step.argtypes = [vp, C.POINTER(FvmCoef), C.c_double, vp, vp, C.c_double, C.c_double, ci, ci, dp, vp]
+    lib.bte_fvm_set_sl_grid.argtypes = [vp, dp, C.c_double, C.c_double]
+    lib.bte_fvm_sl_advect.argtypes = [vp, C.POINTER(FvmCoef), vp, vp, vp, vp]
+    lib.bte_fvm_sl_step.argtypes = [vp, C.POINTER(FvmCoef), vp, vp, vp, vp]
     lib.bte_fvm_launches.argtypes = [vp]
     lib.bte_fvm_launches.restype = C.c_longlong
     lib.bte_fvm_last_error.restype = C.c_char_p

@@ -1,4 +1,4 @@
-"""The finite-volume 1D3V solver: its operator set-up and the op-split step on the GPU.
+"""The finite-volume 1D3V solver: its operator set-up and its steps on the GPU.
 
 Counterpart of the reference's `bte_1d3v` with the FVM v-space (`vspace_type = 0`,
 BESolver/python/bte_1d3v_solver.py): cells in v_r (the B-spline basis's per-interval Gauss
@@ -28,7 +28,9 @@ The layout swaps between the stages run through bte_permute3.
 Fully implicit step (`FvmImplicit`, `bte_1d3v_fvm.step`; :1890-2009) from the library's
 `bte_fvm_*` entry points (`include/bte_fvm_gb300.h`): restarted GMRES on the fused operator
 rhs_mvec, right-preconditioned with the op-split step, whose collision solve uses the
-closed-form inverse instead of a dense PmatC.
+closed-form inverse instead of a dense PmatC. Semi-Lagrangian step (solver_type
+"sl_implicit", :2024-2027,2244-2314): interpolation at the departure points, then the
+closed-form collision inverse.
 """
 from __future__ import annotations
 
@@ -431,6 +433,32 @@ class FvmImplicit:
                            "status": int(info[3])}
         return Vd.reshape(self.Nr * self.Nvt, self.Nx)
 
+    def set_sl_grid(self, x, vmin, vmax):
+        """Grids of the semi-Lagrangian step: the x points and the cells' velocity domain."""
+        self._xg = _host(x)
+        if len(self._xg) != self.Nx:
+            raise ValueError("x must have Nx points")
+        self._fail(_lib.load().bte_fvm_set_sl_grid(self._h, _dp(self._xg), float(vmin), float(vmax)),
+                   "bte_fvm_set_sl_grid")
+
+    def sl_advect(self, coef, E, V):
+        """step_adv_vx_sl: V interpolated at its departure points over coef.dt."""
+        n = self.Nr * self.Nvt * self.Nx
+        Vd, Ed = self._dev(V, n), self._dev(E, self.Nx)
+        Y = self.torch.empty_like(Vd)
+        self._fail(_lib.load().bte_fvm_sl_advect(self._h, C.byref(coef), _ptr(Ed), _ptr(Vd), _ptr(Y), _stream()),
+                   "bte_fvm_sl_advect")
+        return Y.reshape(self.Nr * self.Nvt, self.Nx)
+
+    def sl_step(self, coef, E, V):
+        """One semi-Lagrangian step: the collision inverse of sl_advect(V)."""
+        n = self.Nr * self.Nvt * self.Nx
+        Vd, Ed = self._dev(V, n), self._dev(E, self.Nx)
+        Y = self.torch.empty_like(Vd)
+        self._fail(_lib.load().bte_fvm_sl_step(self._h, C.byref(coef), _ptr(Ed), _ptr(Vd), _ptr(Y), _stream()),
+                   "bte_fvm_sl_step")
+        return Y.reshape(self.Nr * self.Nvt, self.Nx)
+
     def launches(self):
         return int(_lib.load().bte_fvm_launches(self._h))
 
@@ -439,13 +467,13 @@ class FvmImplicit:
 # the reference-facing solver
 # ----------------------------------------------------------------------------------
 XVTVRC = 3          # pc_type.XVTVRC (bte_1d3v_solver.py:58-63), the one op-split order the reference implements
-_SOLVERS = {"fully_implicit": "fully_implicit", "XVTVRC": "op_split"}
+_SOLVERS = {"fully_implicit": "fully_implicit", "XVTVRC": "op_split", "sl_implicit": "semi_lagrangian"}
 
 
 def fvm_setup(par):
     """The host set-up of the FVM solver from the reference's parameter table (a TOML path with a
     [bte] table, or the table as a dict): vspace_type = 0, solver_type "fully_implicit" or
-    "XVTVRC", the op-split (XVTVRC) preconditioner, `collisions` an LXCat file. Returns a
+    "XVTVRC" or "sl_implicit", the op-split (XVTVRC) preconditioner, `collisions` an LXCat file. Returns a
     namespace: params, vth, vmax, vr, vr_qw, vt, vt_qw, x, grid_info, collisions (an
     `FvmCollisions`), bands (the six `fvm_bands` arrays). Mirrors bte_1d3v.__init__ / init()
     (bte_1d3v_solver.py:77-216,245-266,377-470,1403-1470)."""
@@ -500,8 +528,8 @@ def step_coefficients(p, vth, dt, dtx):
 class bte_1d3v_fvm:
     """The reference's `bte_1d3v` with the finite-volume v-space on one GPU. `par`: the
     parameter file (TOML with a [bte] table) or the same table as a dict, with
-    vspace_type = 0 and solver_type "fully_implicit" or "XVTVRC"; `collisions` names an
-    LXCat file (single species)."""
+    vspace_type = 0 and solver_type "fully_implicit", "XVTVRC" or "sl_implicit"; `collisions`
+    names an LXCat file (single species)."""
 
     def __init__(self, par, device=0):
         import torch
@@ -516,6 +544,7 @@ class bte_1d3v_fvm:
         self.dof_v = self.dof_vr * self.dof_vt
         self.op_col, self.bands = st.collisions, st.bands
         self.solver = FvmImplicit(st.vr, st.vt, st.vt_qw, p.Np, self.bands, self.op_col, device=self.device)
+        self.solver.set_sl_grid(st.x, 0.0, self.vmax)
         self.c_gamma = C_GAMMA
         self.gmres_info = None
         self._dt_init = None
@@ -544,12 +573,19 @@ class bte_1d3v_fvm:
         c = self._coef(dt)
         return self.solver.precond(c.tau * c.cA, c.ax, float(alpha) * float(dt), E, v)
 
+    def step_adv_vx_sl(self, E, v, time, dt, verbose=0):
+        """step_adv_vx_sl (:2244-2314): v interpolated at its departure points over dt."""
+        return self.solver.sl_advect(self._coef(dt), E, v)
+
     def step(self, E, v, dv, time, dt, verbose=0, gmres_pc_vr=1.0, gmres_pc_vt=1.0, pc_left=False):
         """step (:1872-2030): the fully implicit solve (GMRES preconditioned by the op-split
-        step at gmres_pc_vr dt) or, with solver_type "XVTVRC", one op-split step."""
+        step at gmres_pc_vr dt); with solver_type "XVTVRC" one op-split step; with "sl_implicit"
+        the collision inverse of the semi-Lagrangian advection (:2024-2027)."""
         p = self.params
         if p.solver == "op_split":
             return self.step_op_split(E, v, dv, time, dt, XVTVRC, verbose)
+        if p.solver == "semi_lagrangian":
+            return self.solver.sl_step(self._coef(dt), E, v)
         if pc_left:
             raise NotImplementedError("only right preconditioning is provided")
         out = self.solver.step(self._coef(dt), E, v, alpha=gmres_pc_vr, rtol=p.rtol, atol=p.atol,

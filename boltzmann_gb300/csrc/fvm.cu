@@ -11,6 +11,8 @@
 // the first layout swap (k_fvm_coll_permute), then the library's v_r, v_theta and x sweeps with
 // their layout swaps (sweeps.cu).
 // Solver: restarted right-preconditioned GMRES (fvm_core.h), device vectors, FP64.
+// Semi-Lagrangian step (solver_type "sl_implicit", :2024-2027): one kernel interpolates every
+// value at its departure point (k_fvm_sl), then the closed-form collision inverse.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -38,6 +40,9 @@ struct bte_fvm {
     double* Kr = nullptr;
     int kcap = 0;
     double *part = nullptr, *hd = nullptr;
+    double *xg = nullptr, *vrp = nullptr, *vta = nullptr;   // semi-Lagrangian grids (set once)
+    double sl_vmin = 0.0;
+    bool have_sl = false;
     std::vector<void*> allocs;
     long long launches = 0;
 };
@@ -97,9 +102,25 @@ __global__ void k_fvm_coll_permute(FvmView v, const double* __restrict__ dinv, c
     out[o] = fvm_coll_apply_at(v, dinv, T, B, r, j, x);
 }
 
-__global__ void k_fvm_scale_vec(size_t n, double a, const double* __restrict__ x, double* __restrict__ y) {
+// Y (Nr, Nvt, Nx) = the collision inverse applied to B, same layout
+__global__ void k_fvm_coll_apply(FvmView v, const double* __restrict__ dinv, const double* __restrict__ T,
+                                 const double* __restrict__ B, double* __restrict__ Y) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) y[i] = a * x[i];
+    const size_t n = (size_t)v.Nr * v.Nvt * v.Nx;
+    if (i >= n) return;
+    const int x = (int)(i % v.Nx);
+    const size_t rj = i / v.Nx;
+    Y[i] = fvm_coll_apply_at(v, dinv, T, B, (int)(rj / v.Nvt), (int)(rj % v.Nvt), x);
+}
+
+// Y = the semi-Lagrangian advection of V, one thread per value
+__global__ void k_fvm_sl(FvmSl sl, const double* __restrict__ E, const double* __restrict__ V, double* __restrict__ Y) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t n = (size_t)sl.Nr * sl.Nvt * sl.Nx;
+    if (i >= n) return;
+    const int x = (int)(i % sl.Nx);
+    const size_t rj = i / sl.Nx;
+    Y[i] = fvm_sl_at(sl, E, V, (int)(rj / sl.Nvt), (int)(rj % sl.Nvt), x);
 }
 
 // y = a x (x may alias y)
@@ -216,10 +237,40 @@ int fvm_precond(bte_fvm* h, double hstep, const double* X, double* Y, cudaStream
 
 // aE = cE E on the device, axvr = ax v_r
 int fvm_coefficients(bte_fvm* h, double cE, double ax, const double* E, cudaStream_t s) {
-    k_fvm_scale_vec<<<fblocks(h->Nx), FT, 0, s>>>((size_t)h->Nx, cE, E, h->aE);
-    k_fvm_scale_vec<<<fblocks(h->Nr), FT, 0, s>>>((size_t)h->Nr, ax, h->vr, h->axvr);
+    k_fvm_scale<<<fblocks(h->Nx), FT, 0, s>>>((size_t)h->Nx, cE, E, h->aE);
+    k_fvm_scale<<<fblocks(h->Nr), FT, 0, s>>>((size_t)h->Nr, ax, h->vr, h->axvr);
     h->launches += 2;
     return launched("coefficients");
+}
+
+FvmSl sl_of(const bte_fvm* h, const FvmCoef& c) {
+    FvmSl sl;
+    sl.Nr = h->Nr; sl.Nvt = h->Nvt; sl.Nx = h->Nx;
+    sl.vr = h->vr; sl.vt = h->vt; sl.cos_t = h->cos_t; sl.vrp = h->vrp; sl.vta = h->vta; sl.x = h->xg;
+    sl.vmin = h->sl_vmin;
+    sl.cX = c.dt * c.ax;
+    sl.cE = c.dt * c.tau * c.cA;
+    return sl;
+}
+
+// Y = step_adv_vx_sl(V) (Y must not alias V)
+int fvm_sl(bte_fvm* h, const FvmCoef& c, const double* E, const double* V, double* Y, cudaStream_t s) {
+    k_fvm_sl<<<fblocks(h->N), FT, 0, s>>>(sl_of(h, c), E, V, Y);
+    ++h->launches;
+    return launched("k_fvm_sl");
+}
+
+// Y = (I - c C)^-1 B in the natural layout (Y must not alias B)
+int fvm_coll_solve(bte_fvm* h, const double* B, double* Y, cudaStream_t s) {
+    const FvmView v = view_of(h);
+    const size_t nrx = (size_t)h->Nr * h->Nx;
+    k_fvm_moment<<<fblocks(nrx), FT, 0, s>>>(v, B, h->M);
+    if (int rc = launched("k_fvm_moment")) return rc;
+    if (int rc = sweep_rc(bte_dgemm_nn(h->Nr, h->Nx, h->Nr, h->H, h->Nr, h->M, h->Nx, h->T, h->Nx, s), "collision inverse"))
+        return rc;
+    k_fvm_coll_apply<<<fblocks(h->N), FT, 0, s>>>(v, h->dinv, h->T, B, Y);
+    h->launches += 3;
+    return launched("k_fvm_coll_apply");
 }
 
 struct DeviceOps {
@@ -386,6 +437,67 @@ int bte_fvm_precond(bte_fvm* h, double cE, double ax, double hstep, const double
     cudaStream_t s = (cudaStream_t)stream;
     if (int rc = fvm_coefficients(h, cE, ax, E, s)) return rc;
     return fvm_precond(h, hstep, X, Y, s);
+}
+
+int bte_fvm_set_sl_grid(bte_fvm* h, const double* x, double vmin, double vmax) {
+    if (!h || !x) return fvm_fail(BTE_ERR_ARG, "bte_fvm_set_sl_grid: null argument");
+    const int Nr = h->Nr, Nvt = h->Nvt, Nx = h->Nx;
+    std::vector<double> hv(Nvt);
+    if (cudaSetDevice(h->device) != cudaSuccess ||
+        cudaMemcpy(hv.data(), h->vt, (size_t)Nvt * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return fvm_fail(BTE_ERR_CUDA, "bte_fvm_set_sl_grid: copy failed");
+    std::vector<double> hr(Nr);
+    if (cudaMemcpy(hr.data(), h->vr, (size_t)Nr * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return fvm_fail(BTE_ERR_CUDA, "bte_fvm_set_sl_grid: copy failed");
+    const double pi = 3.14159265358979323846;
+    std::vector<double> vrp(Nr + 2), vta(Nvt + 2);
+    vrp[0] = vmin;
+    vrp[Nr + 1] = vmax;
+    for (int r = 0; r < Nr; ++r) vrp[r + 1] = hr[r];
+    vta[0] = 0.0;
+    vta[Nvt + 1] = pi;
+    for (int j = 0; j < Nvt; ++j) vta[j + 1] = hv[Nvt - 1 - j];
+    bool ascending = true;
+    for (int i = 0; i + 1 < Nr + 2; ++i) ascending = ascending && vrp[i] < vrp[i + 1];
+    for (int i = 0; i + 1 < Nvt + 2; ++i) ascending = ascending && vta[i] < vta[i + 1];
+    for (int i = 0; i + 1 < Nx; ++i) ascending = ascending && x[i] < x[i + 1];
+    if (!ascending)
+        return fvm_fail(BTE_ERR_ARG, "bte_fvm_set_sl_grid: need vmin < vr < vmax, ordinates in (0, pi) descending, x ascending");
+    int rc = BTE_OK;
+    if (!h->have_sl) {
+        if (rc == BTE_OK) rc = fvm_alloc(h, (void**)&h->xg, (size_t)Nx * 8);
+        if (rc == BTE_OK) rc = fvm_alloc(h, (void**)&h->vrp, (size_t)(Nr + 2) * 8);
+        if (rc == BTE_OK) rc = fvm_alloc(h, (void**)&h->vta, (size_t)(Nvt + 2) * 8);
+        if (rc != BTE_OK) return rc;
+    }
+    if (cudaMemcpy(h->xg, x, (size_t)Nx * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(h->vrp, vrp.data(), (size_t)(Nr + 2) * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(h->vta, vta.data(), (size_t)(Nvt + 2) * 8, cudaMemcpyHostToDevice) != cudaSuccess)
+        return fvm_fail(BTE_ERR_CUDA, "bte_fvm_set_sl_grid: copy failed");
+    h->sl_vmin = vmin;
+    h->have_sl = true;
+    return BTE_OK;
+}
+
+int bte_fvm_sl_advect(bte_fvm* h, const bte_fvm_coef* c, const double* E, const double* V, double* Y, void* stream) {
+    if (!h || !E || !V || !Y) return fvm_fail(BTE_ERR_ARG, "bte_fvm_sl_advect: null argument");
+    if (!coef_ok(c)) return fvm_fail(BTE_ERR_ARG, "bte_fvm_sl_advect: coefficients missing or not finite");
+    if (!h->have_sl) return fvm_fail(BTE_ERR_STATE, "bte_fvm_sl_advect: no semi-Lagrangian grid set");
+    if (V == Y) return fvm_fail(BTE_ERR_ARG, "bte_fvm_sl_advect: Y must not alias V");
+    cudaSetDevice(h->device);
+    return fvm_sl(h, coef_of(c), E, V, Y, (cudaStream_t)stream);
+}
+
+int bte_fvm_sl_step(bte_fvm* h, const bte_fvm_coef* c, const double* E, const double* V, double* Y, void* stream) {
+    if (!h || !E || !V || !Y) return fvm_fail(BTE_ERR_ARG, "bte_fvm_sl_step: null argument");
+    if (!coef_ok(c)) return fvm_fail(BTE_ERR_ARG, "bte_fvm_sl_step: coefficients missing or not finite");
+    if (!h->have_sl) return fvm_fail(BTE_ERR_STATE, "bte_fvm_sl_step: no semi-Lagrangian grid set");
+    if (!h->have_inverse) return fvm_fail(BTE_ERR_STATE, "bte_fvm_sl_step: no collision inverse set");
+    if (V == Y || V == h->A || Y == h->A) return fvm_fail(BTE_ERR_ARG, "bte_fvm_sl_step: Y must not alias V");
+    cudaSetDevice(h->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (int rc = fvm_sl(h, coef_of(c), E, V, h->A, s)) return rc;
+    return fvm_coll_solve(h, h->A, Y, s);
 }
 
 int bte_fvm_step(bte_fvm* h, const bte_fvm_coef* c, double alpha, const double* E, double* V, double rtol, double atol,

@@ -98,6 +98,88 @@ FVM_HD double fvm_coll_apply_at(const FvmView& v, const double* dinv, const doub
 }
 
 // ---------------------------------------------------------------------------------------
+// Semi-Lagrangian advection (step_adv_vx_sl, bte_1d3v_solver.py:2244-2314): each value is the
+// trilinear interpolant, on the grid padded by one layer in v_r and theta, at its departure
+// point over one step; zero where the departure point leaves the padded grid.
+// ---------------------------------------------------------------------------------------
+struct FvmSl {
+    int Nr, Nvt, Nx;
+    const double* vr;     // Nr cell centres
+    const double* vt;     // Nvt ordinates (pi ... 0)
+    const double* cos_t;  // Nvt
+    const double* vrp;    // Nr + 2: vmin, vr, vmax
+    const double* vta;    // Nvt + 2: 0, vt reversed, pi (ascending)
+    const double* x;      // Nx points, ascending
+    double vmin;
+    double cX;            // dt tau vth / L
+    double cE;            // dt tau qe / (me vth)
+};
+
+// value of the padded grid at (a, b, x): a in [0, Nr + 1] along vrp, b in [0, Nvt + 1] along
+// the reference's descending theta order (b = 0 is theta = pi); V (Nr, Nvt, Nx). The v_r = vmin
+// layer and the theta = pi, 0 layers are linear extrapolations (:2286-2296); v_r = vmax is zero.
+FVM_HD double fvm_sl_pad(const FvmSl& s, const double* V, int a, int b, int x) {
+    const int Nr = s.Nr, Nvt = s.Nvt, Nx = s.Nx;
+    if (a == Nr + 1) return 0.0;
+    const double pi = 3.14159265358979323846;
+    auto at = [&](int r, int j) { return V[((size_t)r * Nvt + j) * Nx + x]; };
+    if (a >= 1) {
+        const int r = a - 1;
+        if (b >= 1 && b <= Nvt) return at(r, b - 1);
+        if (b == 0) return at(r, 0) + (pi - s.vt[0]) * ((at(r, 1) - at(r, 0)) / (s.vt[1] - s.vt[0]));
+        return at(r, Nvt - 1) - s.vt[Nvt - 1] * ((at(r, Nvt - 1) - at(r, Nvt - 2)) / (s.vt[Nvt - 1] - s.vt[Nvt - 2]));
+    }
+    const double cr = s.vr[0] - s.vmin, hr = s.vr[1] - s.vr[0];
+    if (b >= 1 && b <= Nvt) return at(0, b - 1) - cr * ((at(1, b - 1) - at(0, b - 1)) / hr);
+    if (b == 0)
+        return at(0, 0) - cr * ((at(1, 0) - at(0, 0)) / hr) + (pi - s.vt[0]) * ((at(0, 1) - at(0, 0)) / (s.vt[1] - s.vt[0]));
+    return at(0, Nvt - 1) - cr * ((at(1, Nvt - 1) - at(0, Nvt - 1)) / hr) -
+           s.vt[Nvt - 1] * ((at(0, Nvt - 1) - at(0, Nvt - 2)) / (s.vt[Nvt - 1] - s.vt[Nvt - 2]));
+}
+
+// i in [0, n - 2] with g[i] < q <= g[i + 1] (i = 0 at q = g[0]) on an ascending grid of n points
+FVM_HD int fvm_cell(const double* g, int n, double q) {
+    int a = 0, b = n;
+    while (a < b) {
+        const int m = (a + b) >> 1;
+        if (g[m] < q) a = m + 1;
+        else b = m;
+    }
+    return a - 1 < 0 ? 0 : (a - 1 > n - 2 ? n - 2 : a - 1);
+}
+
+FVM_HD double fvm_sl_at(const FvmSl& s, const double* E, const double* V, int r, int j, int x) {
+    const double vrc = s.vr[r] * s.cos_t[j];
+    const double dE = s.cE * E[x];
+    const double xa = s.x[x] - s.cX * vrc;
+    const double va = sqrt(s.vr[r] * s.vr[r] + 2.0 * vrc * dE + dE * dE);
+    // |cos| <= 1 up to rounding; held in [-1, 1] so that acos is defined
+    const double ca = fmin(1.0, fmax(-1.0, (vrc + dE) / va));
+    const double ta = acos(ca);
+    const int nr = s.Nr + 2, nt = s.Nvt + 2;
+    if (!(va >= s.vrp[0] && va <= s.vrp[nr - 1] && ta >= s.vta[0] && ta <= s.vta[nt - 1] && xa >= s.x[0] &&
+          xa <= s.x[s.Nx - 1]))
+        return 0.0;
+    const int ir = fvm_cell(s.vrp, nr, va), it = fvm_cell(s.vta, nt, ta), ix = fvm_cell(s.x, s.Nx, xa);
+    const double tr = (va - s.vrp[ir]) / (s.vrp[ir + 1] - s.vrp[ir]);
+    const double tt = (ta - s.vta[it]) / (s.vta[it + 1] - s.vta[it]);
+    const double tx = (xa - s.x[ix]) / (s.x[ix + 1] - s.x[ix]);
+    double out = 0.0;
+    for (int a = 0; a < 2; ++a) {
+        const double wa = a ? tr : 1.0 - tr;
+        for (int b = 0; b < 2; ++b) {
+            const double wb = b ? tt : 1.0 - tt;
+            const int bd = (nt - 1) - (it + b);   // ascending theta index -> the padded grid's order
+            for (int c = 0; c < 2; ++c) {
+                const double wc = c ? tx : 1.0 - tx;
+                out += wa * wb * wc * fvm_sl_pad(s, V, ir + a, bd, ix + c);
+            }
+        }
+    }
+    return out;
+}
+
+// ---------------------------------------------------------------------------------------
 // Restarted right-preconditioned GMRES(m) (the reference's utils.py:1172-1262 solves the same
 // system): x0 = M^-1 b, classical Gram-Schmidt applied twice, Givens rotations, the residual
 // recomputed at each restart. Ops supplies N, the vectors B (right-hand side), X (solution),

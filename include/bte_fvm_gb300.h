@@ -10,7 +10,7 @@
  * Replaces, in BESolver/python/bte_1d3v_solver.py: the fully implicit branch of step()
  * (:1890-2009) with rhs_mvec (:1915-1955) and its op-split preconditioner
  * (step_op_split, :1745-1870); the dense collision inverse PmatC of init() (:1346-1375) is
- * passed in factored form. */
+ * passed in factored form; the semi-Lagrangian step (:2024-2027, step_adv_vx_sl :2244-2314). */
 #ifndef BTE_FVM_GB300_H
 #define BTE_FVM_GB300_H
 #ifdef __cplusplus
@@ -57,6 +57,19 @@ int bte_fvm_precond(bte_fvm* h, double cE, double ax, double hstep, const double
  * info4: iterations, ||r||, ||r|| / ||b||, status (0 converged, 1 not converged). */
 int bte_fvm_step(bte_fvm* h, const bte_fvm_coef* c, double alpha, const double* E, double* V, double rtol, double atol,
                  int restart, int max_iter, double* info4, void* stream);
+
+/* The grids of the semi-Lagrangian step: x [Nx] ascending, the velocity domain [vmin, vmax]
+ * of the cells (the basis's knot domain). */
+int bte_fvm_set_sl_grid(bte_fvm* h, const double* x, double vmin, double vmax);
+
+/* Y = step_adv_vx_sl(V) (:2244-2314): each value the trilinear interpolant of V, on the grid
+ * padded by one layer in v_r and theta, at its departure point (x - dt ax v_r cos(theta) in x;
+ * the velocity shifted by dt tau cA E along the field axis); zero outside the padded grid. */
+int bte_fvm_sl_advect(bte_fvm* h, const bte_fvm_coef* c, const double* E, const double* V, double* Y, void* stream);
+
+/* One semi-Lagrangian step (solver_type "sl_implicit", :2024-2027): the collision inverse of
+ * bte_fvm_set_collision_inverse applied to step_adv_vx_sl(V). Y must not alias V. */
+int bte_fvm_sl_step(bte_fvm* h, const bte_fvm_coef* c, const double* E, const double* V, double* Y, void* stream);
 
 /* kernel launches issued by this handle so far */
 long long bte_fvm_launches(const bte_fvm* h);

@@ -293,3 +293,68 @@ def implicit_step(g, A_Ep, A_En, xshift, E, v, dt):
     for k in range(n):
         M[:, k] = implicit_matvec(g, A_Ep, A_En, xshift, E, I[:, k], dt).reshape(-1)
     return np.linalg.solve(M, implicit_rhs(g, v).reshape(-1)).reshape(-1, int(g["Nx"]))
+
+
+# ----------------------------------------------------------------------------------
+# The semi-Lagrangian step (bte_1d3v_solver.py:2024-2027, 2244-2314)
+# ----------------------------------------------------------------------------------
+def sl_padded(v, vr, vt, vmin):
+    """The grid values padded by one layer in v_r and theta (:2282-2306): the v_r = vmin layer by
+    linear extrapolation from the first two cells, the theta = pi and theta = 0 layers by linear
+    extrapolation along theta (corners of the vmin layer add both terms), the v_r = vmax layer zero.
+    v: (Nr, Nvt, Nx) -> (Nr + 2, Nvt + 2, Nx) with grids vrp (ascending) and vtp (pi ... 0)."""
+    Nr, Nvt, Nx = v.shape
+    y = np.zeros((Nr + 2, Nvt + 2, Nx))
+    y[1:-1, 1:-1] = v
+    dr = (vr[0] - vmin) * (v[1] - v[0]) / (vr[1] - vr[0])          # (Nvt, Nx)
+    y[0, 1:-1] = v[0] - dr
+    y[0, 0] = v[0, 0] - dr[0] + (np.pi - vt[0]) * (v[0, 1] - v[0, 0]) / (vt[1] - vt[0])
+    y[0, -1] = v[0, -1] - dr[-1] - vt[-1] * (v[0, -1] - v[0, -2]) / (vt[-1] - vt[-2])
+    y[1:-1, 0] = v[:, 0] + (np.pi - vt[0]) * (v[:, 1] - v[:, 0]) / (vt[1] - vt[0])
+    y[1:-1, -1] = v[:, -1] - vt[-1] * (v[:, -1] - v[:, -2]) / (vt[-1] - vt[-2])
+    return y
+
+
+def sl_departure(vr, vt, x, E, dt, tau, vth, L, qe, me):
+    """Departure points of each (r, j, x) value over one step (:2267-2278): x - dt tau vth / L
+    v_r cos(theta), and the velocity (v_r, theta) shifted by dtE = dt tau qe / (me vth) E along
+    the field axis. Returns (vr_ap, vt_ap, x_ap), each (Nr, Nvt, Nx)."""
+    vrc = vr[:, None, None] * np.cos(vt)[None, :, None] * np.ones(len(x))[None, None, :]
+    dtE = (dt * tau * qe / me / vth) * np.ones((len(vr), len(vt)))[:, :, None] * np.asarray(E)[None, None, :]
+    x_ap = x[None, None, :] - (dt * tau * vth / L) * vrc
+    vr_ap = np.sqrt((vr ** 2)[:, None, None] * np.ones((1, len(vt), len(x))) + 2 * vrc * dtE + dtE ** 2)
+    vt_ap = np.arccos((vrc + dtE) / vr_ap)
+    return vr_ap, vt_ap, x_ap
+
+
+def _cell(grid, q):
+    """Index i and fraction t with q = grid[i] + t (grid[i+1] - grid[i]), for an ascending grid;
+    inside is False outside [grid[0], grid[-1]]."""
+    i = np.clip(np.searchsorted(grid, q, side="left") - 1, 0, len(grid) - 2)
+    t = (q - grid[i]) / (grid[i + 1] - grid[i])
+    inside = (q >= grid[0]) & (q <= grid[-1])
+    return i, t, inside
+
+
+def sl_advect(v, vr, vt, x, E, dt, tau, vth, L, qe, me, vmin, vmax):
+    """step_adv_vx_sl (:2244-2314): v (Nr * Nvt, Nx) interpolated trilinearly at the departure
+    points on the padded grid, zero where a departure point leaves it."""
+    Nr, Nvt, Nx = len(vr), len(vt), len(x)
+    Y = sl_padded(np.asarray(v).reshape(Nr, Nvt, Nx), vr, vt, vmin)
+    vrp = np.concatenate([[vmin], vr, [vmax]])
+    vta = np.concatenate([[0.0], vt[::-1], [np.pi]])    # ascending theta; Y's theta axis reversed
+    Ya = Y[:, ::-1, :]
+    vr_ap, vt_ap, x_ap = sl_departure(vr, vt, x, E, dt, tau, vth, L, qe, me)
+    ir, tr, ok_r = _cell(vrp, vr_ap)
+    it, tt, ok_t = _cell(vta, vt_ap)
+    ix, tx, ok_x = _cell(np.asarray(x), x_ap)
+    out = np.zeros_like(vr_ap)
+    for a in (0, 1):
+        wa = tr if a else 1.0 - tr
+        for b in (0, 1):
+            wb = tt if b else 1.0 - tt
+            for c in (0, 1):
+                wc = tx if c else 1.0 - tx
+                out += wa * wb * wc * Ya[ir + a, it + b, ix + c]
+    out[~(ok_r & ok_t & ok_x)] = 0.0
+    return out.reshape(Nr * Nvt, Nx)

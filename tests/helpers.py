@@ -53,3 +53,6 @@ FVM_IMPLICIT_PARAMS = dict(L=2.54e-2, V0=100.0, freq=13.56e6, Tg=300.0, p0=1.0, 
                            Np=12, Nr=7, Nvt=8, lmax=1, dt=1e-3, ev_max=80.0, ev_extend=0, sp_order=3, spline_qpts=5,
                            Te=4.0, xspace_type=0, vspace_type=0, solver_type="fully_implicit", adaptive_grid=1, pvr=2,
                            pvt=2, px=2, rtol=1e-12, atol=1e-14, ic_file="")
+
+# the semi-Lagrangian fixture's table (tests/golden/make_golden_fvm_sl.py)
+FVM_SL_PARAMS = dict(FVM_IMPLICIT_PARAMS, solver_type="sl_implicit", dt=5e-3)

@@ -177,6 +177,26 @@ void fvm_host_precond(const int* dims, const double* vr, const double* vt, const
     precond(s, dinv, H, cE, ax, hstep, E, X, Y);
 }
 
+// the semi-Lagrangian advection: Y = step_adv_vx_sl(V); dims: Nr, Nvt, Nx
+void fvm_host_sl(const int* dims, const double* vr, const double* vt, const double* x, double vmin, double vmax,
+                 double cX, double cE, const double* E, const double* V, double* Y) {
+    const int Nr = dims[0], Nvt = dims[1], Nx = dims[2];
+    std::vector<double> cth(Nvt), vrp(Nr + 2), vta(Nvt + 2);
+    for (int j = 0; j < Nvt; ++j) cth[j] = cos(vt[j]);
+    vrp[0] = vmin;
+    vrp[Nr + 1] = vmax;
+    for (int r = 0; r < Nr; ++r) vrp[r + 1] = vr[r];
+    vta[0] = 0.0;
+    vta[Nvt + 1] = 3.14159265358979323846;
+    for (int j = 0; j < Nvt; ++j) vta[j + 1] = vt[Nvt - 1 - j];
+    FvmSl s;
+    s.Nr = Nr; s.Nvt = Nvt; s.Nx = Nx; s.vr = vr; s.vt = vt; s.cos_t = cth.data(); s.vrp = vrp.data();
+    s.vta = vta.data(); s.x = x; s.vmin = vmin; s.cX = cX; s.cE = cE;
+    for (int r = 0; r < Nr; ++r)
+        for (int j = 0; j < Nvt; ++j)
+            for (int i = 0; i < Nx; ++i) Y[((size_t)r * Nvt + j) * Nx + i] = fvm_sl_at(s, E, V, r, j, i);
+}
+
 // V replaced by the step's solution; info4 as bte_fvm_step's
 int fvm_host_step(const int* dims, const double* vr, const double* vt, const double* w, const double* loss,
                   const double* gain, const double* const* bands, const double* dinv, const double* H, const double* c6,

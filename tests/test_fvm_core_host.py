@@ -111,3 +111,40 @@ def test_gmres_step_matches_the_reference(harness, case, restart):
     assert 0 < info[0] <= 400
     ref = g["step"]
     assert np.max(np.abs(V - ref)) <= 1e-10 * np.max(np.abs(ref))
+
+
+def test_semi_lagrangian_advection_matches_the_reference(harness):
+    """step_adv_vx_sl: the departure points, the padded grid and the trilinear interpolation of
+    the shared core against the reference's own interpolation (SciPy interpn on its CPU path)."""
+    g = dict(np.load(os.path.join(HERE, "golden", "fvm_sl_reference.npz")))
+    dims = (C.c_int * 3)(int(g["Nr"]), int(g["Nvt"]), int(g["Nx"]))
+    keep = [np.ascontiguousarray(g[k], dtype=np.float64) for k in ("vr", "vt", "x", "E", "v0")]
+    dt, tau, vth = float(g["dt"]), float(g["tau"]), float(g["vth"])
+    cX = dt * tau * vth / float(g["L"])
+    cE = dt * tau * float(g["qe"]) / float(g["me"]) / vth
+    Y = np.zeros_like(keep[4])
+    harness.fvm_host_sl(dims, *[_d(a)[1] for a in keep[:3]], C.c_double(float(g["kdomain"][0])),
+                        C.c_double(float(g["kdomain"][1])), C.c_double(cX), C.c_double(cE), _d(keep[3])[1],
+                        _d(keep[4])[1], Y.ctypes.data_as(C.POINTER(C.c_double)))
+    assert np.max(np.abs(Y - g["v_sl"])) <= 1e-13 * np.max(np.abs(g["v_sl"]))
+    assert (Y == 0.0).any()          # departure points outside the domain (inflow)
+
+
+def test_semi_lagrangian_step_matches_the_reference(harness, synthetic_xs):
+    """The step: the shared core's advection, then the product's closed-form collision inverse
+    built from the fixture's parameter table, against the reference's PmatC v_sl."""
+    from helpers import FVM_SL_PARAMS
+    g = dict(np.load(os.path.join(HERE, "golden", "fvm_sl_reference.npz")))
+    st = P.fvm_setup(dict(FVM_SL_PARAMS, collisions=synthetic_xs))
+    p = st.params
+    dt = float(p.dt)
+    c6 = P.step_coefficients(p, st.vth, dt, dt)
+    dims = (C.c_int * 3)(len(st.vr), len(st.vt), len(st.x))
+    keep = [np.ascontiguousarray(a, dtype=np.float64) for a in (st.vr, st.vt, st.x, g["E"], g["v0"])]
+    Y = np.zeros_like(keep[4])
+    harness.fvm_host_sl(dims, *[_d(a)[1] for a in keep[:3]], C.c_double(0.0), C.c_double(st.vmax),
+                        C.c_double(dt * c6[5]), C.c_double(dt * c6[2] * c6[4]), _d(keep[3])[1], _d(keep[4])[1],
+                        Y.ctypes.data_as(C.POINTER(C.c_double)))
+    assert np.max(np.abs(Y - g["v_sl"])) <= 1e-13 * np.max(np.abs(g["v_sl"]))
+    y = st.collisions.inverse_dense(dt * c6[2] * c6[3]) @ Y
+    assert np.max(np.abs(y - g["step"])) <= 1e-12 * np.max(np.abs(g["step"]))

@@ -133,3 +133,14 @@ def test_implicit_matvec_rhs_and_step_match_the_reference(gi):
 def test_implicit_preconditioner_is_the_op_split_step(g, gi):
     Mu = F.op_split_step(g, gi["E"], gi["u"].reshape(-1, int(g["Nx"])), float(g["dt"]))
     assert np.max(np.abs(Mu.reshape(-1) - gi["Mu"])) <= 1e-13 * np.max(np.abs(gi["Mu"]))
+
+
+def test_semi_lagrangian_step_matches_the_reference():
+    """The oracle's explicit trilinear interpolation at the departure points against the
+    reference's own step_adv_vx_sl (SciPy interpn) and step (PmatC v_sl)."""
+    gs = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "fvm_sl_reference.npz")))
+    v_sl = F.sl_advect(gs["v0"], gs["vr"], gs["vt"], gs["x"], gs["E"], float(gs["dt"]), float(gs["tau"]),
+                       float(gs["vth"]), float(gs["L"]), float(gs["qe"]), float(gs["me"]), float(gs["kdomain"][0]),
+                       float(gs["kdomain"][1]))
+    assert np.max(np.abs(v_sl - gs["v_sl"])) <= 1e-14 * np.max(np.abs(gs["v_sl"]))
+    assert np.max(np.abs(gs["PmatC"] @ v_sl - gs["step"])) <= 1e-14 * np.max(np.abs(gs["step"]))

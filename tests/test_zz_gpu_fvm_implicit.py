@@ -63,3 +63,18 @@ def test_step_before_init_is_refused(synthetic_xs):
     s = bte_1d3v_fvm(dict(PARAMS, collisions=synthetic_xs))
     with pytest.raises(RuntimeError):
         s.step(np.ones(s.dof_x), np.ones((s.dof_v, s.dof_x)), None, 0.0, 1e-3)
+
+
+def test_semi_lagrangian_step_matches_the_reference(synthetic_xs):
+    """solver_type "sl_implicit": the advection (step_adv_vx_sl) and the step against the
+    reference's (tests/golden/fvm_sl_reference.npz)."""
+    from boltzmann_gb300.bte_1d3v_fvm import bte_1d3v_fvm
+    from helpers import FVM_SL_PARAMS
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "fvm_sl_reference.npz")))
+    s = bte_1d3v_fvm(dict(FVM_SL_PARAMS, collisions=synthetic_xs))
+    dt = float(g["dt"])
+    s.init(dt)
+    v_sl = s.step_adv_vx_sl(g["E"], g["v0"], 0.0, dt).cpu().numpy()
+    assert _rel(v_sl, g["v_sl"]) <= 1e-13
+    y = s.step(g["E"], g["v0"], None, 0.0, dt).cpu().numpy()
+    assert _rel(y, g["step"]) <= 1e-12
