@@ -135,7 +135,7 @@ def load() -> C.CDLL:
     lib.bte_fvm_set_collision_inverse.argtypes = [vp, dp, dp]
     lib.bte_fvm_mvec.argtypes = [vp, C.POINTER(FvmCoef), vp, vp, vp, vp]
     lib.bte_fvm_precond.argtypes = [vp, C.c_double, C.c_double, C.c_double, vp, vp, vp, vp]
-    lib.bte_fvm_step.argtypes = [vp, C.POINTER(FvmCoef), C.c_double, vp, vp, C.c_double, C.c_double, ci, ci, dp, vp]
+    lib.bte_fvm_step.argtypes = [vp, C.POINTER(FvmCoef), C.c_double, ci, vp, vp, C.c_double, C.c_double, ci, ci, dp, vp]
     lib.bte_fvm_set_sl_grid.argtypes = [vp, dp, C.c_double, C.c_double]
     lib.bte_fvm_sl_advect.argtypes = [vp, C.POINTER(FvmCoef), vp, vp, vp, vp]
     lib.bte_fvm_sl_step.argtypes = [vp, C.POINTER(FvmCoef), vp, vp, vp, vp]

@@ -421,13 +421,14 @@ class FvmImplicit:
                                                _ptr(Y), _stream()), "bte_fvm_precond")
         return Y.reshape(self.Nr * self.Nvt, self.Nx)
 
-    def step(self, coef, E, V, alpha=1.0, rtol=1e-12, atol=1e-14, restart=30, max_iter=600):
-        """Solve rhs_mvec(V') = V (inflow values zeroed); returns V' (Nr * Nvt, Nx)."""
+    def step(self, coef, E, V, alpha=1.0, rtol=1e-12, atol=1e-14, restart=30, max_iter=600, pc_left=False):
+        """Solve rhs_mvec(V') = V (inflow values zeroed), the op-split preconditioner on the right
+        or (pc_left) on the left; returns V' (Nr * Nvt, Nx)."""
         n = self.Nr * self.Nvt * self.Nx
         Vd, Ed = self._dev(V, n).clone(), self._dev(E, self.Nx)
         info = (C.c_double * 4)()
-        rc = _lib.load().bte_fvm_step(self._h, C.byref(coef), float(alpha), _ptr(Ed), _ptr(Vd), float(rtol),
-                                      float(atol), int(restart), int(max_iter), info, _stream())
+        rc = _lib.load().bte_fvm_step(self._h, C.byref(coef), float(alpha), int(bool(pc_left)), _ptr(Ed), _ptr(Vd),
+                                      float(rtol), float(atol), int(restart), int(max_iter), info, _stream())
         self._fail(rc, "bte_fvm_step")
         self.gmres_info = {"iterations": int(info[0]), "residual_abs": info[1], "residual_rel": info[2],
                            "status": int(info[3])}
@@ -579,17 +580,16 @@ class bte_1d3v_fvm:
 
     def step(self, E, v, dv, time, dt, verbose=0, gmres_pc_vr=1.0, gmres_pc_vt=1.0, pc_left=False):
         """step (:1872-2030): the fully implicit solve (GMRES preconditioned by the op-split
-        step at gmres_pc_vr dt); with solver_type "XVTVRC" one op-split step; with "sl_implicit"
-        the collision inverse of the semi-Lagrangian advection (:2024-2027)."""
+        step at gmres_pc_vr dt, on the left when pc_left); with solver_type "XVTVRC" one op-split
+        step; with "sl_implicit" the collision inverse of the semi-Lagrangian advection
+        (:2024-2027)."""
         p = self.params
         if p.solver == "op_split":
             return self.step_op_split(E, v, dv, time, dt, XVTVRC, verbose)
         if p.solver == "semi_lagrangian":
             return self.solver.sl_step(self._coef(dt), E, v)
-        if pc_left:
-            raise NotImplementedError("only right preconditioning is provided")
         out = self.solver.step(self._coef(dt), E, v, alpha=gmres_pc_vr, rtol=p.rtol, atol=p.atol,
-                               restart=p.gmres_rsrt, max_iter=p.gmres_maxiter)
+                               restart=p.gmres_rsrt, max_iter=p.gmres_maxiter, pc_left=pc_left)
         info = self.solver.gmres_info
         self.gmres_info = info
         if info["status"] != 0:

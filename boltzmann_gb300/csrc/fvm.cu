@@ -500,8 +500,8 @@ int bte_fvm_sl_step(bte_fvm* h, const bte_fvm_coef* c, const double* E, const do
     return fvm_coll_solve(h, h->A, Y, s);
 }
 
-int bte_fvm_step(bte_fvm* h, const bte_fvm_coef* c, double alpha, const double* E, double* V, double rtol, double atol,
-                 int restart, int max_iter, double* info4, void* stream) {
+int bte_fvm_step(bte_fvm* h, const bte_fvm_coef* c, double alpha, int pc_left, const double* E, double* V, double rtol,
+                 double atol, int restart, int max_iter, double* info4, void* stream) {
     if (!h || !E || !V || !info4) return fvm_fail(BTE_ERR_ARG, "bte_fvm_step: null argument");
     if (!coef_ok(c) || !std::isfinite(alpha)) return fvm_fail(BTE_ERR_ARG, "bte_fvm_step: coefficients not finite");
     if (restart < 1 || restart > 500 || max_iter < 0) return fvm_fail(BTE_ERR_ARG, "bte_fvm_step: 1 <= restart <= 500");
@@ -537,7 +537,9 @@ int bte_fvm_step(bte_fvm* h, const bte_fvm_coef* c, double alpha, const double* 
     if (int rc = sweep_rc(bte_fvm_inflow_zero(h->Nr, h->Nvt, h->Nx, h->vt, h->B, s), "inflow")) return rc;
     DeviceOps op{h, s, fc, E, alpha * fc.dt, N, h->B, h->X, h->R, h->W, h->Z, h->Tv, h->Kr};
     FvmGmresInfo info{};
-    if (int rc = fvm_gmres(op, restart, rtol, atol, max_iter, &info)) return rc;
+    if (int rc = pc_left ? fvm_gmres_left(op, restart, rtol, atol, max_iter, &info)
+                         : fvm_gmres(op, restart, rtol, atol, max_iter, &info))
+        return rc;
     if (cudaMemcpyAsync(V, h->X, N * 8, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
         return fvm_fail(BTE_ERR_CUDA, "bte_fvm_step: copy of the solution failed");

@@ -271,3 +271,104 @@ int fvm_gmres(Ops& op, int m, double rtol, double atol, int max_iter, FvmGmresIn
     info->bnorm = bnorm;
     return 0;
 }
+
+// Left-preconditioned restarted GMRES (the reference's gmres_pcl, utils.py:1266-1357): x0 = 0,
+// the Krylov space of M^-1 A from M^-1 r0, and, as the reference does, the true residual
+// ||b - A x|| of each iterate checked against max(atol, rtol ||b||) (one extra operator
+// application per iteration). Same Ops as fvm_gmres.
+template <class Ops>
+int fvm_gmres_left(Ops& op, int m, double rtol, double atol, int max_iter, FvmGmresInfo* info) {
+    const size_t N = op.N;
+    int rc;
+    double bnorm = 0.0;
+    if ((rc = op.dots(1, op.B, op.B, &bnorm))) return rc;
+    bnorm = sqrt(bnorm);
+    const double tol = std::max(atol, rtol * bnorm);
+    if ((rc = op.scale(0.0, op.B, op.X))) return rc;
+    int it = 0;
+    double rnorm = 0.0;
+    bool conv = false;
+    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), hh(m + 1), y(m);
+    auto solve_y = [&](int k) {
+        for (int i = k - 1; i >= 0; --i) {
+            double acc = g[i];
+            for (int j = i + 1; j < k; ++j) acc -= H[(size_t)i * m + j] * y[j];
+            y[i] = H[(size_t)i * m + i] != 0.0 ? acc / H[(size_t)i * m + i] : 0.0;
+        }
+    };
+    while (true) {
+        if ((rc = op.matvec(op.X, op.W))) return rc;
+        if ((rc = op.sub(op.B, op.W, op.R))) return rc;
+        if ((rc = op.dots(1, op.R, op.R, &rnorm))) return rc;
+        rnorm = sqrt(rnorm);
+        if (rnorm <= tol) {
+            conv = true;
+            break;
+        }
+        if (it >= max_iter) break;
+        if ((rc = op.precond(op.R, op.Z))) return rc;
+        double beta = 0.0;
+        if ((rc = op.dots(1, op.Z, op.Z, &beta))) return rc;
+        beta = sqrt(beta);
+        if (!(beta > 0.0)) break;
+        if ((rc = op.scale(1.0 / beta, op.Z, op.Kr))) return rc;
+        std::fill(g.begin(), g.end(), 0.0);
+        g[0] = beta;
+        int k = 0;
+        bool done = false;
+        for (; k < m && it < max_iter; ++k, ++it) {
+            double* vk = op.Kr + (size_t)k * N;
+            double* vk1 = vk + N;
+            if ((rc = op.matvec(vk, op.W))) return rc;
+            if ((rc = op.precond(op.W, vk1))) return rc;
+            for (int pass = 0; pass < 2; ++pass) {
+                if ((rc = op.dots(k + 1, op.Kr, vk1, hh.data()))) return rc;
+                if ((rc = op.sub_combo(k + 1, op.Kr, hh.data(), vk1))) return rc;
+                for (int j = 0; j <= k; ++j) H[(size_t)j * m + k] = (pass == 0 ? 0.0 : H[(size_t)j * m + k]) + hh[j];
+            }
+            double nn = 0.0;
+            if ((rc = op.dots(1, vk1, vk1, &nn))) return rc;
+            nn = sqrt(nn);
+            H[(size_t)(k + 1) * m + k] = nn;
+            if (nn > 0.0 && (rc = op.scale(1.0 / nn, vk1, vk1))) return rc;
+            for (int j = 0; j < k; ++j) {
+                const double a = H[(size_t)j * m + k], b = H[(size_t)(j + 1) * m + k];
+                H[(size_t)j * m + k] = cs[j] * a + sn[j] * b;
+                H[(size_t)(j + 1) * m + k] = -sn[j] * a + cs[j] * b;
+            }
+            const double a = H[(size_t)k * m + k], b = H[(size_t)(k + 1) * m + k];
+            const double rr = hypot(a, b);
+            cs[k] = rr > 0.0 ? a / rr : 1.0;
+            sn[k] = rr > 0.0 ? b / rr : 0.0;
+            H[(size_t)k * m + k] = rr;
+            H[(size_t)(k + 1) * m + k] = 0.0;
+            g[k + 1] = -sn[k] * g[k];
+            g[k] = cs[k] * g[k];
+            // the iterate x + V y and its true residual
+            solve_y(k + 1);
+            if ((rc = op.combo(k + 1, op.Kr, y.data(), op.T))) return rc;
+            if ((rc = op.axpy(1.0, op.X, op.T))) return rc;
+            if ((rc = op.matvec(op.T, op.W))) return rc;
+            if ((rc = op.sub(op.B, op.W, op.R))) return rc;
+            if ((rc = op.dots(1, op.R, op.R, &rnorm))) return rc;
+            rnorm = sqrt(rnorm);
+            if (rnorm <= tol || nn == 0.0) {
+                ++k;
+                ++it;
+                done = rnorm <= tol;
+                break;
+            }
+        }
+        // restart from the last iterate
+        if ((rc = op.scale(1.0, op.T, op.X))) return rc;
+        if (done) {
+            conv = true;
+            break;
+        }
+    }
+    info->iterations = it;
+    info->converged = conv ? 1 : 0;
+    info->rnorm = rnorm;
+    info->bnorm = bnorm;
+    return 0;
+}

@@ -52,11 +52,12 @@ int bte_fvm_precond(bte_fvm* h, double cE, double ax, double hstep, const double
                     void* stream);
 
 /* One fully implicit step (:1890-2009): solves rhs_mvec(V') = V with its inflow values zeroed,
- * by restarted GMRES(restart) right-preconditioned with the op-split step at alpha dt, to
+ * by restarted GMRES(restart) preconditioned with the op-split step at alpha dt, on the right
+ * (pc_left = 0; utils.py:1172-1262) or on the left (pc_left = 1; utils.py:1266-1357), to
  * ||r|| <= max(atol, rtol ||b||) or max_iter iterations; V [Nr * Nvt * Nx] is replaced by V'.
  * info4: iterations, ||r||, ||r|| / ||b||, status (0 converged, 1 not converged). */
-int bte_fvm_step(bte_fvm* h, const bte_fvm_coef* c, double alpha, const double* E, double* V, double rtol, double atol,
-                 int restart, int max_iter, double* info4, void* stream);
+int bte_fvm_step(bte_fvm* h, const bte_fvm_coef* c, double alpha, int pc_left, const double* E, double* V, double rtol,
+                 double atol, int restart, int max_iter, double* info4, void* stream);
 
 /* The grids of the semi-Lagrangian step: x [Nx] ascending, the velocity domain [vmin, vmax]
  * of the cells (the basis's knot domain). */

@@ -200,8 +200,8 @@ void fvm_host_sl(const int* dims, const double* vr, const double* vt, const doub
 // V replaced by the step's solution; info4 as bte_fvm_step's
 int fvm_host_step(const int* dims, const double* vr, const double* vt, const double* w, const double* loss,
                   const double* gain, const double* const* bands, const double* dinv, const double* H, const double* c6,
-                  double alpha, const double* E, double* V, double rtol, double atol, int restart, int max_iter,
-                  double* info4) {
+                  double alpha, int pc_left, const double* E, double* V, double rtol, double atol, int restart,
+                  int max_iter, double* info4) {
     Setup s = make_setup(dims[0], dims[1], dims[2], dims[3], dims[4], dims[5], vr, vt, w, loss, gain, bands);
     const FvmCoef c = coef(c6);
     const size_t N = (size_t)dims[0] * dims[1] * dims[2];
@@ -211,7 +211,8 @@ int fvm_host_step(const int* dims, const double* vr, const double* vt, const dou
     HostOps op{&s, c, E, dinv, H, c.tau * c.cA, alpha * c.dt, N, B.data(), X.data(), R.data(), W.data(), Z.data(),
                T.data(), Kr.data()};
     FvmGmresInfo info{};
-    const int rc = fvm_gmres(op, restart, rtol, atol, max_iter, &info);
+    const int rc = pc_left ? fvm_gmres_left(op, restart, rtol, atol, max_iter, &info)
+                           : fvm_gmres(op, restart, rtol, atol, max_iter, &info);
     memcpy(V, X.data(), N * sizeof(double));
     info4[0] = info.iterations;
     info4[1] = info.rnorm;

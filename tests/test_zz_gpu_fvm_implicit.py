@@ -49,9 +49,10 @@ def test_preconditioner_matches_the_reference_op_split_step(solver, g):
     assert _rel(Y.reshape(-1), g["Mu"]) <= 1e-12
 
 
-def test_step_matches_the_reference(solver, g):
+@pytest.mark.parametrize("pc_left", [False, True])
+def test_step_matches_the_reference(solver, g, pc_left):
     n0 = solver.launches()
-    y = solver.step(g["E"], g["v0"], None, 0.0, float(g["dt"])).cpu().numpy()
+    y = solver.step(g["E"], g["v0"], None, 0.0, float(g["dt"]), pc_left=pc_left).cpu().numpy()
     assert solver.gmres_info["status"] == 0
     assert 0 < solver.gmres_info["iterations"] <= 100
     assert _rel(y, g["step"]) <= 1e-10
