@@ -152,6 +152,47 @@ struct HostOps {
     int sub(const double* a, const double* b, double* cc) { for (size_t i = 0; i < N; ++i) cc[i] = a[i] - b[i]; return 0; }
 };
 
+// a dense operator with a diagonal preconditioner, for the solver alone
+struct DenseOps {
+    size_t N;
+    const double* A;      // N x N row-major
+    const double* minv;   // N: the preconditioner's diagonal
+    double *B, *X, *R, *W, *Z, *T, *Kr;
+    int matvec(const double* x, double* y) {
+        for (size_t i = 0; i < N; ++i) {
+            double acc = 0.0;
+            for (size_t j = 0; j < N; ++j) acc += A[i * N + j] * x[j];
+            y[i] = acc;
+        }
+        return 0;
+    }
+    int precond(const double* x, double* y) { for (size_t i = 0; i < N; ++i) y[i] = minv[i] * x[i]; return 0; }
+    int dots(int k, const double* V, const double* w, double* out) {
+        for (int j = 0; j < k; ++j) {
+            double acc = 0.0;
+            for (size_t i = 0; i < N; ++i) acc += V[(size_t)j * N + i] * w[i];
+            out[j] = acc;
+        }
+        return 0;
+    }
+    int sub_combo(int k, const double* V, const double* h, double* w) {
+        for (size_t i = 0; i < N; ++i)
+            for (int j = 0; j < k; ++j) w[i] -= h[j] * V[(size_t)j * N + i];
+        return 0;
+    }
+    int combo(int k, const double* V, const double* cc, double* y) {
+        for (size_t i = 0; i < N; ++i) {
+            double acc = 0.0;
+            for (int j = 0; j < k; ++j) acc += cc[j] * V[(size_t)j * N + i];
+            y[i] = acc;
+        }
+        return 0;
+    }
+    int scale(double a, const double* x, double* y) { for (size_t i = 0; i < N; ++i) y[i] = a * x[i]; return 0; }
+    int axpy(double a, const double* x, double* y) { for (size_t i = 0; i < N; ++i) y[i] += a * x[i]; return 0; }
+    int sub(const double* a, const double* b, double* cc) { for (size_t i = 0; i < N; ++i) cc[i] = a[i] - b[i]; return 0; }
+};
+
 FvmCoef coef(const double* c6) {
     FvmCoef c;
     c.dt = c6[0]; c.dtx = c6[1]; c.tau = c6[2]; c.kappa = c6[3]; c.cA = c6[4]; c.ax = c6[5];
@@ -175,6 +216,23 @@ void fvm_host_precond(const int* dims, const double* vr, const double* vt, const
                       double ax, double hstep, const double* E, const double* X, double* Y) {
     Setup s = make_setup(dims[0], dims[1], dims[2], dims[3], dims[4], dims[5], vr, vt, w, loss, gain, bands);
     precond(s, dinv, H, cE, ax, hstep, E, X, Y);
+}
+
+// the solver alone on a dense system A x = b with the preconditioner diag(minv); x out
+int gmres_host_dense(int n, const double* A, const double* minv, const double* b, double* x, int restart, double rtol,
+                     double atol, int max_iter, int pc_left, double* info4) {
+    const size_t N = (size_t)n;
+    std::vector<double> B(b, b + N), X(N), R(N), W(N), Z(N), T(N), Kr((size_t)(restart + 1) * N);
+    DenseOps op{N, A, minv, B.data(), X.data(), R.data(), W.data(), Z.data(), T.data(), Kr.data()};
+    FvmGmresInfo info{};
+    const int rc = pc_left ? fvm_gmres_left(op, restart, rtol, atol, max_iter, &info)
+                           : fvm_gmres(op, restart, rtol, atol, max_iter, &info);
+    memcpy(x, X.data(), N * sizeof(double));
+    info4[0] = info.iterations;
+    info4[1] = info.rnorm;
+    info4[2] = info.bnorm > 0.0 ? info.rnorm / info.bnorm : 0.0;
+    info4[3] = info.converged ? 0.0 : 1.0;
+    return rc;
 }
 
 // the semi-Lagrangian advection: Y = step_adv_vx_sl(V); dims: Nr, Nvt, Nx

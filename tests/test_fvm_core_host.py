@@ -148,3 +148,25 @@ def test_semi_lagrangian_step_matches_the_reference(harness, synthetic_xs):
     assert np.max(np.abs(Y - g["v_sl"])) <= 1e-13 * np.max(np.abs(g["v_sl"]))
     y = st.collisions.inverse_dense(dt * c6[2] * c6[3]) @ Y
     assert np.max(np.abs(y - g["step"])) <= 1e-12 * np.max(np.abs(g["step"]))
+
+
+@pytest.mark.parametrize("pc_left", [1, 0])
+def test_gmres_on_the_reference_test_system(harness, pc_left):
+    """The solver alone on the system of the reference's own GMRES test (test_gmres.py:12-22):
+    A = I + 0.1 U(0,1) (n = 1000), the Jacobi preconditioner, restart 20, rtol 1e-12, against a
+    dense solve; both preconditioner sides (the reference's test runs the left one)."""
+    rng = np.random.default_rng(0)
+    n = 1000
+    A = np.eye(n) + 1e-1 * rng.random((n, n))
+    minv = 1.0 / np.diag(A)
+    b = rng.random(n)
+    x = np.zeros(n)
+    info = (C.c_double * 4)()
+    harness.gmres_host_dense.restype = C.c_int
+    rc = harness.gmres_host_dense(C.c_int(n), _d(A)[1], _d(minv)[1], _d(b)[1], x.ctypes.data_as(C.POINTER(C.c_double)),
+                                  C.c_int(20), C.c_double(1e-12), C.c_double(1e-20), C.c_int(500), C.c_int(pc_left),
+                                  info)
+    assert rc == 0 and info[3] == 0.0, list(info)
+    assert np.linalg.norm(b - A @ x) <= 1e-12 * np.linalg.norm(b) * 1.0001
+    xs = np.linalg.solve(A, b)
+    assert np.max(np.abs(x - xs)) <= 1e-9 * np.max(np.abs(xs))
