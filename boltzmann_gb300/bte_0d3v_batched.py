@@ -28,6 +28,7 @@ import time
 import numpy as np
 
 from . import _lib
+from .bte_1d3v import ME, QE
 from .lxcat import read_available_species, read_cross_section_data
 
 
@@ -86,6 +87,14 @@ def _torch():
 
 def _ptr(t):
     return C.c_void_p(t.data_ptr())
+
+
+def normalization_scale(mass, F, vth):
+    """The per-column scale of normalized_distribution (bte_0d3v_batched.py:1204-1217):
+    (mass . f) / (Y_00 4 pi) * 2 (vth / c_gamma)^3, Y_00 4 pi = sqrt(4 pi). Works on NumPy arrays
+    and on tensors."""
+    c_gamma = np.sqrt(2.0 * QE / ME)
+    return (mass @ F) / np.sqrt(4.0 * np.pi) * (2.0 * (vth / c_gamma) ** 3)
 
 
 class bte_0d3v_batched:
@@ -252,6 +261,74 @@ class bte_0d3v_batched:
                 self._par_bte_params[idx][k] = v.cpu().numpy()
         self.xp_module = np
         prof[pp.D2H].stop()
+
+    # ------------------------------------------------------------------ counts and small utilities
+    def rhs_and_jac_flops(self):
+        """The reference's flop model of one residual and one Jacobian evaluation
+        (bte_0d3v_batched.py:823-854): (res_flops(n, p), jac_flops(n, p)), n unknowns per
+        point, p points; the e-e terms count only with args.ee_collisions = 1. The model counts
+        the reference's own dense products, so it is the common unit of comparison."""
+        s = len(self._avail_species[0])
+        ee = int(getattr(self._args, "ee_collisions", 0)) == 1
+
+        def res_flops(n, p):
+            gam = p * (2 * n - 1) * 2 + 3 * p
+            col = (n - 1) * p * (2 * n - 1) + (2 * s - 1) * (n - 1) * p
+            gas = (n - 1) * p * (2 * n - 1) + (n - 1) * p
+            scl = (n - 1) * p * 3
+            adv = (n - 1) * p * (2 * n - 1) + (n - 1) * p
+            ion = p * (2 * n - 1) + p + (n - 1) * p * (2 * n - 1) + (n - 1) * p
+            cee = n * n * p * (2 * n - 1)
+            cex = n * p * (2 * n - 1) + (n - 1) * p * (2 * n - 1) + (n - 1) * p
+            base = col + gas + scl + adv + ion
+            return base + gam + cee + cex if ee else base
+
+        def jac_flops(n, p):
+            gam = p * (2 * n - 1) * 2 + 3 * p
+            cc = n * n * p * (2 * n - 1) * 2 + n * n * p
+            mu = p * (2 * n - 1) + p
+            lin = (n - 1) * (n - 1) * p * (2 * s - 1) + p * (n - 1) * (n - 1) * 2
+            proj = n * p * (n - 1) * (2 * n - 1) + (n - 1) * (n - 1) * p * (2 * n - 1) + (n - 1) * (n - 1) * p
+            diag = p * (n - 1) * (n - 1)
+            return gam + cc + mu + lin + proj + diag if ee else mu + lin + diag
+
+        return res_flops, jac_flops
+
+    def normalized_distribution(self, grid_idx: int, ff):
+        """bte_0d3v_batched.py:1204-1217: each column of ff (n, n_pts) divided by its mass
+        functional in the reference's units, (mass . f) / sqrt(4 pi) * 2 (vth / c_gamma)^3."""
+        torch = _torch()
+        on_host = not torch.is_tensor(ff)
+        F = self._dev(ff)
+        mass = self.export_operator(grid_idx, "MASS_VEC")
+        out = F / normalization_scale(mass, F, self._grid_info[grid_idx]["vth"])
+        return out.cpu().numpy() if on_host else out
+
+    def batched_inv(self, grid_idx, Jmat):
+        """bte_0d3v_batched.py:856-880: the inverses of a stack of dense matrices (P, m, m), from
+        the library's batched FP64 LU (bte_lu_factor) and one bte_lu_solve per unit vector.
+        A singular matrix raises numpy.linalg.LinAlgError, as the reference's inv does."""
+        torch = _torch()
+        on_host = not torch.is_tensor(Jmat)
+        A = self._dev(Jmat).clone()
+        if A.dim() != 3 or A.shape[1] != A.shape[2]:
+            raise ValueError("Jmat must be (P, m, m)")
+        P, m = int(A.shape[0]), int(A.shape[1])
+        lib = _lib.load()
+        stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        piv = torch.empty((P, m), dtype=torch.int32, device="cuda")
+        info = torch.empty(P, dtype=torch.int32, device="cuda")
+        _lib.check(lib.bte_lu_factor(0, P, m, _ptr(A), m, m * m, _ptr(piv), _ptr(info), stream), "bte_lu_factor")
+        if bool((info != 0).any()):
+            raise np.linalg.LinAlgError("Singular matrix")
+        out = torch.empty((P, m, m), dtype=torch.float64, device="cuda")
+        b = torch.empty((P, m), dtype=torch.float64, device="cuda")
+        for c in range(m):
+            b.zero_()
+            b[:, c] = 1.0
+            _lib.check(lib.bte_lu_solve(0, P, m, _ptr(A), m, m * m, _ptr(piv), _ptr(b), stream), "bte_lu_solve")
+            out[:, :, c] = b
+        return out.cpu().numpy() if on_host else out
 
     # ------------------------------------------------------------------ helpers
     def _dev(self, v, shape=None):

@@ -1,0 +1,38 @@
+"""Host-side methods of the drop-in class bte_0d3v_batched that need no GPU: the reference's
+flop model (against values produced by the reference's own class, tests/golden/flops_reference.json)
+and the scale of normalized_distribution (against the reference's converged c1 EDF)."""
+import json
+import os
+import types
+
+import numpy as np
+import pytest
+
+from boltzmann_gb300.bte_0d3v_batched import bte_0d3v_batched, normalization_scale
+from boltzmann_gb300.workloads import EV_MAX, TE_NORM
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.mark.parametrize("ee", [0, 1])
+def test_flop_model_matches_the_reference(synthetic_xs, ee):
+    ref = json.load(open(os.path.join(HERE, "golden", "flops_reference.json")))["ee%d" % ee]
+    args = types.SimpleNamespace(threads=1, sp_order=3, spline_qpts=5, ee_collisions=ee, verbose=0, use_gpu=1,
+                                 Efreq=0.0, dt=1e-3, cycles=1, solver_type="steady-state", l_max=1, Nr=63, n_pts=1)
+    s = bte_0d3v_batched(args, np.array([EV_MAX]), np.array([TE_NORM]), np.array([63]), [[[0, 0], [1, 0]]], 1,
+                         [synthetic_xs])
+    res, jac = s.rhs_and_jac_flops()
+    for n, p, r, j in ref:
+        assert (res(n, p), jac(n, p)) == (r, j), (n, p)
+
+
+def test_normalization_scale_matches_the_reference():
+    """The reference's converged c1 EDF is normalized: scaling it by 3.7 and normalizing again
+    returns it, and its own scale is one."""
+    g = dict(np.load(os.path.join(HERE, "golden", "c1_reference.npz")))
+    from boltzmann_gb300.bte_1d3v_fvm import thermal_velocity
+    vth = thermal_velocity(TE_NORM)
+    ff = g["ff"]
+    np.testing.assert_allclose(normalization_scale(g["mass_op"], ff, vth), 1.0, rtol=1e-12)
+    f2 = 3.7 * ff
+    np.testing.assert_allclose(f2 / normalization_scale(g["mass_op"], f2, vth), ff, rtol=1e-12, atol=0)

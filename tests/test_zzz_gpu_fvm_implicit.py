@@ -1,8 +1,8 @@
 """The finite-volume 1D3V fully implicit step on the GPU (boltzmann_gb300.bte_1d3v_fvm, the
 library's bte_fvm_* entry points) against the reference's own operator, preconditioner and
 step (tests/golden/fvm_implicit_reference.npz), with the product's own host set-up built from
-the same parameter table. The file is named so that pytest collects it after the solver's
-parity tests."""
+the same parameter table. The file is named so that pytest collects it last, after the
+parity tests of the batched solver."""
 import os
 
 import numpy as np
@@ -79,3 +79,24 @@ def test_semi_lagrangian_step_matches_the_reference(synthetic_xs):
     assert _rel(v_sl, g["v_sl"]) <= 1e-13
     y = s.step(g["E"], g["v0"], None, 0.0, dt).cpu().numpy()
     assert _rel(y, g["step"]) <= 1e-12
+
+
+# ---- drop-in utilities of bte_0d3v_batched added with this file's path
+
+
+def test_normalized_distribution_and_batched_inv(synthetic_xs):
+    """normalized_distribution against the reference's converged (normalized) c1 EDF, and
+    batched_inv against NumPy's inverse; a singular matrix raises as numpy.linalg.inv does."""
+    from helpers import gpu_solver
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "c1_reference.npz")))
+    s, _ = gpu_solver(synthetic_xs, 64, 1, False, 1)
+    ff = g["ff"]
+    out = s.normalized_distribution(0, 3.7 * ff)
+    assert _rel(out, ff) <= 1e-12
+    rng = np.random.default_rng(5)
+    J = np.eye(40)[None] * 4.0 + rng.standard_normal((6, 40, 40))
+    inv = s.batched_inv(0, J)
+    assert _rel(inv, np.linalg.inv(J)) <= 1e-10
+    J[2] = 0.0
+    with pytest.raises(np.linalg.LinAlgError):
+        s.batched_inv(0, J)
