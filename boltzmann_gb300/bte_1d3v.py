@@ -24,6 +24,7 @@ same solution to the solver tolerance. Only the BE Chebyshev x-space and the spe
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 import types
 
@@ -104,6 +105,18 @@ def load_params(par, fvm=False):
     return p
 
 
+def spectral_qoi_rows(mass, temp, rates, vth, nsh):
+    """The spectral grid's QoI rows (bte_1d3v_solver.py:588-598) over the n = Nr * nsh
+    coefficients: mass (utils.mass_op), temperature in eV (utils.temp_op vth^2 0.5 me (2/3/kB) /
+    (e/kB): `temp` is the grid's TEMP_VEC export, without the vth^2), and per process the rate
+    functional (n_proc x Nr) on the l = 0 coefficients. Returns (2 + n_proc) x n."""
+    mass, temp, rates = (np.asarray(a, dtype=np.float64) for a in (mass, temp, rates))
+    Q = np.zeros((2 + rates.shape[0], mass.shape[0]))
+    Q[0], Q[1] = mass, temp * vth ** 2
+    Q[2:, 0::nsh] = rates
+    return Q
+
+
 class bte_1d3v:
     """Spectral 1D3V solver on one GPU. `par` is the reference's parameter file (TOML with a
     [bte] table) or the same table as a dict; `collisions` in it names an LXCat file."""
@@ -169,6 +182,7 @@ class bte_1d3v:
             raise RuntimeError("bte1d_create failed (%d): %s" % (rc, lib.bte1d_last_error().decode()))
         self._h = h
         self.mass_op = s.export_operator(0, "MASS_VEC")
+        self.op_qoi = None   # the QoI rows, built on the first compute_qoi
         self.gmres_info = None
 
     def __del__(self):
@@ -267,6 +281,25 @@ class bte_1d3v:
         h = f0 / (self.mass_op @ f0)
         vo = (self.torch.as_tensor(self.op_psh2o, device="cuda") @ h.reshape(self.dof_vr, self.num_sh).t()).t()
         return vo.reshape(-1, 1) * self.torch.as_tensor(ne, device="cuda")[None, :]
+
+    def compute_qoi(self, v, time, dt):
+        """compute_qoi (:1179-1215) per x point from the ordinates v: "rates" (Nx, n_proc), "ne",
+        "Te"; "mu" and "D" are 0 as in the reference. The harmonics of v meet the QoI rows in
+        one FP64 GEMM (bte_dgemm_nn)."""
+        from .bte_1d3v_fvm import qoi_from_moments
+        if self.op_qoi is None:
+            s = self.grid
+            rows = spectral_qoi_rows(self.mass_op.cpu().numpy(), s.export_operator(0, "TEMP_VEC").cpu().numpy(),
+                                     s.export_operator(0, "RATES").cpu().numpy(), self.vth, self.num_sh)
+            self.op_qoi = self.torch.as_tensor(rows, dtype=self.torch.float64, device="cuda")
+        U = self.ords_to_sph(v).contiguous()
+        Q = self.op_qoi
+        Y = self.torch.empty((Q.shape[0], self.dof_x), dtype=self.torch.float64, device="cuda")
+        rc = _lib.load().bte_dgemm_nn(Q.shape[0], self.dof_x, self.dof_v, _lib.ptr(Q), self.dof_v, _lib.ptr(U),
+                                      self.dof_x, _lib.ptr(Y), self.dof_x, self._s())
+        if rc != 0:
+            raise RuntimeError("QoI functionals failed (%d): %s" % (rc, _lib.load().bte_sweep_last_error().decode()))
+        return qoi_from_moments(Y, self.vth, self.params.np0, math.sqrt(4.0 * math.pi))
 
     def launches(self):
         return int(_lib.load().bte1d_launches(self._h))

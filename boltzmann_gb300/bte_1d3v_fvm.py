@@ -274,6 +274,38 @@ def fvm_collisions(processes, vr, vt_qw, vth, vmax):
 
 
 # ----------------------------------------------------------------------------------
+# quantities of interest
+# ----------------------------------------------------------------------------------
+TEMP_K_1EV = QE / KB
+
+
+def fvm_qoi_functionals(processes, vr, vr_qw, vt_qw, vth):
+    """The FVM grid's QoI functionals (bte_1d3v_solver.py:493-502), rows of a (2 + n_proc) x
+    (Nr * Nvt) matrix: mass 2 pi (v_r^2 dv_r (x) w_theta); temperature in eV
+    2 pi vth^2 (v_r^4 dv_r (x) w_theta) 0.5 me (2 / 3 / kB) / (e / kB); per process the rate
+    2 pi (2 vth^4 / c_gamma^3) (v_r^3 dv_r sigma(eps(v_r)) (x) w_theta)."""
+    vr, vr_qw, vt_qw = (np.asarray(a, dtype=np.float64) for a in (vr, vr_qw, vt_qw))
+    ev_fac = 0.5 * ME * (2.0 / 3.0 / KB) / TEMP_K_1EV
+    rows = [2.0 * np.pi * np.kron(vr ** 2 * vr_qw, vt_qw),
+            2.0 * np.pi * vth ** 2 * np.kron(vr ** 4 * vr_qw, vt_qw) * ev_fac]
+    for proc in processes:
+        sig = _sigma(proc, (vr * vth / C_GAMMA) ** 2)
+        rows.append(2.0 * np.pi * (2.0 * vth ** 4 / C_GAMMA ** 3) * np.kron(vr ** 3 * vr_qw * sig, vt_qw))
+    return np.array(rows)
+
+
+def qoi_from_moments(Y, vth, np0, mass_scale):
+    """compute_qoi (bte_1d3v_solver.py:1179-1215) from Y = Q v, Q the (2 + n_proc) QoI rows:
+    ne = m0 np0, Te = (temp . v) / m0, rates = (rate . v) / s with the normalization
+    s = m0 / mass_scale * 2 (vth / c_gamma)^3 (mass_scale 1 on the FVM grid, sqrt(4 pi) for the
+    harmonics); mobility and diffusion are 0, as the reference returns. Works on NumPy arrays
+    and on tensors; rates are (Nx, n_proc)."""
+    m0 = Y[0]
+    scale = m0 / mass_scale * (2.0 * (vth / C_GAMMA) ** 3)
+    return {"rates": (Y[2:] / scale).T, "mu": 0.0, "D": 0.0, "ne": m0 * np0, "Te": Y[1] / m0}
+
+
+# ----------------------------------------------------------------------------------
 # the op-split step on the GPU
 # ----------------------------------------------------------------------------------
 class FvmOpSplit:
@@ -507,7 +539,8 @@ def fvm_setup(par):
     bands = fvm_bands(fvm_upwind_operators(vr, vt, x, p.pvr, p.pvt, p.px, vmax), p.pvr, p.pvt, p.px)
     return types.SimpleNamespace(params=p, vth=vth, vmax=vmax, vr=vr, vr_qw=vr_qw, vt=vt, vt_qw=vt_qw, x=x,
                                  grid_info={"x": x, "vr": vr, "vr_qw": vr_qw, "vt": vt, "vt_qw": vt_qw},
-                                 collisions=coll, bands=bands)
+                                 collisions=coll, bands=bands,
+                                 qoi=fvm_qoi_functionals(procs, vr, vr_qw, vt_qw, vth))
 
 
 def fvm_initial_condition(p, vth, vr, Nvt, x):
@@ -544,6 +577,7 @@ class bte_1d3v_fvm:
         self.dof_vr, self.dof_vt, self.dof_x = len(st.vr), len(st.vt), p.Np
         self.dof_v = self.dof_vr * self.dof_vt
         self.op_col, self.bands = st.collisions, st.bands
+        self.op_qoi = torch.as_tensor(st.qoi, dtype=torch.float64, device="cuda")
         self.solver = FvmImplicit(st.vr, st.vt, st.vt_qw, p.Np, self.bands, self.op_col, device=self.device)
         self.solver.set_sl_grid(st.x, 0.0, self.vmax)
         self.c_gamma = C_GAMMA
@@ -603,6 +637,17 @@ class bte_1d3v_fvm:
             raise NotImplementedError
         v = fvm_initial_condition(self.params, self.bs_vth, self.grid_info["vr"], self.dof_vt, self.xp)
         return self.torch.as_tensor(v, dtype=self.torch.float64, device="cuda")
+
+    def compute_qoi(self, v, time, dt):
+        """compute_qoi (:1179-1215) per x point: "rates" (Nx, n_proc), "ne", "Te"; "mu" and "D"
+        are 0 as in the reference. The QoI rows multiply v in one FP64 GEMM (bte_dgemm_nn)."""
+        torch = self.torch
+        V = torch.as_tensor(v, dtype=torch.float64, device="cuda").reshape(self.dof_v, self.dof_x).contiguous()
+        Q = self.op_qoi
+        Y = torch.empty((Q.shape[0], self.dof_x), dtype=torch.float64, device="cuda")
+        _check(_lib.load().bte_dgemm_nn(Q.shape[0], self.dof_x, self.dof_v, _ptr(Q), self.dof_v, _ptr(V), self.dof_x,
+                                        _ptr(Y), self.dof_x, _stream()), "QoI functionals")
+        return qoi_from_moments(Y, self.bs_vth, self.params.np0, 1.0)
 
     def launches(self):
         return self.solver.launches()

@@ -36,3 +36,25 @@ def test_normalization_scale_matches_the_reference():
     np.testing.assert_allclose(normalization_scale(g["mass_op"], ff, vth), 1.0, rtol=1e-12)
     f2 = 3.7 * ff
     np.testing.assert_allclose(f2 / normalization_scale(g["mass_op"], f2, vth), ff, rtol=1e-12, atol=0)
+
+
+def test_spectral_1d3v_qoi_rows_and_arithmetic(synthetic_xs):
+    """bte_1d3v.compute_qoi's rows and arithmetic on the host, with the oracle's operators of the
+    1D3V golden grid (16 B-splines, l_max 1, plain knots) and its ordinate-to-harmonic
+    projection, against the reference's compute_qoi (tests/golden/qoi_1d3v_reference.npz)."""
+    from boltzmann_gb300.bte_1d3v import spectral_qoi_rows
+    from boltzmann_gb300.bte_1d3v_fvm import qoi_from_moments
+    from oracle import bte_oracle as O
+    g = dict(np.load(os.path.join(HERE, "golden", "bte1d_reference.npz")))
+    q = dict(np.load(os.path.join(HERE, "golden", "qoi_1d3v_reference.npz")))
+    ops = O.Operators(O.processes_from_lxcat(synthetic_xs), 80.0, 4.0, 16, 1, ee=False, snap=False)
+    np.testing.assert_allclose(ops.op_mass, g["op_mass"], rtol=0, atol=1e-14 * np.abs(g["op_mass"]).max())
+    Q = spectral_qoi_rows(ops.op_mass, ops.op_temp, ops.op_rate, ops.vth, 2)
+    Po = g["op_po2sh"]                                   # (nsh, Nvt)
+    for k in ("v0", "v1", "v3"):
+        V = g[k].reshape(16, Po.shape[1], -1)            # (Nr, Nvt, Nx)
+        U = np.einsum("lj,rjx->rlx", Po, V).reshape(16 * 2, -1)
+        out = qoi_from_moments(Q @ U, ops.vth, float(g["np0"]), np.sqrt(4 * np.pi))
+        for name in ("rates", "ne", "Te"):
+            ref = q["spec_%s_%s" % (k, name)]
+            assert np.max(np.abs(out[name] - ref)) <= 1e-12 * np.max(np.abs(ref)), (k, name)

@@ -118,3 +118,18 @@ def test_initial_condition_matches_the_reference(synthetic_xs):
     st = P.fvm_setup(dict(FVM_IMPLICIT_PARAMS, collisions=synthetic_xs))
     v = P.fvm_initial_condition(st.params, st.vth, st.vr, len(st.vt), st.x)
     assert np.max(np.abs(v - gi["v0"])) <= 1e-14 * np.max(np.abs(gi["v0"]))
+
+
+def test_qoi_functionals_and_compute_qoi_match_the_reference(synthetic_xs):
+    """The FVM QoI rows and compute_qoi's arithmetic (on the host, from Q v) against the
+    reference's op_mass/op_temp/op_rate and compute_qoi (tests/golden/qoi_1d3v_reference.npz)."""
+    from helpers import FVM_IMPLICIT_PARAMS
+    q = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "qoi_1d3v_reference.npz")))
+    st = P.fvm_setup(dict(FVM_IMPLICIT_PARAMS, collisions=synthetic_xs))
+    for i, ref in enumerate([q["fvm_op_mass"], q["fvm_op_temp"]] + list(q["fvm_op_rate"])):
+        assert np.max(np.abs(st.qoi[i] - ref)) <= 1e-14 * np.max(np.abs(ref)), i
+    for k in ("v0", "vp"):
+        out = P.qoi_from_moments(st.qoi @ q["fvm_%s" % k], st.vth, st.params.np0, 1.0)
+        for name in ("rates", "ne", "Te"):
+            ref = q["fvm_%s_%s" % (k, name)]
+            assert np.max(np.abs(out[name] - ref)) <= 1e-13 * np.max(np.abs(ref)), (k, name)

@@ -100,3 +100,23 @@ def test_normalized_distribution_and_batched_inv(synthetic_xs):
     J[2] = 0.0
     with pytest.raises(np.linalg.LinAlgError):
         s.batched_inv(0, J)
+
+
+def test_compute_qoi_both_v_spaces(synthetic_xs):
+    """compute_qoi of the FVM and the spectral 1D3V solvers against the reference's
+    (tests/golden/qoi_1d3v_reference.npz)."""
+    import ast
+    from boltzmann_gb300.bte_1d3v import bte_1d3v
+    from boltzmann_gb300.bte_1d3v_fvm import bte_1d3v_fvm
+    q = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "qoi_1d3v_reference.npz")))
+    f = bte_1d3v_fvm(dict(PARAMS, collisions=synthetic_xs))
+    for k in ("v0", "vp"):
+        out = f.compute_qoi(q["fvm_%s" % k], 0.0, 1e-3)
+        for name in ("rates", "ne", "Te"):
+            assert _rel(out[name].cpu().numpy(), q["fvm_%s_%s" % (k, name)]) <= 1e-12, (k, name)
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "bte1d_reference.npz")))
+    s = bte_1d3v(dict(ast.literal_eval(str(g["params"])), collisions=synthetic_xs))
+    for k in ("v0", "v1", "v3"):
+        out = s.compute_qoi(np.real(g[k]), 0.0, 1e-3)
+        for name in ("rates", "ne", "Te"):
+            assert _rel(out[name].cpu().numpy(), q["spec_%s_%s" % (k, name)]) <= 1e-11, (k, name)
