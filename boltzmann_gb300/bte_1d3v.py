@@ -301,5 +301,11 @@ class bte_1d3v:
             raise RuntimeError("QoI functionals failed (%d): %s" % (rc, _lib.load().bte_sweep_last_error().decode()))
         return qoi_from_moments(Y, self.vth, self.params.np0, math.sqrt(4.0 * math.pi))
 
+    def compute_radial_components(self, ev, v):
+        """compute_radial_components (:1139-1160): f_l(eps) of the ordinates v at the energies ev
+        (eV), (Nx, num_sh, len(ev)) NumPy array, from the grid's B-spline evaluation
+        (bte_radial_components) on the harmonics of v."""
+        return self.grid.compute_radial_components(0, ev, self.ords_to_sph(v))
+
     def launches(self):
         return int(_lib.load().bte1d_launches(self._h))

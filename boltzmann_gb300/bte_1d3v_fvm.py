@@ -40,7 +40,7 @@ import math
 import numpy as np
 
 from . import _lib
-from .bte_1d3v import KB, ME, QE, chebyshev, load_params, ordinates
+from .bte_1d3v import KB, ME, QE, chebyshev, load_params, ordinates, sph_ords_projections
 from .native_kernels import _check, _ptr, _stream
 
 C_GAMMA = math.sqrt(2.0 * QE / ME)   # v = C_GAMMA sqrt(eps [eV])
@@ -303,6 +303,23 @@ def qoi_from_moments(Y, vth, np0, mass_scale):
     m0 = Y[0]
     scale = m0 / mass_scale * (2.0 * (vth / C_GAMMA) ** 3)
     return {"rates": (Y[2:] / scale).T, "mu": 0.0, "D": 0.0, "ne": m0 * np0, "Te": Y[1] / m0}
+
+
+def fvm_radial_components(vsh, vr, nsh, ev, vth):
+    """compute_radial_components on the FVM grid (bte_1d3v_solver.py:1162-1177): the harmonics
+    vsh (Nr * nsh, Nx) interpolated linearly in v_r at v(eps) = sqrt(eps) c_gamma / vth;
+    returns (Nx, nsh, len(ev)). An energy whose speed lies outside the cells raises ValueError,
+    as the reference's interpolation (bounds_error=True) does."""
+    vr = np.asarray(vr, dtype=np.float64)
+    Nr = len(vr)
+    V = np.asarray(vsh, dtype=np.float64).reshape(Nr, nsh, -1)
+    q = np.sqrt(np.asarray(ev, dtype=np.float64)) * C_GAMMA / vth
+    if np.any(q < vr[0]) or np.any(q > vr[-1]):
+        raise ValueError("an energy's speed lies outside the cells [%.6g, %.6g]" % (vr[0], vr[-1]))
+    i = np.clip(np.searchsorted(vr, q, side="right") - 1, 0, Nr - 2)
+    t = (q - vr[i]) / (vr[i + 1] - vr[i])
+    out = (1.0 - t)[None, None, :] * V[i] .transpose(2, 1, 0) + t[None, None, :] * V[i + 1].transpose(2, 1, 0)
+    return out
 
 
 # ----------------------------------------------------------------------------------
@@ -578,6 +595,10 @@ class bte_1d3v_fvm:
         self.dof_v = self.dof_vr * self.dof_vt
         self.op_col, self.bands = st.collisions, st.bands
         self.op_qoi = torch.as_tensor(st.qoi, dtype=torch.float64, device="cuda")
+        self.num_sh = p.l_max + 1
+        psh2o, po2sh = sph_ords_projections(st.vt, st.vt_qw, p.l_max)
+        self.op_psh2o = torch.as_tensor(psh2o, dtype=torch.float64, device="cuda").contiguous()
+        self.op_po2sh = torch.as_tensor(po2sh, dtype=torch.float64, device="cuda").contiguous()
         self.solver = FvmImplicit(st.vr, st.vt, st.vt_qw, p.Np, self.bands, self.op_col, device=self.device)
         self.solver.set_sl_grid(st.x, 0.0, self.vmax)
         self.c_gamma = C_GAMMA
@@ -637,6 +658,37 @@ class bte_1d3v_fvm:
             raise NotImplementedError
         v = fvm_initial_condition(self.params, self.bs_vth, self.grid_info["vr"], self.dof_vt, self.xp)
         return self.torch.as_tensor(v, dtype=self.torch.float64, device="cuda")
+
+    def _project(self, P, x, n_in, n_out):
+        """(Nr, n_in, Nx) -> (Nr, n_out, Nx) by P (n_out x n_in) along the middle axis: two layout
+        swaps (bte_permute3) around one FP64 GEMM (bte_dgemm_nn)."""
+        torch = self.torch
+        lib, s = _lib.load(), _stream()
+        Nr, Nx = self.dof_vr, self.dof_x
+        X = torch.as_tensor(x, dtype=torch.float64, device="cuda").reshape(-1).contiguous()
+        if X.numel() != Nr * n_in * Nx:
+            raise ValueError("expected (%d, %d) values" % (Nr * n_in, Nx))
+        A = torch.empty(Nr * n_in * Nx, dtype=torch.float64, device="cuda")
+        B = torch.empty(Nr * n_out * Nx, dtype=torch.float64, device="cuda")
+        _check(lib.bte_permute3(Nr, n_in, Nx, 1, 0, 2, _ptr(X), _ptr(A), s), "layout")        # (n_in, Nr, Nx)
+        _check(lib.bte_dgemm_nn(n_out, Nr * Nx, n_in, _ptr(P), n_in, _ptr(A), Nr * Nx, _ptr(B), Nr * Nx, s),
+               "projection")
+        out = torch.empty(Nr * n_out * Nx, dtype=torch.float64, device="cuda")
+        _check(lib.bte_permute3(n_out, Nr, Nx, 1, 0, 2, _ptr(B), _ptr(out), s), "layout")     # (Nr, n_out, Nx)
+        return out.reshape(Nr * n_out, Nx)
+
+    def ords_to_sph(self, x):
+        """ords_to_sph (:678-685): (Nr * Nvt, Nx) ordinates -> (Nr * num_sh, Nx) harmonics."""
+        return self._project(self.op_po2sh, x, self.dof_vt, self.num_sh)
+
+    def sph_to_ords(self, x):
+        """sph_to_ords (:687-694): (Nr * num_sh, Nx) harmonics -> (Nr * Nvt, Nx) ordinates."""
+        return self._project(self.op_psh2o, x, self.num_sh, self.dof_vt)
+
+    def compute_radial_components(self, ev, v):
+        """compute_radial_components (:1162-1177): (Nx, num_sh, len(ev)) NumPy array."""
+        vsh = self.ords_to_sph(v).cpu().numpy()
+        return fvm_radial_components(vsh, self.grid_info["vr"], self.num_sh, ev, self.bs_vth)
 
     def compute_qoi(self, v, time, dt):
         """compute_qoi (:1179-1215) per x point: "rates" (Nx, n_proc), "ne", "Te"; "mu" and "D"

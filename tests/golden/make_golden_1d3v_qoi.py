@@ -6,7 +6,10 @@ reference's own `bte_1d3v` on CPU:
   step states v1 and v3 recorded in `bte1d_reference.npz`;
 * finite-volume (the table of `make_golden_fvm.py`): the QoIs of the initial condition and of
   a seeded perturbation of it (so that the rates see a non-Maxwellian distribution), with the
-  reference's QoI functionals op_mass, op_temp and op_rate (:493-502).
+  reference's QoI functionals op_mass, op_temp and op_rate (:493-502);
+* for both, the radial components f_l(eps) of the last state at 50 energies
+  (`compute_radial_components`, :1139-1177) and, for the FVM one, its harmonics
+  (`ords_to_sph`, :678-685).
 
 Runs only where the reference checkout is available (imported through
 `oracle/reference_import.py`); the GPU host never runs this script.
@@ -51,6 +54,8 @@ def main():
         for k in ("v0", "v1", "v3"):
             r, ne, te = _qoi(b, spec[k])
             out.update({"spec_%s_rates" % k: r, "spec_%s_ne" % k: ne, "spec_%s_Te" % k: te})
+        ev = np.linspace(0.1, 70.0, 50)
+        out.update(ev=ev, spec_v3_radial=np.asarray(b.compute_radial_components(ev, np.copy(spec["v3"]))))
         par = os.path.join(tmp, "fvm.toml")
         G.write_toml(par, GF.PARAMS, xs, os.path.join(tmp, "run_f"))
         b = S.bte_1d3v(types.SimpleNamespace(par_file=par))
@@ -60,7 +65,8 @@ def main():
             r, ne, te = _qoi(b, v)
             out.update({"fvm_%s" % k: v, "fvm_%s_rates" % k: r, "fvm_%s_ne" % k: ne, "fvm_%s_Te" % k: te})
         out.update(fvm_op_mass=np.asarray(b.op_mass), fvm_op_temp=np.asarray(b.op_temp),
-                   fvm_op_rate=np.asarray(b.op_rate))
+                   fvm_op_rate=np.asarray(b.op_rate), fvm_vp_sph=np.asarray(b.ords_to_sph(np.copy(vp))),
+                   fvm_vp_radial=np.asarray(b.compute_radial_components(ev, np.copy(vp))))
         np.savez_compressed(os.path.join(HERE, "qoi_1d3v_reference.npz"), **out)
         print("wrote qoi_1d3v_reference.npz:", sorted(out))
     finally:

@@ -133,3 +133,20 @@ def test_qoi_functionals_and_compute_qoi_match_the_reference(synthetic_xs):
         for name in ("rates", "ne", "Te"):
             ref = q["fvm_%s_%s" % (k, name)]
             assert np.max(np.abs(out[name] - ref)) <= 1e-13 * np.max(np.abs(ref)), (k, name)
+
+
+def test_radial_components_match_the_reference(synthetic_xs):
+    """ords_to_sph's projection and compute_radial_components's interpolation on the FVM grid
+    against the reference's (tests/golden/qoi_1d3v_reference.npz); speeds outside the cells
+    raise as the reference's interpolation does."""
+    from helpers import FVM_IMPLICIT_PARAMS
+    from boltzmann_gb300.bte_1d3v import sph_ords_projections
+    q = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "qoi_1d3v_reference.npz")))
+    st = P.fvm_setup(dict(FVM_IMPLICIT_PARAMS, collisions=synthetic_xs))
+    _, po2sh = sph_ords_projections(st.vt, st.vt_qw, st.params.l_max)
+    U = np.einsum("li,rix->rlx", po2sh, q["fvm_vp"].reshape(len(st.vr), len(st.vt), -1)).reshape(-1, len(st.x))
+    assert np.max(np.abs(U - q["fvm_vp_sph"])) <= 1e-14 * np.max(np.abs(q["fvm_vp_sph"]))
+    R = P.fvm_radial_components(U, st.vr, 2, q["ev"], st.vth)
+    assert np.max(np.abs(R - q["fvm_vp_radial"])) <= 1e-14 * np.max(np.abs(q["fvm_vp_radial"]))
+    with pytest.raises(ValueError):
+        P.fvm_radial_components(U, st.vr, 2, np.array([79.9]), st.vth)

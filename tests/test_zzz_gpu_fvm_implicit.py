@@ -120,3 +120,20 @@ def test_compute_qoi_both_v_spaces(synthetic_xs):
         out = s.compute_qoi(np.real(g[k]), 0.0, 1e-3)
         for name in ("rates", "ne", "Te"):
             assert _rel(out[name].cpu().numpy(), q["spec_%s_%s" % (k, name)]) <= 1e-11, (k, name)
+
+
+def test_projections_and_radial_components(synthetic_xs):
+    """ords_to_sph / sph_to_ords and compute_radial_components of both 1D3V solvers against the
+    reference's (tests/golden/qoi_1d3v_reference.npz)."""
+    import ast
+    from boltzmann_gb300.bte_1d3v import bte_1d3v
+    from boltzmann_gb300.bte_1d3v_fvm import bte_1d3v_fvm
+    q = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "qoi_1d3v_reference.npz")))
+    f = bte_1d3v_fvm(dict(PARAMS, collisions=synthetic_xs))
+    U = f.ords_to_sph(q["fvm_vp"])
+    assert _rel(U.cpu().numpy(), q["fvm_vp_sph"]) <= 1e-13
+    assert f.sph_to_ords(U).shape == (f.dof_v, f.dof_x)
+    assert _rel(f.compute_radial_components(q["ev"], q["fvm_vp"]), q["fvm_vp_radial"]) <= 1e-13
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "bte1d_reference.npz")))
+    s = bte_1d3v(dict(ast.literal_eval(str(g["params"])), collisions=synthetic_xs))
+    assert _rel(s.compute_radial_components(q["ev"], np.real(g["v3"])), q["spec_v3_radial"]) <= 1e-11
