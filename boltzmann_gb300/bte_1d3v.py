@@ -105,6 +105,23 @@ def load_params(par, fvm=False):
     return p
 
 
+def write_checkpoint(fprefix, v, time, dt, ne, Te):
+    """store_checkpoint (bte_1d3v_solver.py:2065-2090) in NumPy's .npz format (the reference
+    writes HDF5, whose library this package does not use): `fprefix`.npz with the reference's
+    dataset names "time[T]", "dt[T]", "edf", "ne[m^-3]" and "Te[eV]". Raises OSError on a
+    failed write (the reference prints and carries on)."""
+    host = lambda a: a.cpu().numpy() if hasattr(a, "cpu") else np.asarray(a)
+    with open("%s.npz" % fprefix, "wb") as fh:
+        np.savez(fh, **{"time[T]": np.array([float(time)]), "dt[T]": np.array([float(dt)]), "edf": host(v),
+                        "ne[m^-3]": host(ne), "Te[eV]": host(Te)})
+
+
+def read_checkpoint(fprefix):
+    """restore_checkpoint (bte_1d3v_solver.py:2092-2103): (time, dt, edf) from `fprefix`.npz."""
+    with np.load("%s.npz" % fprefix) as F:
+        return float(F["time[T]"][0]), float(F["dt[T]"][0]), np.array(F["edf"])
+
+
 def spectral_qoi_rows(mass, temp, rates, vth, nsh):
     """The spectral grid's QoI rows (bte_1d3v_solver.py:588-598) over the n = Nr * nsh
     coefficients: mass (utils.mass_op), temperature in eV (utils.temp_op vth^2 0.5 me (2/3/kB) /
@@ -300,6 +317,16 @@ class bte_1d3v:
         if rc != 0:
             raise RuntimeError("QoI functionals failed (%d): %s" % (rc, _lib.load().bte_sweep_last_error().decode()))
         return qoi_from_moments(Y, self.vth, self.params.np0, math.sqrt(4.0 * math.pi))
+
+    def store_checkpoint(self, v, time, dt, fprefix):
+        """store_checkpoint (:2065-2090): v with its ne and Te, to `fprefix`.npz."""
+        q = self.compute_qoi(v, time, dt)
+        write_checkpoint(fprefix, v, time, dt, q["ne"], q["Te"])
+
+    def restore_checkpoint(self, fprefix):
+        """restore_checkpoint (:2092-2103): (time, dt, v) with v on the device."""
+        t, dt, v = read_checkpoint(fprefix)
+        return t, dt, self.torch.as_tensor(v, dtype=self.torch.float64, device="cuda")
 
     def compute_radial_components(self, ev, v):
         """compute_radial_components (:1139-1160): f_l(eps) of the ordinates v at the energies ev

@@ -40,7 +40,8 @@ import math
 import numpy as np
 
 from . import _lib
-from .bte_1d3v import KB, ME, QE, chebyshev, load_params, ordinates, sph_ords_projections
+from .bte_1d3v import (KB, ME, QE, chebyshev, load_params, ordinates, read_checkpoint, sph_ords_projections,
+                       write_checkpoint)
 from .native_kernels import _check, _ptr, _stream
 
 C_GAMMA = math.sqrt(2.0 * QE / ME)   # v = C_GAMMA sqrt(eps [eV])
@@ -318,8 +319,9 @@ def fvm_radial_components(vsh, vr, nsh, ev, vth):
         raise ValueError("an energy's speed lies outside the cells [%.6g, %.6g]" % (vr[0], vr[-1]))
     i = np.clip(np.searchsorted(vr, q, side="right") - 1, 0, Nr - 2)
     t = (q - vr[i]) / (vr[i + 1] - vr[i])
-    out = (1.0 - t)[None, None, :] * V[i] .transpose(2, 1, 0) + t[None, None, :] * V[i + 1].transpose(2, 1, 0)
-    return out
+    lo = V[i].transpose(2, 1, 0)       # (Nx, nsh, n_ev)
+    hi = V[i + 1].transpose(2, 1, 0)
+    return (1.0 - t) * lo + t * hi
 
 
 # ----------------------------------------------------------------------------------
@@ -684,6 +686,16 @@ class bte_1d3v_fvm:
     def sph_to_ords(self, x):
         """sph_to_ords (:687-694): (Nr * num_sh, Nx) harmonics -> (Nr * Nvt, Nx) ordinates."""
         return self._project(self.op_psh2o, x, self.num_sh, self.dof_vt)
+
+    def store_checkpoint(self, v, time, dt, fprefix):
+        """store_checkpoint (:2065-2090): v with its ne and Te, to `fprefix`.npz."""
+        q = self.compute_qoi(v, time, dt)
+        write_checkpoint(fprefix, v, time, dt, q["ne"], q["Te"])
+
+    def restore_checkpoint(self, fprefix):
+        """restore_checkpoint (:2092-2103): (time, dt, v) with v on the device."""
+        t, dt, v = read_checkpoint(fprefix)
+        return t, dt, self.torch.as_tensor(v, dtype=self.torch.float64, device="cuda")
 
     def compute_radial_components(self, ev, v):
         """compute_radial_components (:1162-1177): (Nx, num_sh, len(ev)) NumPy array."""

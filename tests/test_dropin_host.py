@@ -58,3 +58,17 @@ def test_spectral_1d3v_qoi_rows_and_arithmetic(synthetic_xs):
         for name in ("rates", "ne", "Te"):
             ref = q["spec_%s_%s" % (k, name)]
             assert np.max(np.abs(out[name] - ref)) <= 1e-12 * np.max(np.abs(ref)), (k, name)
+
+
+def test_checkpoint_round_trip(tmp_path):
+    """write_checkpoint / read_checkpoint keep the reference's dataset names and values."""
+    from boltzmann_gb300.bte_1d3v import read_checkpoint, write_checkpoint
+    rng = np.random.default_rng(2)
+    v, ne, Te = rng.random((20, 6)), rng.random(6), rng.random(6)
+    pre = str(tmp_path / "cp_00001")
+    write_checkpoint(pre, v, 0.25, 1e-3, ne, Te)
+    t, dt, v2 = read_checkpoint(pre)
+    assert (t, dt) == (0.25, 1e-3) and np.array_equal(v2, v)
+    with np.load(pre + ".npz") as F:
+        assert sorted(F.files) == sorted(["time[T]", "dt[T]", "edf", "ne[m^-3]", "Te[eV]"])
+        assert np.array_equal(F["ne[m^-3]"], ne) and np.array_equal(F["Te[eV]"], Te)

@@ -137,3 +137,15 @@ def test_projections_and_radial_components(synthetic_xs):
     g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "bte1d_reference.npz")))
     s = bte_1d3v(dict(ast.literal_eval(str(g["params"])), collisions=synthetic_xs))
     assert _rel(s.compute_radial_components(q["ev"], np.real(g["v3"])), q["spec_v3_radial"]) <= 1e-11
+
+
+def test_checkpoint_through_the_solver(synthetic_xs, tmp_path):
+    from boltzmann_gb300.bte_1d3v_fvm import bte_1d3v_fvm
+    q = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "qoi_1d3v_reference.npz")))
+    f = bte_1d3v_fvm(dict(PARAMS, collisions=synthetic_xs))
+    pre = str(tmp_path / "fvm_cp")
+    f.store_checkpoint(q["fvm_vp"], 0.5, 1e-3, pre)
+    t, dt, v = f.restore_checkpoint(pre)
+    assert (t, dt) == (0.5, 1e-3) and np.array_equal(v.cpu().numpy(), q["fvm_vp"])
+    with np.load(pre + ".npz") as F:
+        assert _rel(F["ne[m^-3]"], q["fvm_vp_ne"]) <= 1e-12
