@@ -47,3 +47,28 @@ def test_argument_errors_without_gpu(lib):
     rc = l.bte_grid_create(None, None, None)
     assert rc == -1
     assert b"null" in l.bte_last_error()
+
+
+def test_fvm_entry_points_refuse_bad_arguments(lib):
+    """The FVM entry points check their arguments before any device work: null pointers,
+    sizes out of range and a missing handle return BTE_ERR_ARG (no GPU is touched)."""
+    import ctypes as C
+    from boltzmann_gb300 import _lib
+    l = _lib.load()
+    dp = C.POINTER(C.c_double)
+    h = C.c_void_p()
+    null = dp()
+    one = (C.c_double * 64)(*([1.0] * 64))
+    ptrs = [C.cast(one, dp)] * 11
+    assert l.bte_fvm_create(0, 4, 4, 4, 2, 2, 2, *([null] * 11), C.byref(h)) < 0
+    assert b"null" in l.bte_fvm_last_error()
+    assert l.bte_fvm_create(0, 4, 3, 4, 2, 2, 2, *ptrs, C.byref(h)) < 0        # odd ordinate count
+    assert l.bte_fvm_create(0, 4, 4, 4, 5, 2, 2, *ptrs, C.byref(h)) < 0        # more diagonals than cells
+    assert b"range" in l.bte_fvm_last_error()
+    coef = _lib.FvmCoef(1e-3, 1e-3, 1e-7, 1.0, 1.0, 1.0)
+    info = (C.c_double * 4)()
+    assert l.bte_fvm_step(None, C.byref(coef), 1.0, 0, None, None, 1e-10, 1e-14, 30, 100, info, None) < 0
+    assert l.bte_fvm_mvec(None, C.byref(coef), None, None, None, None) < 0
+    assert l.bte_fvm_sl_step(None, C.byref(coef), None, None, None, None) < 0
+    assert l.bte_fvm_set_collision_inverse(None, null, null) < 0
+    assert l.bte_fvm_destroy(None) == 0
