@@ -170,3 +170,55 @@ def test_gmres_on_the_reference_test_system(harness, pc_left):
     assert np.linalg.norm(b - A @ x) <= 1e-12 * np.linalg.norm(b) * 1.0001
     xs = np.linalg.solve(A, b)
     assert np.max(np.abs(x - xs)) <= 1e-9 * np.max(np.abs(xs))
+
+
+@pytest.mark.parametrize("Nr_sp,Nvt,Nx,p,seed", [(6, 4, 7, 1, 1), (9, 6, 9, 3, 2), (7, 10, 5, 2, 3), (8, 8, 11, 3, 4)])
+def test_core_against_the_oracle_on_other_grids(harness, synthetic_xs, Nr_sp, Nvt, Nx, p, seed):
+    """The operator, the preconditioner and the semi-Lagrangian advection of the shared core
+    against the oracle's restatements on grids and stencil orders the fixtures do not cover
+    (orders 1 and 3, odd and even sizes), with a field of both signs."""
+    from oracle import bte1d_fvm_oracle as F
+    from boltzmann_gb300.bte_1d3v import ordinates
+    from boltzmann_gb300.lxcat import read_cross_section_data
+    rng = np.random.default_rng(seed)
+    vr, vr_qw, vmax = P.radial_cells(80.0, 4.0, Nr_sp, 3, 3)
+    vt, vt_qw = ordinates(Nvt)
+    x = P.x_points(Nx)
+    vth = P.thermal_velocity(4.0)
+    procs = list(read_cross_section_data(synthetic_xs).values())
+    coll = P.FvmCollisions(*P.fvm_collisions(procs, vr, vt_qw, vth, vmax), 2.0 * np.pi * vt_qw)
+    bands = P.fvm_bands(P.fvm_upwind_operators(vr, vt, x, p, p, p, vmax), p, p, p)
+    Nr = len(vr)
+    dt, tau, L, kappa = 2e-3, 7.4e-8, 1.27e-2, 3.2e22
+    cA = 1.602176634e-19 / 9.1093837139e-31 / vth
+    ax = vth * tau / L
+    E = 4e4 * rng.standard_normal(Nx)
+    u = rng.standard_normal((Nr * Nvt, Nx))
+    g = dict(Nr=Nr, Nvt=Nvt, Nx=Nx, pvr=p, pvt=p, px=p, tau=tau, qe=1.602176634e-19, me=9.1093837139e-31,
+             vth=vth, L=L, vr=vr, vt=vt, n0=kappa, np0=1.0, op_col_en=coll.dense(),
+             PmatC=coll.inverse_dense(dt * tau * kappa), **bands)
+    case = dict(g=dict(g, Nr=np.array(Nr), Nvt=np.array(Nvt), Nx=np.array(Nx)), p=[p, p, p], bands=bands, coll=coll)
+    a = _Args(case)
+    # operator
+    Ep, En = F.adv_v_fvm(vr, vt, p, p, vmax)
+    xs = F.x_shift_bands(vr, vt, x, p, ax, dt)
+    ref = F.implicit_matvec(g, cA * Ep, cA * En, xs, E, u, dt)
+    Y = np.zeros_like(u)
+    harness.fvm_host_mvec(*a.common, a.p([dt, dt, tau, kappa, cA, ax]), a.p(E), a.p(u),
+                          Y.ctypes.data_as(C.POINTER(C.c_double)))
+    assert np.max(np.abs(Y - ref)) <= 1e-12 * np.max(np.abs(ref))
+    # preconditioner
+    dinv, H = coll.inverse_factors(dt * tau * kappa)
+    ref = F.op_split_step(g, E, u, dt)
+    harness.fvm_host_precond(*a.common, a.p(dinv), a.p(H), C.c_double(tau * cA), C.c_double(ax), C.c_double(dt),
+                             a.p(E), a.p(u), Y.ctypes.data_as(C.POINTER(C.c_double)))
+    assert np.max(np.abs(Y - ref)) <= 1e-11 * np.max(np.abs(ref))
+    # semi-Lagrangian advection at a step and field that move the departure points by a fraction
+    # of a cell to a few cells in x and in v
+    dts, Es = 5e-3, 0.1 * E
+    ref = F.sl_advect(u, vr, vt, x, Es, dts, tau, vth, L, g["qe"], g["me"], 0.0, vmax)
+    assert 0.0 < np.mean(ref == 0.0) < 0.5
+    dims = (C.c_int * 3)(Nr, Nvt, Nx)
+    harness.fvm_host_sl(dims, a.p(vr), a.p(vt), a.p(x), C.c_double(0.0), C.c_double(vmax), C.c_double(dts * ax),
+                        C.c_double(dts * tau * cA), a.p(Es), a.p(u), Y.ctypes.data_as(C.POINTER(C.c_double)))
+    assert np.max(np.abs(Y - ref)) <= 1e-12 * np.max(np.abs(ref))
