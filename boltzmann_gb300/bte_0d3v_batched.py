@@ -89,6 +89,17 @@ def _ptr(t):
     return C.c_void_p(t.data_ptr())
 
 
+def anisotropic_from_maxwellian(f, nsh):
+    """The "anisotropic" initial state from the Maxwellian one (bte_0d3v_batched.py:500-503): the
+    Maxwellian times 1 + cos(theta) = 2 sqrt(pi) Y_00 + sqrt(4 pi / 3) Y_10, so its l = 1
+    coefficients are the l = 0 ones divided by sqrt(3) and the rest stay as they are (zero for
+    l >= 2). f: (n, n_pts), layout p * nsh + l."""
+    out = np.array(f, dtype=np.float64, copy=True)
+    if nsh >= 2:
+        out[1::nsh] = out[0::nsh] / np.sqrt(3.0)
+    return out
+
+
 def normalization_scale(mass, F, vth):
     """The per-column scale of normalized_distribution (bte_0d3v_batched.py:1204-1217):
     (mass . f) / (Y_00 4 pi) * 2 (vth / c_gamma)^3, Y_00 4 pi = sqrt(4 pi). Works on NumPy arrays
@@ -216,10 +227,11 @@ class bte_0d3v_batched:
         return out
 
     def initialize(self, grid_idx, n_pts, init_type="maxwellian"):
-        """Maxwellian initial state, (n, n_pts) NumPy array as the reference returns
-        (bte_0d3v_batched.py:481-520)."""
-        if init_type != "maxwellian":
-            raise NotImplementedError("only the maxwellian initial condition is supported")
+        """Initial state, (n, n_pts) NumPy array as the reference returns
+        (bte_0d3v_batched.py:481-520): "maxwellian", or "anisotropic" (the Maxwellian times
+        1 + cos(theta), `anisotropic_from_maxwellian`)."""
+        if init_type not in ("maxwellian", "anisotropic"):
+            raise NotImplementedError("init_type must be maxwellian or anisotropic")
         torch = _torch()
         prof = self.profile_tt_all[grid_idx]
         prof[pp.INIT_COND].start()
@@ -228,6 +240,8 @@ class bte_0d3v_batched:
         stream = torch.cuda.current_stream().cuda_stream
         _lib.check(_lib.load().bte_initialize(self._grid[grid_idx], n_pts, _ptr(f), C.c_void_p(stream)), "bte_initialize")
         out = f.t().contiguous().cpu().numpy()
+        if init_type == "anisotropic":
+            out = anisotropic_from_maxwellian(out, len(self._par_lm[grid_idx]))
         prof[pp.INIT_COND].stop()
         return out
 

@@ -72,3 +72,14 @@ def test_checkpoint_round_trip(tmp_path):
     with np.load(pre + ".npz") as F:
         assert sorted(F.files) == sorted(["time[T]", "dt[T]", "edf", "ne[m^-3]", "Te[eV]"])
         assert np.array_equal(F["ne[m^-3]"], ne) and np.array_equal(F["Te[eV]"], Te)
+
+
+def test_anisotropic_initial_state_matches_the_reference():
+    """init_type "anisotropic" from the Maxwellian against the reference's own
+    initialize(..., "anisotropic") (tests/golden/init_reference.npz), l_max 1 and 2."""
+    from boltzmann_gb300.bte_0d3v_batched import anisotropic_from_maxwellian
+    g = dict(np.load(os.path.join(HERE, "golden", "init_reference.npz")))
+    for n_sp, l_max in ((64, 1), (16, 2)):
+        ref = g["anisotropic_%d_%d" % (n_sp, l_max)]
+        out = anisotropic_from_maxwellian(g["maxwellian_%d_%d" % (n_sp, l_max)], l_max + 1)
+        assert np.max(np.abs(out - ref)) <= 1e-13 * np.max(np.abs(ref)), (n_sp, l_max)

@@ -149,3 +149,11 @@ def test_checkpoint_through_the_solver(synthetic_xs, tmp_path):
     assert (t, dt) == (0.5, 1e-3) and np.array_equal(v.cpu().numpy(), q["fvm_vp"])
     with np.load(pre + ".npz") as F:
         assert _rel(F["ne[m^-3]"], q["fvm_vp_ne"]) <= 1e-12
+
+
+def test_anisotropic_initial_state(synthetic_xs):
+    """initialize(..., "anisotropic") through the library's Maxwellian against the reference's."""
+    from helpers import gpu_solver
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "init_reference.npz")))
+    s, _ = gpu_solver(synthetic_xs, 64, 1, False, 2)
+    assert _rel(s.initialize(0, 2, "anisotropic"), g["anisotropic_64_1"]) <= 1e-12
