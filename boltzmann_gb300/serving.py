@@ -237,6 +237,23 @@ class BteServer:
             self._cv.notify_all()
         return req
 
+    def cancel(self, req: SolveRequest) -> bool:
+        """Withdraw a request that is still queued: it completes at once with error "cancelled"
+        and holds no slots or budget. A request already admitted runs to the end (its points
+        share the engine's batched iterations); the call then returns False."""
+        key = (int(req.n_sp), int(req.l_max))
+        with self._cv:
+            w = self._workers.get(key)
+            idx = None if w is None else next((i for i, r in enumerate(w.queue) if r is req), None)
+            if idx is None:
+                return False
+            del w.queue[idx]
+            req.error = "cancelled"
+            req.t_done = time.perf_counter()
+            self._cv.notify_all()
+        req.done.set()
+        return True
+
     def close(self):
         with self._cv:
             self._stop = True

@@ -141,3 +141,31 @@ def test_bad_requests_and_engine_failure():
         assert srv.errors
         with pytest.raises(RuntimeError, match="failed"):
             srv.submit(make_req(rng, P=2))               # the grid's worker has stopped
+
+
+def test_cancel_a_queued_request():
+    """A request still queued behind a full engine can be withdrawn: it completes at once with
+    error "cancelled", never reaches the engine, and the requests behind it still run. A request
+    already admitted cannot be withdrawn."""
+    rng = np.random.default_rng(8)
+    eng = {}
+
+    def factory(k):
+        eng[k] = FakeEngine(k, capacity=16, step_s=0.05)
+        return eng[k]
+
+    with BteServer(None, [(64, 1)], backend_factory=factory) as srv:
+        big = make_req(rng, P=16)
+        big.E = np.full(16, 3.5)                       # four engine steps
+        srv.submit(big)
+        t0 = time.perf_counter()
+        while big.t_admit == 0.0 and time.perf_counter() - t0 < 5:
+            time.sleep(0.005)
+        a, b = srv.submit(make_req(rng, P=8)), srv.submit(make_req(rng, P=8))
+        assert srv.cancel(a)
+        assert a.done.is_set() and a.error == "cancelled" and a.ff is None
+        assert not srv.cancel(big)                     # already admitted
+        wait_all([big, b], timeout=10)
+        assert big.error is None and b.error is None and b.ff is not None
+        assert not srv.cancel(b)                       # finished
+        assert srv.used == 0
