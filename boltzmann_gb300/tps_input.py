@@ -84,3 +84,24 @@ def requests_from_tps(params: dict, n_sp: int, l_max: int, max_points: int = 512
                                 Tg=params["Tg"][a:b].copy(), E=params["E"][a:b].copy(),
                                 ns_by_n0=np.ascontiguousarray(params["ns_by_n0"][:, a:b]), ee=ee, rid=k))
     return out
+
+
+def write_qoi_csv(fname: str, n0, ne, ni, Tg, E, qoi: dict, collision_names) -> str:
+    """The batched driver's QoI output (bte_0d3v_batched_driver.py:215-232): `fname`_qoi.csv
+    with the header n0, ne, ni, Tg, E, energy, mobility, diffusion and one column per
+    collision name, one row per point, numbers written as the driver's csv writer writes its
+    NumPy rows. qoi holds "energy", "mobility", "diffusion" (P,) and "rates" (n_proc, P), as
+    the solver returns them (device tensors are copied to the host). Returns the path."""
+    host = lambda a: np.asarray(a.cpu().numpy() if hasattr(a, "cpu") else a, dtype=np.float64)
+    cols = [host(v).reshape(-1, 1) for v in (n0, ne, ni, Tg, E, qoi["energy"], qoi["mobility"], qoi["diffusion"])]
+    rates = host(qoi["rates"])
+    if rates.shape[0] != len(collision_names):
+        raise ValueError("rates has %d rows for %d collisions" % (rates.shape[0], len(collision_names)))
+    cols += [rates[i].reshape(-1, 1) for i in range(rates.shape[0])]
+    data = np.concatenate(cols, axis=1)
+    path = "%s_qoi.csv" % fname
+    with open(path, "w", encoding="UTF8") as fh:
+        w = csv.writer(fh, delimiter=",")
+        w.writerow(["n0", "ne", "ni", "Tg", "E", "energy", "mobility", "diffusion"] + [str(g) for g in collision_names])
+        w.writerows(data)
+    return path

@@ -65,3 +65,21 @@ def test_requests_split_in_row_order(tmp_path):
     np.testing.assert_array_equal(np.concatenate([r.E for r in reqs]), prm["E"])
     np.testing.assert_array_equal(np.concatenate([r.ns_by_n0 for r in reqs], axis=1), prm["ns_by_n0"])
     assert all(r.n_sp == 64 and r.l_max == 1 and r.ee for r in reqs)
+
+
+def test_qoi_csv_has_the_driver_layout(tmp_path):
+    """write_qoi_csv: the driver's header and one row per point, values read back exactly."""
+    import csv
+    from boltzmann_gb300.tps_input import write_qoi_csv
+    rng = np.random.default_rng(4)
+    P = 5
+    n0, ne, Tg, E = rng.uniform(1e22, 4e22, P), rng.uniform(1e14, 1e16, P), np.full(P, 300.0), rng.uniform(1, 1e3, P)
+    qoi = {"energy": rng.random(P), "mobility": rng.random(P), "diffusion": rng.random(P), "rates": rng.random((3, P))}
+    path = write_qoi_csv(str(tmp_path / "run"), n0, ne, ne, Tg, E, qoi, ["C0", "C1", "C2"])
+    rows = list(csv.reader(open(path)))
+    assert rows[0] == ["n0", "ne", "ni", "Tg", "E", "energy", "mobility", "diffusion", "C0", "C1", "C2"]
+    got = np.array(rows[1:], dtype=np.float64)
+    want = np.column_stack([n0, ne, ne, Tg, E, qoi["energy"], qoi["mobility"], qoi["diffusion"], qoi["rates"].T])
+    assert got.shape == (P, 11) and np.array_equal(got, want)
+    with pytest.raises(ValueError):
+        write_qoi_csv(str(tmp_path / "bad"), n0, ne, ne, Tg, E, qoi, ["C0"])
