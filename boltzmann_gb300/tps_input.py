@@ -87,10 +87,10 @@ def requests_from_tps(params: dict, n_sp: int, l_max: int, max_points: int = 512
 
 
 def write_qoi_csv(fname: str, n0, ne, ni, Tg, E, qoi: dict, collision_names) -> str:
-    """The batched driver's QoI output (bte_0d3v_batched_driver.py:215-232): `fname`_qoi.csv
-    with the header n0, ne, ni, Tg, E, energy, mobility, diffusion and one column per
-    collision name, one row per point, numbers written as the driver's csv writer writes its
-    NumPy rows. qoi holds "energy", "mobility", "diffusion" (P,) and "rates" (n_proc, P), as
+    """The QoI output of the reference's batched driver script (bte_0d3v_batched_driver.py:215-232):
+    `fname`_qoi.csv with the header n0, ne, ni, Tg, E, energy, mobility, diffusion and one column
+    per collision name, one row per point, numbers written as that script's csv writer writes
+    its NumPy rows. qoi holds "energy", "mobility", "diffusion" (P,) and "rates" (n_proc, P), as
     the solver returns them (device tensors are copied to the host). Returns the path."""
     host = lambda a: np.asarray(a.cpu().numpy() if hasattr(a, "cpu") else a, dtype=np.float64)
     cols = [host(v).reshape(-1, 1) for v in (n0, ne, ni, Tg, E, qoi["energy"], qoi["mobility"], qoi["diffusion"])]
