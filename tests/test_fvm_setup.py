@@ -150,3 +150,13 @@ def test_radial_components_match_the_reference(synthetic_xs):
     assert np.max(np.abs(R - q["fvm_vp_radial"])) <= 1e-14 * np.max(np.abs(q["fvm_vp_radial"]))
     with pytest.raises(ValueError):
         P.fvm_radial_components(U, st.vr, 2, np.array([79.9]), st.vth)
+
+
+@pytest.mark.parametrize("p", [1, 3])
+def test_bands_at_other_orders_match_the_reference(p):
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "fvm_orders_reference.npz")))
+    q = lambda k: g["p%d_%s" % (p, k)]
+    ops = P.fvm_upwind_operators(q("vr"), q("vt"), q("x"), p, p, p, float(q("domain")[1]))
+    for k, b in P.fvm_bands(ops, p, p, p).items():
+        assert b.shape == q(k).shape
+        assert np.max(np.abs(b - q(k))) <= 1e-12 * np.max(np.abs(q(k))), k

@@ -144,3 +144,19 @@ def test_semi_lagrangian_step_matches_the_reference():
                        float(gs["kdomain"][1]))
     assert np.max(np.abs(v_sl - gs["v_sl"])) <= 1e-14 * np.max(np.abs(gs["v_sl"]))
     assert np.max(np.abs(gs["PmatC"] @ v_sl - gs["step"])) <= 1e-14 * np.max(np.abs(gs["step"]))
+
+
+@pytest.mark.parametrize("p", [1, 3])
+def test_upwind_operators_at_other_orders(p):
+    """The oracle's bands, v-space advection matrices and x-shift bands against the reference's
+    own set-up at stencil orders 1 and 3 (tests/golden/fvm_orders_reference.npz)."""
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "fvm_orders_reference.npz")))
+    q = lambda k: g["p%d_%s" % (p, k)]
+    vr, vt, x, vmax = q("vr"), q("vt"), q("x"), float(q("domain")[1])
+    for k, b in F.fvm_upwind_bands(vr, vt, x, p, p, p, vmax).items():
+        assert np.max(np.abs(b - q(k))) <= 1e-12 * np.max(np.abs(q(k))), k
+    Ep, En = F.adv_v_fvm(vr, vt, p, p, vmax)
+    for mine, k in ((Ep, "op_adv_v_Ep"), (En, "op_adv_v_En")):
+        assert np.max(np.abs(float(q("cA")) * mine - q(k))) <= 1e-12 * np.max(np.abs(q(k))), k
+    xs = F.x_shift_bands(vr, vt, x, p, float(q("ax")), float(q("dt")))
+    assert np.max(np.abs(xs - q("bte_x_shift_diag"))) <= 1e-12 * np.max(np.abs(q("bte_x_shift_diag")))
