@@ -433,8 +433,11 @@ class FvmImplicit:
     def __del__(self):
         h = getattr(self, "_h", None)
         if h:
-            _lib.load().bte_fvm_destroy(h)
             self._h = None
+            try:
+                _lib.load().bte_fvm_destroy(h)
+            except Exception:   # interpreter shutdown: the library may already be gone
+                pass
 
     @staticmethod
     def _fail(rc, what):

@@ -403,6 +403,9 @@ int bte_fvm_create(int device, int Nr, int Nvt, int Nx, int ndr, int ndt, int nd
 int bte_fvm_destroy(bte_fvm* h) {
     if (!h) return BTE_OK;
     cudaSetDevice(h->device);
+    cudaFree(h->Kr);   // the GMRES buffers, sized by the largest restart so far
+    cudaFree(h->part);
+    cudaFree(h->hd);
     fvm_free(h);
     delete h;
     return BTE_OK;
