@@ -475,13 +475,13 @@ class FvmImplicit:
                                                _ptr(Y), _stream()), "bte_fvm_precond")
         return Y.reshape(self.Nr * self.Nvt, self.Nx)
 
-    def step(self, coef, E, V, alpha=1.0, rtol=1e-12, atol=1e-14, restart=30, max_iter=600, pc_left=False):
-        """Solve rhs_mvec(V') = V (inflow values zeroed), the op-split preconditioner on the right
-        or (pc_left) on the left; returns V' (Nr * Nvt, Nx)."""
+    def step(self, coef, E, V, alpha=1.0, rtol=1e-12, atol=1e-14, restart=30, max_iter=600, pc_mode=0):
+        """Solve rhs_mvec(V') = V (inflow values zeroed); pc_mode 0: the op-split preconditioner
+        on the right, 1: on the left, 2: none. Returns V' (Nr * Nvt, Nx)."""
         n = self.Nr * self.Nvt * self.Nx
         Vd, Ed = self._dev(V, n).clone(), self._dev(E, self.Nx)
         info = (C.c_double * 4)()
-        rc = _lib.load().bte_fvm_step(self._h, C.byref(coef), float(alpha), int(bool(pc_left)), _ptr(Ed), _ptr(Vd),
+        rc = _lib.load().bte_fvm_step(self._h, C.byref(coef), float(alpha), int(pc_mode), _ptr(Ed), _ptr(Vd),
                                       float(rtol), float(atol), int(restart), int(max_iter), info, _stream())
         self._fail(rc, "bte_fvm_step")
         self.gmres_info = {"iterations": int(info[0]), "residual_abs": info[1], "residual_rel": info[2],
@@ -528,7 +528,8 @@ _SOLVERS = {"fully_implicit": "fully_implicit", "XVTVRC": "op_split", "sl_implic
 def fvm_setup(par):
     """The host set-up of the FVM solver from the reference's parameter table (a TOML path with a
     [bte] table, or the table as a dict): vspace_type = 0, solver_type "fully_implicit" or
-    "XVTVRC" or "sl_implicit", the op-split (XVTVRC) preconditioner, `collisions` an LXCat file. Returns a
+    "XVTVRC" or "sl_implicit", pc_type "xvtvrc_solve" (the default) or "none", `collisions` an
+    LXCat file. Returns a
     namespace: params, vth, vmax, vr, vr_qw, vt, vt_qw, x, grid_info, collisions (an
     `FvmCollisions`), bands (the six `fvm_bands` arrays). Mirrors bte_1d3v.__init__ / init()
     (bte_1d3v_solver.py:77-216,245-266,377-470,1403-1470)."""
@@ -543,8 +544,8 @@ def fvm_setup(par):
     p.pvr, p.pvt, p.px = int(tp.get("pvr", 3)), int(tp.get("pvt", 3)), int(tp.get("px", 1))
     p.adaptive_grid = bool(tp.get("adaptive_grid", 1))
     p.pc_type = str(tp.get("pc_type", "xvtvrc_solve"))
-    if p.pc_type != "xvtvrc_solve":
-        raise NotImplementedError("only the op-split XVTVRC preconditioner is provided")
+    if p.pc_type not in ("xvtvrc_solve", "none"):
+        raise NotImplementedError("pc_type must be the op-split XVTVRC preconditioner or none")
     if tp.get("solver_type") not in _SOLVERS:
         raise NotImplementedError("solver_type must be one of %s for the FVM v-space" % sorted(_SOLVERS))
     p.solver = _SOLVERS[tp["solver_type"]]
@@ -648,8 +649,9 @@ class bte_1d3v_fvm:
             return self.step_op_split(E, v, dv, time, dt, XVTVRC, verbose)
         if p.solver == "semi_lagrangian":
             return self.solver.sl_step(self._coef(dt), E, v)
+        mode = 2 if p.pc_type == "none" else (1 if pc_left else 0)
         out = self.solver.step(self._coef(dt), E, v, alpha=gmres_pc_vr, rtol=p.rtol, atol=p.atol,
-                               restart=p.gmres_rsrt, max_iter=p.gmres_maxiter, pc_left=pc_left)
+                               restart=p.gmres_rsrt, max_iter=p.gmres_maxiter, pc_mode=mode)
         info = self.solver.gmres_info
         self.gmres_info = info
         if info["status"] != 0:

@@ -281,9 +281,15 @@ struct DeviceOps {
     double hstep;
     size_t N;
     double *B, *X, *R, *W, *Z, *T, *Kr;
+    bool identity;   // pc_type "none": no preconditioner
 
     int matvec(const double* x, double* y) { return fvm_mvec(h, c, E, x, y, s); }
-    int precond(const double* x, double* y) { return fvm_precond(h, hstep, x, y, s); }
+    int precond(const double* x, double* y) {
+        if (!identity) return fvm_precond(h, hstep, x, y, s);
+        if (cudaMemcpyAsync(y, x, N * 8, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+            return fvm_fail(BTE_ERR_CUDA, "copy failed");
+        return BTE_OK;
+    }
     int dots(int k, const double* V, const double* w, double* out) {
         k_fvm_dots_partial<<<dim3(FVM_RED, k), FT, 0, s>>>(N, V, w, h->part);
         k_fvm_dots_final<<<k, FT, 0, s>>>(FVM_RED, h->part, h->hd);
@@ -503,12 +509,13 @@ int bte_fvm_sl_step(bte_fvm* h, const bte_fvm_coef* c, const double* E, const do
     return fvm_coll_solve(h, h->A, Y, s);
 }
 
-int bte_fvm_step(bte_fvm* h, const bte_fvm_coef* c, double alpha, int pc_left, const double* E, double* V, double rtol,
+int bte_fvm_step(bte_fvm* h, const bte_fvm_coef* c, double alpha, int pc_mode, const double* E, double* V, double rtol,
                  double atol, int restart, int max_iter, double* info4, void* stream) {
     if (!h || !E || !V || !info4) return fvm_fail(BTE_ERR_ARG, "bte_fvm_step: null argument");
     if (!coef_ok(c) || !std::isfinite(alpha)) return fvm_fail(BTE_ERR_ARG, "bte_fvm_step: coefficients not finite");
     if (restart < 1 || restart > 500 || max_iter < 0) return fvm_fail(BTE_ERR_ARG, "bte_fvm_step: 1 <= restart <= 500");
-    if (!h->have_inverse) return fvm_fail(BTE_ERR_STATE, "bte_fvm_step: no collision inverse set");
+    if (pc_mode < 0 || pc_mode > 2) return fvm_fail(BTE_ERR_ARG, "bte_fvm_step: pc_mode must be 0, 1 or 2");
+    if (pc_mode != 2 && !h->have_inverse) return fvm_fail(BTE_ERR_STATE, "bte_fvm_step: no collision inverse set");
     cudaSetDevice(h->device);
     cudaStream_t s = (cudaStream_t)stream;
     const size_t N = h->N;
@@ -538,10 +545,10 @@ int bte_fvm_step(bte_fvm* h, const bte_fvm_coef* c, double alpha, int pc_left, c
     if (cudaMemcpyAsync(h->B, V, N * 8, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
         return fvm_fail(BTE_ERR_CUDA, "bte_fvm_step: copy of the state failed");
     if (int rc = sweep_rc(bte_fvm_inflow_zero(h->Nr, h->Nvt, h->Nx, h->vt, h->B, s), "inflow")) return rc;
-    DeviceOps op{h, s, fc, E, alpha * fc.dt, N, h->B, h->X, h->R, h->W, h->Z, h->Tv, h->Kr};
+    DeviceOps op{h, s, fc, E, alpha * fc.dt, N, h->B, h->X, h->R, h->W, h->Z, h->Tv, h->Kr, pc_mode == 2};
     FvmGmresInfo info{};
-    if (int rc = pc_left ? fvm_gmres_left(op, restart, rtol, atol, max_iter, &info)
-                         : fvm_gmres(op, restart, rtol, atol, max_iter, &info))
+    if (int rc = pc_mode == 1 ? fvm_gmres_left(op, restart, rtol, atol, max_iter, &info)
+                              : fvm_gmres(op, restart, rtol, atol, max_iter, &info))
         return rc;
     if (cudaMemcpyAsync(V, h->X, N * 8, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)

@@ -52,11 +52,12 @@ int bte_fvm_precond(bte_fvm* h, double cE, double ax, double hstep, const double
                     void* stream);
 
 /* One fully implicit step (:1890-2009): solves rhs_mvec(V') = V with its inflow values zeroed,
- * by restarted GMRES(restart) preconditioned with the op-split step at alpha dt, on the right
- * (pc_left = 0; utils.py:1172-1262) or on the left (pc_left = 1; utils.py:1266-1357), to
- * ||r|| <= max(atol, rtol ||b||) or max_iter iterations; V [Nr * Nvt * Nx] is replaced by V'.
+ * by restarted GMRES(restart) to ||r|| <= max(atol, rtol ||b||) or max_iter iterations;
+ * V [Nr * Nvt * Nx] is replaced by V'. pc_mode: 0 the op-split step at alpha dt as a right
+ * preconditioner (utils.py:1172-1262), 1 as a left one (utils.py:1266-1357), 2 none
+ * (pc_type "none", :1979-1982; no collision inverse needed).
  * info4: iterations, ||r||, ||r|| / ||b||, status (0 converged, 1 not converged). */
-int bte_fvm_step(bte_fvm* h, const bte_fvm_coef* c, double alpha, int pc_left, const double* E, double* V, double rtol,
+int bte_fvm_step(bte_fvm* h, const bte_fvm_coef* c, double alpha, int pc_mode, const double* E, double* V, double rtol,
                  double atol, int restart, int max_iter, double* info4, void* stream);
 
 /* The grids of the semi-Lagrangian step: x [Nx] ascending, the velocity domain [vmin, vmax]

@@ -117,8 +117,10 @@ struct HostOps {
     double cE, hstep;
     size_t N;
     double *B, *X, *R, *W, *Z, *T, *Kr;
+    bool identity;
     int matvec(const double* x, double* y) { mvec(*s, c, E, x, y); return 0; }
     int precond(const double* x, double* y) {
+        if (identity) { memcpy(y, x, N * sizeof(double)); return 0; }
         std::vector<double> tmp(x, x + N);
         ::precond(*s, dinv, H, cE, c.ax, hstep, E, tmp.data(), y);
         return 0;
@@ -258,7 +260,7 @@ void fvm_host_sl(const int* dims, const double* vr, const double* vt, const doub
 // V replaced by the step's solution; info4 as bte_fvm_step's
 int fvm_host_step(const int* dims, const double* vr, const double* vt, const double* w, const double* loss,
                   const double* gain, const double* const* bands, const double* dinv, const double* H, const double* c6,
-                  double alpha, int pc_left, const double* E, double* V, double rtol, double atol, int restart,
+                  double alpha, int pc_mode, const double* E, double* V, double rtol, double atol, int restart,
                   int max_iter, double* info4) {
     Setup s = make_setup(dims[0], dims[1], dims[2], dims[3], dims[4], dims[5], vr, vt, w, loss, gain, bands);
     const FvmCoef c = coef(c6);
@@ -267,10 +269,10 @@ int fvm_host_step(const int* dims, const double* vr, const double* vt, const dou
     for (int r = 0; r < dims[0]; ++r)
         for (int j = 0; j < dims[1]; ++j) B[((size_t)r * dims[1] + j) * dims[2] + (s.north[j] ? 0 : dims[2] - 1)] = 0.0;
     HostOps op{&s, c, E, dinv, H, c.tau * c.cA, alpha * c.dt, N, B.data(), X.data(), R.data(), W.data(), Z.data(),
-               T.data(), Kr.data()};
+               T.data(), Kr.data(), pc_mode == 2};
     FvmGmresInfo info{};
-    const int rc = pc_left ? fvm_gmres_left(op, restart, rtol, atol, max_iter, &info)
-                           : fvm_gmres(op, restart, rtol, atol, max_iter, &info);
+    const int rc = pc_mode == 1 ? fvm_gmres_left(op, restart, rtol, atol, max_iter, &info)
+                                : fvm_gmres(op, restart, rtol, atol, max_iter, &info);
     memcpy(V, X.data(), N * sizeof(double));
     info4[0] = info.iterations;
     info4[1] = info.rnorm;

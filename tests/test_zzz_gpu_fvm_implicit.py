@@ -157,3 +157,13 @@ def test_anisotropic_initial_state(synthetic_xs):
     g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "init_reference.npz")))
     s, _ = gpu_solver(synthetic_xs, 64, 1, False, 2)
     assert _rel(s.initialize(0, 2, "anisotropic"), g["anisotropic_64_1"]) <= 1e-12
+
+
+def test_step_without_preconditioner(synthetic_xs, g):
+    """pc_type "none": plain GMRES on rhs_mvec reaches the reference's step."""
+    from boltzmann_gb300.bte_1d3v_fvm import bte_1d3v_fvm
+    s = bte_1d3v_fvm(dict(PARAMS, collisions=synthetic_xs, pc_type="none"))
+    s.init(float(g["dt"]))
+    y = s.step(g["E"], g["v0"], None, 0.0, float(g["dt"])).cpu().numpy()
+    assert s.gmres_info["status"] == 0
+    assert _rel(y, g["step"]) <= 1e-10
