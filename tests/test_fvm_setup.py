@@ -104,7 +104,7 @@ def test_setup_from_the_parameter_table(synthetic_xs, g):
     assert p.n0 == pytest.approx(float(g["n0"]), rel=1e-14) and p.solver == "fully_implicit"
 
 
-@pytest.mark.parametrize("change", [dict(vspace_type=1), dict(pc_type="none"), dict(solver_type="xvx_strang_split"),
+@pytest.mark.parametrize("change", [dict(vspace_type=1), dict(pc_type="xvx_solve"), dict(solver_type="xvx_strang_split"),
                                     dict(ic_file="ic.h5"), dict(xspace_type=2)])
 def test_setup_refuses_what_is_not_provided(synthetic_xs, change):
     from helpers import FVM_IMPLICIT_PARAMS
