@@ -328,6 +328,23 @@ class bte_1d3v:
         t, dt, v = read_checkpoint(fprefix)
         return t, dt, self.torch.as_tensor(v, dtype=self.torch.float64, device="cuda")
 
+    def normalize_edf(self, v):
+        """normalize_edf (:2043-2055): the ordinates v divided, per x, by the mass functional of
+        their harmonics in the reference's units, (mass . v_lm) / sqrt(4 pi) 2 (vth / c_gamma)^3."""
+        from .bte_0d3v_batched import normalization_scale
+        V = self.torch.as_tensor(v, dtype=self.torch.float64, device="cuda").reshape(self.dof_vr * self.dof_vt,
+                                                                                      self.dof_x)
+        return V / normalization_scale(self.mass_op, self.ords_to_sph(V), self.vth)
+
+    def asnumpy(self, x):
+        return x.cpu().numpy() if hasattr(x, "cpu") else np.asarray(x)
+
+    def copy_operators_H2D(self, dev_id=0):
+        """The operators live on the device from construction on: nothing to copy."""
+
+    def copy_operators_D2H(self, dev_id=0):
+        """The operators stay on the device; their host copies are the set-up matrices."""
+
     def compute_radial_components(self, ev, v):
         """compute_radial_components (:1139-1160): f_l(eps) of the ordinates v at the energies ev
         (eV), (Nx, num_sh, len(ev)) NumPy array, from the grid's B-spline evaluation

@@ -702,6 +702,20 @@ class bte_1d3v_fvm:
         t, dt, v = read_checkpoint(fprefix)
         return t, dt, self.torch.as_tensor(v, dtype=self.torch.float64, device="cuda")
 
+    def normalize_edf(self, v):
+        """normalize_edf (:2043-2062) on the FVM grid: v / ((mass . v) 2 (vth / c_gamma)^3) per x."""
+        V = self.torch.as_tensor(v, dtype=self.torch.float64, device="cuda").reshape(self.dof_v, self.dof_x)
+        return V / ((self.op_qoi[0] @ V) * (2.0 * (self.bs_vth / C_GAMMA) ** 3))
+
+    def asnumpy(self, x):
+        return x.cpu().numpy() if hasattr(x, "cpu") else np.asarray(x)
+
+    def copy_operators_H2D(self, dev_id=0):
+        """The operators live on the device from construction on: nothing to copy."""
+
+    def copy_operators_D2H(self, dev_id=0):
+        """The operators stay on the device; host copies are the set-up's (fvm_setup)."""
+
     def compute_radial_components(self, ev, v):
         """compute_radial_components (:1162-1177): (Nx, num_sh, len(ev)) NumPy array."""
         vsh = self.ords_to_sph(v).cpu().numpy()

@@ -167,3 +167,21 @@ def test_step_without_preconditioner(synthetic_xs, g):
     y = s.step(g["E"], g["v0"], None, 0.0, float(g["dt"])).cpu().numpy()
     assert s.gmres_info["status"] == 0
     assert _rel(y, g["step"]) <= 1e-10
+
+
+def test_normalize_edf_both_v_spaces(synthetic_xs):
+    """normalize_edf: on the FVM grid against the reference's formula with its own mass
+    functional; on the spectral grid, scale-invariant and consistent with compute_qoi's rates."""
+    import ast
+    from boltzmann_gb300.bte_1d3v import bte_1d3v
+    from boltzmann_gb300.bte_1d3v_fvm import C_GAMMA, bte_1d3v_fvm
+    q = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "qoi_1d3v_reference.npz")))
+    f = bte_1d3v_fvm(dict(PARAMS, collisions=synthetic_xs))
+    v = q["fvm_vp"]
+    want = v / ((q["fvm_op_mass"] @ v) * (2.0 * (f.bs_vth / C_GAMMA) ** 3))
+    assert _rel(f.normalize_edf(v).cpu().numpy(), want) <= 1e-12
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "bte1d_reference.npz")))
+    s = bte_1d3v(dict(ast.literal_eval(str(g["params"])), collisions=synthetic_xs))
+    v3 = np.real(g["v3"])
+    n1, n3 = s.normalize_edf(v3).cpu().numpy(), s.normalize_edf(3.0 * v3).cpu().numpy()
+    assert _rel(n3, n1) <= 1e-13
