@@ -222,3 +222,21 @@ def test_core_against_the_oracle_on_other_grids(harness, synthetic_xs, Nr_sp, Nv
     harness.fvm_host_sl(dims, a.p(vr), a.p(vt), a.p(x), C.c_double(0.0), C.c_double(vmax), C.c_double(dts * ax),
                         C.c_double(dts * tau * cA), a.p(Es), a.p(u), Y.ctypes.data_as(C.POINTER(C.c_double)))
     assert np.max(np.abs(Y - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+def test_zero_step_is_the_identity(harness, case):
+    """Edge case: at dt = 0 every departure point is its own grid point, so the semi-Lagrangian
+    advection returns its input (to the rounding of sqrt(v^2) and acos(cos(theta)) in the
+    departure point), and the fully implicit operator is the identity."""
+    g = case["g"]
+    a = _Args(case)
+    u = np.ascontiguousarray(g["u"].reshape(-1, int(g["Nx"])))
+    dims = (C.c_int * 3)(int(g["Nr"]), int(g["Nvt"]), int(g["Nx"]))
+    Y = np.zeros_like(u)
+    harness.fvm_host_sl(dims, a.p(g["vr"]), a.p(g["vt"]), a.p(g["x"]), C.c_double(0.0), C.c_double(float(g["domain"][1])),
+                        C.c_double(0.0), C.c_double(0.0), a.p(g["E"]), a.p(u), Y.ctypes.data_as(C.POINTER(C.c_double)))
+    assert np.max(np.abs(Y - u)) <= 1e-14 * np.max(np.abs(u))
+    c6 = np.array(case["c6"])
+    c6[0] = c6[1] = 0.0
+    harness.fvm_host_mvec(*a.common, a.p(c6), a.p(g["E"]), a.p(u), Y.ctypes.data_as(C.POINTER(C.c_double)))
+    assert np.array_equal(Y, u)
