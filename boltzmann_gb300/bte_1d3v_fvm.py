@@ -549,6 +549,10 @@ def fvm_setup(par):
     if tp.get("solver_type") not in _SOLVERS:
         raise NotImplementedError("solver_type must be one of %s for the FVM v-space" % sorted(_SOLVERS))
     p.solver = _SOLVERS[tp["solver_type"]]
+    if p.solver == "fully_implicit" and int(tp.get("xspace_type", 1)) != 0:
+        # the reference's rhs_mvec needs the banded x-shift, which it builds only for the upwind
+        # x-space (bte_1d3v_solver.py:843-861, 1938-1939)
+        raise NotImplementedError("the fully implicit FVM step needs xspace_type = 0 (upwind x)")
     if tp.get("ic_file", ""):
         raise NotImplementedError("initial conditions from files are not provided")
     p.qe, p.me = QE, ME

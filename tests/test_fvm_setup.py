@@ -105,7 +105,7 @@ def test_setup_from_the_parameter_table(synthetic_xs, g):
 
 
 @pytest.mark.parametrize("change", [dict(vspace_type=1), dict(pc_type="xvx_solve"), dict(solver_type="xvx_strang_split"),
-                                    dict(ic_file="ic.h5"), dict(xspace_type=2)])
+                                    dict(ic_file="ic.h5"), dict(xspace_type=2), dict(xspace_type=1)])
 def test_setup_refuses_what_is_not_provided(synthetic_xs, change):
     from helpers import FVM_IMPLICIT_PARAMS
     with pytest.raises((NotImplementedError, ValueError)):
