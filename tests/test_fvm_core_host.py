@@ -240,3 +240,30 @@ def test_zero_step_is_the_identity(harness, case):
     c6[0] = c6[1] = 0.0
     harness.fvm_host_mvec(*a.common, a.p(c6), a.p(g["E"]), a.p(u), Y.ctypes.data_as(C.POINTER(C.c_double)))
     assert np.array_equal(Y, u)
+
+
+def test_operator_column_by_column(harness, case):
+    """Matrix-free against assembled, the reference's own matvec test pattern
+    (test_bte_1d_matvec.py): the shared core's rhs_mvec on every unit vector equals the
+    oracle's operator, column by column."""
+    from oracle import bte1d_fvm_oracle as F
+    g = case["g"]
+    Nr, Nvt, Nx = int(g["Nr"]), int(g["Nvt"]), int(g["Nx"])
+    n = Nr * Nvt * Nx
+    c6 = case["c6"]
+    Ep, En = F.adv_v_fvm(g["vr"], g["vt"], *case["p"][:2], float(g["domain"][1]))
+    xs = F.x_shift_bands(g["vr"], g["vt"], g["x"], case["p"][2], float(c6[5]), float(c6[1]))
+    go = dict(g, op_col_en=case["coll"].dense(), n0=float(c6[3]), np0=1.0)
+    a = _Args(case)
+    pc, pE = a.p(c6), a.p(g["E"])
+    e = np.zeros((n // Nx, Nx))
+    col = np.zeros_like(e)
+    worst = 0.0
+    for k in range(n):
+        e.reshape(-1)[k] = 1.0
+        harness.fvm_host_mvec(*a.common, pc, pE, e.ctypes.data_as(C.POINTER(C.c_double)),
+                              col.ctypes.data_as(C.POINTER(C.c_double)))
+        ref = F.implicit_matvec(go, c6[4] * Ep, c6[4] * En, xs, g["E"], e, float(c6[0]))
+        worst = max(worst, np.max(np.abs(col - ref)) / max(np.max(np.abs(ref)), 1e-300))
+        e.reshape(-1)[k] = 0.0
+    assert worst <= 1e-12, worst
