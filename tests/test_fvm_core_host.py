@@ -272,7 +272,7 @@ def test_operator_column_by_column(harness, case):
 def test_preconditioner_column_by_column(harness, case):
     """The op-split preconditioner (closed-form collision inverse and sweeps) on unit vectors
     equals the oracle's op-split step with the dense PmatC, column by column: 300 seeded
-    columns, including the first and last of every (r, j) line's x range."""
+    columns plus both ends of the first and the last x line."""
     from oracle import bte1d_fvm_oracle as F
     g = case["g"]
     Nx = int(g["Nx"])
