@@ -94,16 +94,18 @@ def test_preconditioner_matches_the_reference_op_split_step(harness, case):
     assert np.max(np.abs(Y - g["Mu"])) <= 1e-12 * np.max(np.abs(g["Mu"]))
 
 
-@pytest.mark.parametrize("restart,pc_mode", [(30, 0), (4, 0), (30, 1), (4, 1), (30, 2)])
-def test_gmres_step_matches_the_reference(harness, case, restart, pc_mode):
+@pytest.mark.parametrize("restart,pc_mode,alpha", [(30, 0, 1.0), (4, 0, 1.0), (30, 1, 1.0), (4, 1, 1.0), (30, 2, 1.0),
+                                                   (30, 0, 0.5)])
+def test_gmres_step_matches_the_reference(harness, case, restart, pc_mode, alpha):
     """The step to rtol 1e-12, the preconditioner on the right, on the left and none (also with
-    a short restart, so that restarts happen), against the reference's GMRES result."""
+    a short restart, so that restarts happen, and with the preconditioner's step scaled by
+    gmres_pc_vr = 0.5), against the reference's GMRES result."""
     g = case["g"]
     a = _Args(case)
     V = np.ascontiguousarray(g["v0"], dtype=np.float64).copy()
     info = (C.c_double * 4)()
     harness.fvm_host_step.restype = C.c_int
-    rc = harness.fvm_host_step(*a.common, a.p(case["dinv"]), a.p(case["H"]), a.p(case["c6"]), C.c_double(1.0),
+    rc = harness.fvm_host_step(*a.common, a.p(case["dinv"]), a.p(case["H"]), a.p(case["c6"]), C.c_double(alpha),
                                C.c_int(pc_mode), a.p(g["E"]), V.ctypes.data_as(C.POINTER(C.c_double)), C.c_double(float(g["rtol"])),
                                C.c_double(float(g["atol"])), C.c_int(restart), C.c_int(400), info)
     assert rc == 0
