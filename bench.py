@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--c5-plain-points", type=int, default=256,
                     help="points of the plain FP64 run of the config-5 sample (the same points, for a fair ratio)")
     ap.add_argument("--steps-1d", type=int, default=20)
+    ap.add_argument("--lu-kernel", type=int, default=0,
+                    help="FP32 factorization of the mixed form: 0 library choice, 2 tensor cores, 3 SIMT left-looking")
     return ap.parse_args()
 
 
@@ -144,7 +146,8 @@ def make_solver(xs, a, precision, dev):
     from boltzmann_gb300.workloads import EV_MAX, TE_NORM
     args = types.SimpleNamespace(threads=1, sp_order=3, spline_qpts=5, ee_collisions=1, verbose=0, use_gpu=1,
                                  Efreq=0.0, dt=1e-3, cycles=1, solver_type="steady-state", l_max=a.l_max,
-                                 Nr=a.n_sp - 1, n_pts=a.n_pts, precision=precision)
+                                 Nr=a.n_sp - 1, n_pts=a.n_pts, precision=precision,
+                                 lu_kernel=getattr(a, "lu_kernel", 0))
     s = bte_0d3v_batched(args, np.array([EV_MAX]), np.array([TE_NORM]), np.array([a.n_sp - 1]),
                          [[[l, 0] for l in range(a.l_max + 1)]], 1, [xs])
     s._dev_id = dev

@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libbte_gb300.so")
 BUILD_DIR = os.path.join(HERE, "_build")
-SOURCES = ["assembly.cu", "newton.cu", "lu.cu", "capi.cu", "bte1d.cu", "sweeps.cu", "fvm.cu"]
+SOURCES = ["assembly.cu", "newton.cu", "lu.cu", "lu_tc.cu", "capi.cu", "bte1d.cu", "sweeps.cu", "fvm.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr"]

@@ -531,8 +531,13 @@ cudaError_t factor_right(int P, int N, int NC, T* A, int ld, long long stride, i
 
 }  // namespace
 
+int bte_lu_tc_max_n();
+cudaError_t bte_lu_factor_tc(int P, int N, int NC, float* A, int ld, long long stride, int32_t* piv, int32_t* info,
+                             cudaStream_t s);
+
 // Factor P matrices in place; piv[P][N] receives perm (position -> stored row).
-// kernel: 0 = automatic (left-looking for N <= 512), 1 = right-looking.
+// kernel: 0 = automatic (left-looking for N <= 512), 1 = right-looking, 2 = FP32 with the
+// trailing updates on the tensor cores (lu_tc.cu; N <= 512), 3 = left-looking (N <= 512).
 template <typename T>
 cudaError_t bte_lu_factor_t(int P, int N, int NC, T* A, int ld, long long stride, int32_t* piv, int32_t* info,
                             cudaStream_t s, int kernel) {
@@ -540,6 +545,14 @@ cudaError_t bte_lu_factor_t(int P, int N, int NC, T* A, int ld, long long stride
     if (N < 1 || N > LU_MAX_N || NC < N || NC > N + 1 || ld < NC) return cudaErrorInvalidValue;
     // FP64: the right-looking kernel (the left-looking one serialises FP64 substitutions)
     if (sizeof(T) == 8 && kernel == 0) kernel = 1;
+    if (kernel == 2) {
+        if (sizeof(T) != 4 || N > bte_lu_tc_max_n()) return cudaErrorInvalidValue;
+        return bte_lu_factor_tc(P, N, NC, reinterpret_cast<float*>(A), ld, stride, piv, info, s);
+    }
+    if (kernel == 3) {
+        if (N > 512) return cudaErrorInvalidValue;
+        kernel = 0;
+    }
     if (kernel == 0 && N <= 128) return launch_left<T, 4>(P, N, NC, A, ld, stride, piv, info, s);
     if (kernel == 0 && N <= 256) return launch_left<T, 8>(P, N, NC, A, ld, stride, piv, info, s);
     if (kernel == 0 && N <= 384) return launch_left<T, 12>(P, N, NC, A, ld, stride, piv, info, s);

@@ -1563,6 +1563,13 @@ static cudaError_t gmres_refine(SolveCtx& c, Lane& L, int nact, bool all) {
     return cudaGetLastError();
 }
 
+// FP32 factorization kernel for a Newton system of size N (bte_solve_opts.lu_kernel): a
+// kernel that does not take N falls back to the library's choice
+static int lu_kernel_for(int requested, int N) {
+    if ((requested == 2 || requested == 3) && N > 512) return 0;
+    return (requested >= 0 && requested <= 3) ? requested : 0;
+}
+
 // One Newton iteration (Jacobian, factorization, step, refinement, line search, acceptance,
 // convergence test) for the `nact` points of lane L whose F, aux, scal and r are current;
 // returns the points still running, whose list is then L.act (the list before the
@@ -1602,7 +1609,8 @@ static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
                                                                  jm.stage, 1.0, 0.0, L.kc);
             }));
             CKR(pf.run(PF_LU, s, nact * lu_flops(N), lub, 1, [&] {
-                le = bte_lu_factor_t<float>(nact, N, N + 1, (float*)L.J, ld, jstride, L.piv, L.info, s, 0);
+                le = bte_lu_factor_t<float>(nact, N, N + 1, (float*)L.J, ld, jstride, L.piv, L.info, s,
+                                            lu_kernel_for(o->lu_kernel, N));
             }));
             CKR(le);
             CKR(pf.run(PF_LUSOLVE, s, nact * (double)N * N, lsb, 1, [&] {

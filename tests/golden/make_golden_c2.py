@@ -1,0 +1,112 @@
+"""Golden EDFs at the benchmarked shapes, from the reference itself (CPU path).
+
+Runs only where the reference checkout is available (imported through
+`oracle/reference_import.py`); the GPU host never runs this script. It writes:
+
+  c2_shape_reference.npz   128 B-splines, l_max 2 (n = 384, the batched workload's grid),
+                           e-e on, 8 points. Three of them sit at E/N < 10 Td with an
+                           ionization degree above 1e-4, where the Coulomb term dominates.
+  c5_reduced_reference.npz 64 B-splines, l_max 4 (n = 320, the large workload's angular
+                           resolution on a coarser radial grid), e-e on, 4 points with
+                           ionization degrees in [1e-6, 1e-2].
+
+Each solve follows the reference driver (`BESolver/python/bte_0d3v_batched_driver.py:192-204`):
+Maxwellian -> e-e-off solve -> e-e-on solve from that result, with atol 1e-20, rtol 1e-14,
+100 iterations, alpha_rho 0.5, c 1e-4. Besides the EDFs and QoIs, the fixture records each
+point's final residual norm of the e-e-on phase and its ratio to the phase's initial norm,
+evaluated with the reference's own `get_rhs_and_jacobian` residual
+(`BESolver/python/bte_0d3v_batched.py:602-821`) at the state the solve stopped at, so a test
+can tell a converged point from one where the reference stopped at its line-search break
+(`:947-956`).
+
+Usage:  python tests/golden/make_golden_c2.py [c2|c5]   (both when no argument is given)
+"""
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, HERE)
+
+from boltzmann_gb300.workloads import write_synthetic_lxcat, N0_1TORR_300K, TD  # noqa: E402
+from oracle.reference_import import import_reference  # noqa: E402
+import make_golden as G  # noqa: E402
+
+# (E/N in Td, ionization degree): the first three are the low-field, strongly ionized points.
+C2_POINTS = [(1.5, 5e-4), (3.0, 2e-4), (7.0, 8e-4), (2.0, 1e-7), (30.0, 1e-5), (100.0, 1e-3),
+             (400.0, 1e-6), (950.0, 3e-4)]
+C5_POINTS = [(1.2, 8e-3), (20.0, 1e-6), (150.0, 1e-4), (700.0, 1e-2)]
+
+
+def _state_of(s, ff):
+    """The solver's unknown h for a normalized EDF: rescaled so that u.h = 1 (the constraint
+    the reference's Newton iterates satisfy, bte_0d3v_batched.py:907-917)."""
+    import utils as bte_utils
+    vth = s._par_vth[0]
+    mw = bte_utils.get_maxwellian_3d(vth, 1)
+    qA = s._op_diag_dg[0]
+    u = np.dot(np.transpose(s._op_mass[0] * mw(0) * vth ** 3), qA)
+    h = np.dot(qA.T, ff / np.dot(u, ff))
+    return h, u
+
+
+def _initial_state(s, f0):
+    """h_prev of steady_state_solve's first iteration (bte_0d3v_batched.py:907-917)."""
+    h, u = _state_of(s, f0)
+    f1 = u / np.dot(u, u)
+    return f1[:, None] + np.dot(s._op_qmat[0], np.dot(s._op_rmat[0], h))
+
+
+def run(m, xs, name, n_sp, l_max, points):
+    P = len(points)
+    t0 = time.time()
+    s, args = G.make_solver(m, xs, n_sp, l_max, True, P)
+    t_setup = time.time() - t0
+    ebyn = np.array([p[0] for p in points])
+    ion = np.array([p[1] for p in points])
+    n0 = np.full(P, N0_1TORR_300K)
+    prm = dict(n0=n0, ne=ion * n0, Tg=np.full(P, 300.0), E=ebyn * n0 * TD, ns_by_n0=np.ones((1, P)))
+    f0 = s.initialize(0, P, "maxwellian")
+    G.set_params(s, prm)
+    args.ee_collisions = 0
+    t1 = time.time()
+    ffw, _ = s.solve(0, f0, G.ATOL, G.RTOL, G.MAXIT, "steady-state", alpha_min=1e-16, alpha_rho=0.5,
+                     line_search_c=1e-4)
+    args.ee_collisions = 1
+    t2 = time.time()
+    ff, qoi = s.solve(0, ffw, G.ATOL, G.RTOL, G.MAXIT, "steady-state", alpha_min=1e-16, alpha_rho=0.5,
+                      line_search_c=1e-4)
+    t3 = time.time()
+    res_func, _ = s.get_rhs_and_jacobian(0, P)
+    r0 = np.linalg.norm(res_func(_initial_state(s, ffw), 0, 0), axis=0)
+    hf, _ = _state_of(s, ff)
+    r1 = np.linalg.norm(res_func(hf, 0, 0), axis=0)
+    out = dict(n_sp=n_sp, l_max=l_max, EbyN=ebyn, ion_deg=ion, f0=f0, ff_warm=ffw, ff=ff,
+               energy=qoi["energy"], mobility=qoi["mobility"], diffusion=qoi["diffusion"], rates=qoi["rates"],
+               abs_error=r1, rel_error=r1 / r0, setup_s=t_setup, solve_s=np.array([t2 - t1, t3 - t2]), **prm)
+    np.savez_compressed(os.path.join(HERE, name), **out)
+    print("wrote %s: setup %.0f s, solves %.0f s + %.0f s, rel_error %s" %
+          (name, t_setup, t2 - t1, t3 - t2, np.array2string(r1 / r0, precision=2)), flush=True)
+
+
+def main():
+    which = sys.argv[1:] or ["c2", "c5"]
+    xs = write_synthetic_lxcat(os.path.join("/tmp", "eAr_golden_%d.lxcat" % os.getpid()))
+    cwd = os.getcwd()
+    m = import_reference()
+    try:
+        if "c2" in which:
+            run(m, xs, "c2_shape_reference.npz", 128, 2, C2_POINTS)
+        if "c5" in which:
+            run(m, xs, "c5_reduced_reference.npz", 64, 4, C5_POINTS)
+    finally:
+        os.chdir(cwd)
+        os.unlink(xs)
+
+
+if __name__ == "__main__":
+    main()

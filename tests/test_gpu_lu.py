@@ -9,8 +9,10 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("N", [1, 7, 31, 64, 129, 385, 600, 1281])
 @pytest.mark.parametrize("dtype", ["f64", "f32"])
-@pytest.mark.parametrize("kernel", [0, 1], ids=["auto", "right"])
+@pytest.mark.parametrize("kernel", [0, 1, 2], ids=["auto", "right", "tc"])
 def test_lu_factor_solve(N, dtype, kernel):
+    if kernel == 2 and (dtype == "f64" or N > 512):
+        pytest.skip("the tensor-core factorization is FP32 with N <= 512")
     import torch
     from boltzmann_gb300 import _lib
     lib = _lib.load()
@@ -92,3 +94,39 @@ def test_lu_negative_zero_is_not_a_pivot(dtype, N):
     assert np.all(info.cpu().numpy() == 0)
     assert np.array_equal(piv.cpu().numpy(), np.broadcast_to(np.arange(N), (P, N)))
     assert torch.equal(x, b)
+
+
+@pytest.mark.parametrize("N", [33, 128, 385, 512])
+@pytest.mark.parametrize("kernel", [0, 2], ids=["auto", "tc"])
+def test_lu_padded_rows_against_fp64(N, kernel):
+    """FP32 factors with 16-byte aligned rows (the Newton solver's layout, vectorised path of
+    the tensor-core kernel): backward error at FP32 level, and the tensor-core factors'
+    solution as accurate as the SIMT kernel's (the split-TF32 products keep FP32 accuracy)."""
+    import torch
+    from boltzmann_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(1000 + N)
+    P, ld = 7, (N + 3) & ~3
+    A = rng.standard_normal((P, N, N)) + np.eye(N) * 0.5
+    b = rng.standard_normal((P, N))
+    Ap = np.zeros((P, N, ld), dtype=np.float32)
+    Ap[:, :, :N] = A
+    dA = torch.as_tensor(Ap, device="cuda").contiguous()
+    db = torch.as_tensor(b, dtype=torch.float32, device="cuda").contiguous()
+    piv = torch.empty((P, N), dtype=torch.int32, device="cuda")
+    info = torch.empty(P, dtype=torch.int32, device="cuda")
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.check(lib.bte_lu_factor_ex(1, P, N, C.c_void_p(dA.data_ptr()), ld, N * ld, C.c_void_p(piv.data_ptr()),
+                                    C.c_void_p(info.data_ptr()), kernel, st), "lu_factor")
+    _lib.check(lib.bte_lu_solve(1, P, N, C.c_void_p(dA.data_ptr()), ld, N * ld, C.c_void_p(piv.data_ptr()),
+                                C.c_void_p(db.data_ptr()), st), "lu_solve")
+    torch.cuda.synchronize()
+    assert np.all(info.cpu().numpy() == 0)
+    x = db.cpu().numpy().astype(np.float64)
+    Ad = A.astype(np.float32).astype(np.float64)
+    bd = b.astype(np.float32).astype(np.float64)
+    res = np.einsum("pij,pj->pi", Ad, x) - bd
+    berr = np.linalg.norm(res, axis=1) / (np.linalg.norm(Ad, ord=2, axis=(1, 2)) * np.linalg.norm(x, axis=1)
+                                           + np.linalg.norm(bd, axis=1))
+    eps = np.finfo(np.float32).eps
+    assert np.max(berr) < 2 * N * eps, (berr, N * eps)

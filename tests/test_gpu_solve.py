@@ -64,16 +64,19 @@ def test_batched_ee(synthetic_xs, precision, tol):
     s, args = gpu_solver(synthetic_xs, n_sp, l_max, True, P, precision)
     o = oracle_ops(synthetic_xs, n_sp, l_max, True)
     prm = params_for(True, P)
-    # keep the points the oracle itself converges on this coarse grid (E/N >= 10 Td)
-    keep = prm["EbyN"] >= 10.0
-    prm = {k: (v[..., keep] if np.ndim(v) else v) for k, v in prm.items()}
-    P = int(keep.sum())
     ff_r, q_r, info = oracle_solution(o, prm, True, P)
-    ok = info["rel_error"] < 1e-11
     ff, q = gpu_solution(s, args, prm, True, P)
     assert np.all(q["status"] <= 1), q["status"]
     err = rel_l2_cols(ff, ff_r)
-    assert np.max(err[ok]) < tol, err
+    # every point is compared: where the oracle (like the reference, whose batch-global loop
+    # it follows) stops above 1e-12 of its initial residual, the tolerance is scaled by the
+    # residual it stopped at, and the GPU must reach a residual at least as small
+    rel = np.asarray(info["rel_error"])
+    ok = rel <= 1e-12
+    assert np.all(err[ok] < tol), (err, rel)
+    if precision == "fp64":
+        assert np.all(np.asarray(q["rel_error"])[~ok] <= rel[~ok]), (q["rel_error"], rel)
+    assert np.all(err[~ok] < tol * rel[~ok] / 1e-12), (err, rel)
 
 
 def test_mixed_matches_fp64(synthetic_xs):
