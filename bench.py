@@ -47,14 +47,18 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=1, help="timed steps of the plain FP64 form")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-points", type=int, default=2)
-    ap.add_argument("--serve-requests", type=int, default=12,
-                    help="requests of the serving mix (Poisson arrivals, 1-512 points, 15 grid sizes)")
+    ap.add_argument("--cpu-points", type=int, default=4, help="points per CPU reference sample solve")
+    ap.add_argument("--cpu-slice-s", type=float, default=8.0, help="seconds of CPU work per reference-arm step")
+    ap.add_argument("--serve-requests", type=int, default=32,
+                    help="requests of the serving mix (Poisson arrivals, 1-512 points, 15 grid sizes); the "
+                         "first requests of the 2000-request stream")
+    ap.add_argument("--serve-loads", default="0.5,0.8,1.0",
+                    help="Poisson offered loads of the lambda sweep, as fractions of the plain FP64 capacity")
     ap.add_argument("--serve-budget-gb", type=float, default=16.0, help="HBM budget of admitted points")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-1d", action="store_true", help="skip the 1D3V (config 4) leg")
-    ap.add_argument("--c5-points", type=int, default=256, help="points of the config-5 sample (0: skip)")
-    ap.add_argument("--c5-plain-points", type=int, default=256,
+    ap.add_argument("--c5-points", type=int, default=2048, help="points of the config-5 sample (0: skip)")
+    ap.add_argument("--c5-plain-points", type=int, default=2048,
                     help="points of the plain FP64 run of the config-5 sample (the same points, for a fair ratio)")
     ap.add_argument("--steps-1d", type=int, default=20)
     ap.add_argument("--lu-kernel", type=int, default=0,
@@ -314,14 +318,26 @@ def serve_bench(a):
             sat[prec] = summ
             torch.cuda.empty_cache()
         cap_fp64 = sat["fp64"]["solves_per_s"]
-        rate = 0.8 * cap_fp64 / (pts / len(specs))  # requests per second
-        specs_p = serving_requests(a.serve_requests, rate)
-        pois, res = {}, {}
-        for prec in ("mixed", "fp64"):
-            summ, reqs = _serve_run(xs, specs_p, prec, a, rate=rate)
-            pois[prec] = summ
-            res[prec] = reqs
-            torch.cuda.empty_cache()
+        # lambda sweep: Poisson arrivals at fractions of the plain FP64 capacity, both forms;
+        # the 0.8 point is the one the error comparison uses
+        loads = [float(x) for x in a.serve_loads.split(",") if x.strip()]
+        if 0.8 not in loads:
+            loads.append(0.8)
+        sweep, res = [], {}
+        for load in loads:
+            rate = load * cap_fp64 / (pts / len(specs))  # requests per second
+            specs_p = serving_requests(a.serve_requests, rate)
+            row = {"offered_load_of_fp64_capacity": load, "rate_requests_per_s": rate,
+                   "offered_solves_per_s": load * cap_fp64}
+            for prec in ("mixed", "fp64"):
+                summ, reqs = _serve_run(xs, specs_p, prec, a, rate=rate)
+                row[prec] = summ
+                if load == 0.8:
+                    res[prec] = reqs
+                torch.cuda.empty_cache()
+            sweep.append(row)
+        pois = next(r for r in sweep if r["offered_load_of_fp64_capacity"] == 0.8)
+        rate = pois["rate_requests_per_s"]
         # per-point EDF difference over points both forms converged (status 0 or 1)
         err, n_unconv = [], 0
         for m, p in zip(res["mixed"], res["fp64"]):
@@ -332,14 +348,17 @@ def serve_bench(a):
     finally:
         os.unlink(xs)
     return {
-        "workload": "%d requests (1-512 points, N_sp in {64,96,128,192,256} x l_max in {1,2,3}, E/N log-uniform "
-                    "[1,1000] Td, ionization degree log-uniform [1e-8,1e-3], e-e warm start then e-e on), seed 20261204; "
-                    "%d points" % (len(specs), pts),
+        "workload": "the first %d requests of the seeded 2000-request stream (1-512 points, N_sp in "
+                    "{64,96,128,192,256} x l_max in {1,2,3}, E/N log-uniform [1,1000] Td, ionization degree log-uniform "
+                    "[1e-8,1e-3], e-e warm start then e-e on), seed 20261204; %d points" % (len(specs), pts),
         "hbm_budget_gb": a.serve_budget_gb,
         "saturation": {"mixed": sat["mixed"], "fp64": sat["fp64"],
                        "mixed_over_fp64": sat["mixed"]["solves_per_s"] / cap_fp64},
         "poisson": {"rate_requests_per_s": rate, "offered_solves_per_s": 0.8 * cap_fp64,
                     "mixed": pois["mixed"], "fp64": pois["fp64"]},
+        "lambda_sweep": [{"load": r["offered_load_of_fp64_capacity"], "rate_requests_per_s": r["rate_requests_per_s"],
+                          "mixed": {k: r["mixed"][k] for k in ("p50_ms", "p99_ms", "solves_per_s")},
+                          "fp64": {k: r["fp64"][k] for k in ("p50_ms", "p99_ms", "solves_per_s")}} for r in sweep],
         "edf_rel_err_mixed_vs_fp64": {"max": float(err.max()), "p50": float(np.median(err)),
                                       "p99": float(np.percentile(err, 99)), "points_above_1e-8": int(np.sum(err > 1e-8)),
                                       "points_compared": int(err.size), "points_unconverged_in_either": n_unconv},
@@ -503,59 +522,151 @@ def bench_1d(a, peaks):
     return out
 
 
+# the pipe each kernel family runs on: roofline denominators from MEASURED_PEAKS.json
+# (HBM copy GB/s, dense bf16 TFLOP/s). The FP32 factorization runs its trailing updates as
+# tcgen05 kind::tf32 MMAs, whose dense rate is half the bf16 rate; FP64 families run on the
+# FP64 pipe, for which no measured peak exists (nominal 1.25 TFLOP/s on GB300).
+FAMILY_PIPE = {"lu_factor": "tensor_tf32", "lu_factor_fp64": "fp64", "jacobian": "fp64", "refine": "fp64",
+               "residual": "fp64", "lu_solve": "hbm", "other": "hbm"}
+FP64_NOMINAL_TFLOPS = 1.25
+
+
+def family_roofline(name, v, peaks):
+    """Roofline of one kernel family: algorithmic flops and bytes per launch over its average
+    launch time (CUDA events), bound by arithmetic intensity against the ridge point."""
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    bf16 = peaks.get("bf16_tflops") or 1900.0
+    pipe = FAMILY_PIPE.get(name, "hbm")
+    n = max(v["launches"], 1)
+    t = v["ms"] / 1e3 / n
+    fl, by = v["flops"] / n, v["bytes"] / n
+    gbs = by / t / 1e9 if t > 0 else 0.0
+    tfs = fl / t / 1e12 if t > 0 else 0.0
+    ai = fl / by if by > 0 else float("inf")
+    if pipe == "tensor_tf32":
+        pk, src = bf16 / 2, "MEASURED_PEAKS.json bf16_tflops / 2 (dense TF32 rate, of measured)"
+    elif pipe == "fp64":
+        pk, src = FP64_NOMINAL_TFLOPS, "nominal GB300 FP64 1.25 TFLOP/s (no measured FP64 peak)"
+    else:
+        pk, src = None, None
+    ridge = pk * 1e12 / (hbm * 1e9) if pk else float("inf")
+    both = {"frac_hbm": gbs / hbm, "frac_pipe": (tfs / pk) if pk else None}
+    if pk and ai >= ridge:
+        return {"kernel": name, "bound": "tensor" if pipe == "tensor_tf32" else "fp64", "achieved": tfs, "peak": pk,
+                "unit": "TFLOP/s", "frac": tfs / pk, "peak_source": src, "arith_intensity": ai, "ridge": ridge,
+                "hbm_gbs_achieved": gbs, "avg_launch_ms": t * 1e3, "alg_flops_per_launch": fl,
+                "alg_bytes_per_launch": by, **both}
+    return {"kernel": name, "bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks.get("hbm_gbs") else "fallback",
+            "arith_intensity": ai, "ridge": ridge, "tflops_achieved": tfs, "avg_launch_ms": t * 1e3,
+            "alg_flops_per_launch": fl, "alg_bytes_per_launch": by, "pipe_peak": pk, "pipe_peak_source": src, **both}
+
+
 def roofline(st, peaks):
-    fams = {k: v for k, v in st.items() if isinstance(v, dict) and "ms" in v}
+    """The dominant kernel family's roofline (the `roofline` object), with every family's
+    beside it. `traffic` is DRAM read + write per launch of the dominant family from the ncu
+    capture summarized in profiles/ (its DRAM bytes per algorithmic byte, scaled to this run's
+    average launch)."""
+    fams = {k: v for k, v in st.items() if isinstance(v, dict) and "ms" in v and v["launches"] > 0}
     dom = max(fams, key=lambda k: fams[k]["ms"])
-    v = fams[dom]
-    hbm = peaks.get("hbm_gbs")
-    per_launch_s = v["ms"] / 1e3 / max(v["launches"], 1)
-    bytes_pl = v["bytes"] / max(v["launches"], 1)
-    flops_pl = v["flops"] / max(v["launches"], 1)
-    achieved = bytes_pl / per_launch_s / 1e9
-    # DRAM traffic of one launch of the dominant family, from the ncu capture summarized in
-    # profiles/: its bytes per algorithmic byte, scaled to this run's average launch
+    out = family_roofline(dom, fams[dom], peaks)
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
         rec = json.load(open(tpath)).get(dom)
         if rec and rec.get("alg_bytes_per_launch"):
-            traffic = rec["dram_bytes_per_launch"] / rec["alg_bytes_per_launch"] * bytes_pl
-    return {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-            "frac": achieved / hbm if hbm else None, "traffic": traffic,
-            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if hbm else "fallback 6800 GB/s",
-            "alg_bytes_per_launch": bytes_pl, "avg_launch_ms": per_launch_s * 1e3,
-            "tflops_achieved": flops_pl / per_launch_s / 1e12,
-            "families_ms": {k: round(f["ms"], 3) for k, f in fams.items()}}
+            traffic = rec["dram_bytes_per_launch"] / rec["alg_bytes_per_launch"] * out["alg_bytes_per_launch"]
+    out["traffic"] = traffic
+    out["families"] = {k: {kk: (round(vv, 6) if isinstance(vv, float) else vv)
+                           for kk, vv in family_roofline(k, f, peaks).items()
+                           if kk in ("bound", "achieved", "unit", "frac", "avg_launch_ms")} for k, f in fams.items()}
+    out["families_ms"] = {k: round(f["ms"], 3) for k, f in fams.items()}
+    return out
 
 
-def cpu_sample(a, n_pts, iters_per_phase=3):
-    """Time the oracle (the reference's algorithm restated in NumPy) on a bounded sample of the
-    same workload: n_pts points, `iters_per_phase` Newton iterations of each phase, extrapolated
-    to the reference's budget of max_iter = 100 iterations per phase (its batch-global loop runs
-    to the cap on this workload)."""
-    import multiprocessing
-    from oracle import bte_oracle as O
-    from boltzmann_gb300.workloads import write_synthetic_lxcat, batch_parameters, EV_MAX, TE_NORM
-    xs = write_synthetic_lxcat()
+class CpuReferenceRun:
+    """The reference's CPU algorithm on the host cores: the oracle port of the reference's
+    bte_0d3v_batched (NumPy/OpenBLAS, all host threads) solving consecutive samples of
+    `n_pts` points of the same seeded workload, each to the reference's own stop criterion
+    (e-e-off solve from the Maxwellian, then the e-e-on solve from its result, batch-global
+    loop up to max_iter = 100 or the line-search break). The solves advance in bounded time
+    slices (whole Newton iterations), so a benchmark step is bounded while every sample still
+    runs to the end; throughput = points of completed samples / seconds spent on them. The
+    operator set-up (assembly, dense Coulomb tensor) is not timed."""
+
+    def __init__(self, a, n_pts):
+        import multiprocessing
+        from oracle import bte_oracle as O
+        from boltzmann_gb300.workloads import write_synthetic_lxcat, EV_MAX, TE_NORM
+        self.O, self.a, self.n_pts = O, a, n_pts
+        self.cores = multiprocessing.cpu_count()
+        xs = write_synthetic_lxcat()
+        t0 = time.perf_counter()
+        try:
+            self.ops = O.Operators(O.processes_from_lxcat(xs), EV_MAX, TE_NORM, a.n_sp, a.l_max, ee=True)
+        finally:
+            os.unlink(xs)
+        self.setup_s = time.perf_counter() - t0
+        self.done = []
+        self.k = 0
+        self._start()
+
+    def _start(self):
+        from boltzmann_gb300.workloads import batch_parameters
+        O = self.O
+        prm = batch_parameters(self.a.n_pts, self.a.seed)
+        sl = slice(self.k * self.n_pts, (self.k + 1) * self.n_pts)
+        P = O.Params(prm["n0"][sl], prm["ne"][sl], prm["Tg"][sl], prm["E"][sl], prm["ns_by_n0"][:, sl])
+        self.gen = self._solve(P)
+        self.spent = 0.0
+
+    def _solve(self, P):
+        O = self.O
+        f0 = O.maxwellian_initial(self.ops, self.n_pts)
+        ff, _, i1 = yield from O.steady_state_iterations(self.ops, P, f0, ATOL, RTOL, MAXIT, False, ALPHA_MIN,
+                                                         ALPHA_RHO, LS_C)
+        _, _, i2 = yield from O.steady_state_iterations(self.ops, P, ff, ATOL, RTOL, MAXIT, True, ALPHA_MIN,
+                                                        ALPHA_RHO, LS_C)
+        return i1, i2
+
+    def run_slice(self, budget_s):
+        """Newton iterations of the current sample (and the next ones) for about budget_s."""
+        t0 = time.perf_counter()
+        while True:
+            t1 = time.perf_counter()
+            try:
+                next(self.gen)
+                self.spent += time.perf_counter() - t1
+            except StopIteration as stop:
+                self.spent += time.perf_counter() - t1
+                i1, i2 = stop.value
+                self.done.append({"points": self.n_pts, "seconds": self.spent, "iters": [i1["iters"], i2["iters"]],
+                                  "stop": [i1["status"], i2["status"]]})
+                self.k += 1
+                self._start()
+            if time.perf_counter() - t0 >= budget_s:
+                return
+
+    def summary(self):
+        pts = sum(d["points"] for d in self.done)
+        sec = sum(d["seconds"] for d in self.done)
+        return {"value": pts / sec if sec > 0 else None, "unit": UNIT, "cores": self.cores, "kind": "port",
+                "sample": "%d completed sample(s) of %d consecutive points of the seeded c2 workload, each solved to "
+                          "the reference's stop criterion (e-e off then e-e on, batch-global loop); Newton iterations "
+                          "per sample %s, stop %s; oracle port of bte_0d3v_batched (NumPy, OpenBLAS on all %d host "
+                          "threads); operator set-up %.1f s not timed"
+                          % (len(self.done), self.n_pts, [d["iters"] for d in self.done],
+                             [d["stop"] for d in self.done], self.cores, self.setup_s),
+                "seconds": sec, "samples": self.done}
+
+
+def cpu_baseline_run(a, cap_s=600.0):
+    """cpu_baseline of the GPU arm: the CPU reference run until its first sample completes."""
+    run = CpuReferenceRun(a, a.cpu_points)
     t0 = time.perf_counter()
-    ops = O.Operators(O.processes_from_lxcat(xs), EV_MAX, TE_NORM, a.n_sp, a.l_max, ee=True)
-    t_setup = time.perf_counter() - t0
-    prm = batch_parameters(n_pts, a.seed)
-    P = O.Params(prm["n0"], prm["ne"], prm["Tg"], prm["E"], prm["ns_by_n0"])
-    f0 = O.maxwellian_initial(ops, n_pts)
-    t0 = time.perf_counter()
-    O.steady_state_solve(ops, P, f0, ATOL, RTOL, iters_per_phase, False, ALPHA_MIN, ALPHA_RHO, LS_C)
-    t_off = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    O.steady_state_solve(ops, P, f0, ATOL, RTOL, iters_per_phase, True, ALPHA_MIN, ALPHA_RHO, LS_C)
-    t_on = time.perf_counter() - t0
-    os.unlink(xs)
-    per_point = (t_off + t_on) / iters_per_phase * MAXIT / n_pts
-    return {"value": 1.0 / per_point, "unit": UNIT, "cores": multiprocessing.cpu_count(), "kind": "port",
-            "sample": "%d points x %d Newton iterations per phase (e-e off, e-e on) of the same workload, "
-                      "extrapolated to %d iterations per phase; NumPy/OpenBLAS threads = all host cores; "
-                      "oracle setup %.1f s not counted" % (n_pts, iters_per_phase, MAXIT, t_setup),
-            "seconds": t_off + t_on}
+    while not run.done and time.perf_counter() - t0 < cap_s:
+        run.run_slice(5.0)
+    return run.summary()
 
 
 def main():
@@ -568,17 +679,28 @@ def main():
     if a.impl == "reference":
         if rank != 0:
             return
-        steps = []
+        # the reference's CPU algorithm: each step a bounded slice of consecutive sample solves,
+        # each sample run to the reference's stop criterion (no extrapolation of iterations)
+        run = CpuReferenceRun(a, a.cpu_points)
         for _ in range(a.warmup):
-            cpu_sample(a, a.cpu_points, 1)
+            run.run_slice(0.0)  # one Newton iteration each
+        t0 = time.perf_counter()
+        steps = 0
         for _ in range(a.steps):
-            steps.append(cpu_sample(a, a.cpu_points, 2))
-        v = float(np.median([s["value"] for s in steps]))
-        line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
-                "ms_per_step": 1e3 * a.n_pts / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f64", "data": "synthetic", "impl": "reference",
-                "config": workload_config(a, "fp64"),
-                "cpu_baseline": {**steps[-1], "value": v},
+            run.run_slice(a.cpu_slice_s)
+            steps += 1
+        while not run.done:  # the timed steps end only once a sample has completed
+            run.run_slice(a.cpu_slice_s)
+            steps += 1
+        elapsed = time.perf_counter() - t0
+        summ = run.summary()
+        v = summ["value"]
+        cfg = workload_config(a, "fp64")
+        cfg["sample_points_per_solve"] = a.cpu_points
+        line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": steps, "warmup": a.warmup,
+                "ms_per_step": 1e3 * elapsed / steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+                "config": cfg, "cpu_baseline": summ,
                 "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -588,7 +710,7 @@ def main():
     serve = None if (a.no_serve or ws > 1) else serve_bench(a)
     one_d = None if (a.no_1d or ws > 1) else bench_1d(a, peaks)
     c5 = None if (a.c5_points <= 0 or ws > 1) else bench_c5(a)
-    cpu = None if a.no_cpu else cpu_sample(a, a.cpu_points, 3)
+    cpu = None if a.no_cpu else cpu_baseline_run(a)
     st = r["stats"]
     steps_ms = sorted(r["steps_ms"])
     line = {

@@ -32,7 +32,7 @@ EXPORTED = ["bte_grid_create", "bte_grid_destroy", "bte_grid_info", "bte_grid_ex
             "bte_fvm_mvec", "bte_fvm_precond", "bte_fvm_step", "bte_fvm_launches", "bte_fvm_last_error",
             "bte_fvm_set_sl_grid", "bte_fvm_sl_advect", "bte_fvm_sl_step"]
 
-STAT_FAMILIES = ["residual", "jacobian", "lu_factor", "lu_solve", "refine", "other"]
+STAT_FAMILIES = ["residual", "jacobian", "lu_factor", "lu_solve", "refine", "other", "lu_factor_fp64"]
 
 
 class GridDesc(C.Structure):

@@ -29,6 +29,9 @@ import numpy as np
 
 from . import _lib
 from .bte_1d3v import ME, QE
+
+KB = 1.380649e-23
+EPS0 = 8.8541878188e-12
 from .lxcat import read_available_species, read_cross_section_data
 
 
@@ -343,6 +346,151 @@ class bte_0d3v_batched:
             _lib.check(lib.bte_lu_solve(0, P, m, _ptr(A), m, m * m, _ptr(piv), _ptr(b), stream), "bte_lu_solve")
             out[:, :, c] = b
         return out.cpu().numpy() if on_host else out
+
+    # ------------------------------------------------------------------ reference-form closures
+    def _projected_ops(self, grid_idx):
+        """The reference's M^-1-scaled operators (bte_0d3v_batched.py:415-424, 444-476) and its
+        constraint basis Q, R (:425-442), built once per grid from the device assembly. Q and R
+        come from a host QR of I - p p^T (numpy.linalg.qr, as the reference computes them) with
+        column (n_sp - 1) * num_sh dropped; the operator products are plain cuBLAS GEMMs."""
+        cache = self.__dict__.setdefault("_rj_cache", {})
+        if grid_idx in cache:
+            return cache[grid_idx]
+        torch = _torch()
+        info = self._grid_info[grid_idx]
+        if info is None:
+            raise RuntimeError("assemble_operators(%d) first" % grid_idx)
+        n, nsh, nsp, vth, mw0 = info["n"], info["num_sh"], info["n_sp"], info["vth"], info["mw0"]
+        Minv = self.export_operator(grid_idx, "MINV")
+        adv = (Minv @ self.export_operator(grid_idx, "ADV_RAW")) * (QE / ME / vth)
+        col_en = torch.stack([Minv @ c for c in self.export_operator(grid_idx, "COL_RAW")])
+        col_gT = Minv @ self.export_operator(grid_idx, "COL_GT_RAW")
+        mass = self.export_operator(grid_idx, "MASS_VEC")
+        temp = self.export_operator(grid_idx, "TEMP_VEC")
+        u = mass * (mw0 * vth ** 3)
+        un = u.cpu().numpy()
+        pv = un / np.sqrt(un @ un)
+        Qm, Rm = np.linalg.qr(np.eye(n) - np.outer(pv, pv))
+        drop = (nsp - 1) * nsh
+        Q = torch.as_tensor(np.delete(Qm, drop, axis=1), device="cuda")
+        R = torch.as_tensor(np.delete(Rm, drop, axis=0), device="cuda")
+        cc = None
+        if info["ee"]:
+            cc = (self.export_operator(grid_idx, "CC_A").reshape(n * n, n) @ self.export_operator(grid_idx, "HL")
+                  + self.export_operator(grid_idx, "CC_B").reshape(n * n, n) @ self.export_operator(grid_idx, "GL"))
+            cc = (Minv @ cc.reshape(n, n * n)).reshape(n, n, n)
+        QT = Q.t().contiguous()
+        ops = dict(n=n, vth=vth, mw0=mw0, Q=Q, R=R, QT=QT, u=u, mass=mass, temp=temp * (QE / KB), cc=cc,
+                   Wmat=torch.einsum("v,svu->su", u, col_en), QT_Cen=torch.einsum("mu,suv->smv", QT, col_en),
+                   QT_Cgt=QT @ col_gT, QT_A=QT @ adv, QT_Cen_Q=torch.einsum("av,svu->sau", QT, col_en @ Q),
+                   QT_Cgt_Q=QT @ (col_gT @ Q), QT_A_Q=QT @ (adv @ Q))
+        cache[grid_idx] = ops
+        return ops
+
+    def get_rhs_and_jacobian(self, grid_idx: int, n_pts: int):
+        """bte_0d3v_batched.py:602-821: closures res_func(x, time, dt) -> (m, n_pts) and
+        jac_func(x, time, dt) -> (n_pts, m, m), the reference's residual and Jacobian projected
+        on its constraint basis Q (m = n - 1), for a caller that drives its own Newton loop (as
+        `step` does). They read the grid's parameters (set_boltzmann_parameter) at each call
+        and args.ee_collisions when created, as the reference's closures do; the Jacobian
+        treats the Coulomb logarithm as constant, as the reference's. x is (n, n_pts); the
+        result is a NumPy array for NumPy input and a CUDA tensor for tensor input. The
+        contractions are cuBLAS GEMMs on device-resident operators; the library's own solves
+        do not use these closures."""
+        torch = _torch()
+        o = self._projected_ops(grid_idx)
+        ee = int(getattr(self._args, "ee_collisions", 0)) == 1
+        if ee and o["cc"] is None:
+            raise RuntimeError("grid %d was assembled without the e-e operator" % grid_idx)
+        vth, mw0 = o["vth"], o["mw0"]
+        Mop, Top = o["mass"].reshape(1, -1), o["temp"].reshape(1, -1)
+        QT, Q = o["QT"], o["Q"]
+        m = Q.shape[1]
+
+        def prm():
+            n0, ne, Tg, E, ns = self._params(grid_idx, n_pts)
+            return n0, ne, Tg, E, ns
+
+        def gamma_a(x, ne):
+            m0 = mw0 * (Mop @ x) * vth ** 3
+            kT = (mw0 * ((Top @ x) / m0) * vth ** 5 * KB).abs().reshape(-1)
+            c_lambda = (12 * np.pi * (EPS0 * kT) ** 1.5) / (QE ** 3 * torch.sqrt(ne))
+            return (torch.log(c_lambda) * QE ** 4) / (4 * np.pi * (EPS0 * ME) ** 2) / vth ** 3
+
+        def wrap(fn):
+            def call(x, time, dt):
+                on_host = not torch.is_tensor(x)
+                y = fn(self._dev(x))
+                return y.cpu().numpy() if on_host else y
+            return call
+
+        def res_func(x):
+            n0, ne, Tg, E, ns = prm()
+            y = (n0 * (torch.einsum("sx,svx->vx", ns, torch.matmul(o["QT_Cen"], x)) + Tg * (o["QT_Cgt"] @ x))
+                 + E * (o["QT_A"] @ x) - n0 * torch.einsum("sx,sx->x", ns, o["Wmat"] @ x) * (QT @ x))
+            if ee:
+                c_ee_x = torch.matmul(o["cc"], x)                  # (n, n, P)
+                c_ee_xx = torch.einsum("abc,bc->ac", c_ee_x, x)
+                y = y + ne * gamma_a(x, ne) * (QT @ c_ee_xx)
+            return y
+
+        def jac_func(x):
+            n0, ne, Tg, E, ns = prm()
+            nsx = n0 * ns
+            L = torch.einsum("sx,svu->xvu", nsx, o["QT_Cen_Q"]) + torch.einsum("a,bc->abc", n0 * Tg, o["QT_Cgt_Q"])
+            mu = torch.einsum("sx,sx->x", nsx, o["Wmat"] @ x)
+            L = L + torch.einsum("a,bc->abc", E, o["QT_A_Q"]) - mu[:, None, None] * torch.eye(m, dtype=x.dtype,
+                                                                                              device=x.device)
+            if ee:
+                cc = torch.matmul(o["cc"], x) + torch.matmul(o["cc"].transpose(1, 2), x)   # (n, n, P)
+                cc = cc.permute(2, 0, 1)                                                  # (P, n, n)
+                QTccQ = torch.matmul(torch.matmul(QT, cc), Q)
+                L = L + (ne * gamma_a(x, ne))[:, None, None] * QTccQ
+            return L
+
+        return wrap(res_func), wrap(jac_func)
+
+    def step(self, grid_idx: int, f0, atol, rtol, max_iter, time, delta_t):
+        """bte_0d3v_batched.py:981-1032: one backward-Euler step of the transient solve from u =
+        f0 (not renormalized) at the grid's current parameters: du - delta_t rhs(u + Q du) = 0
+        by the reference's chord iteration (newton_solver_batched, :59-126; Jacobian
+        I - delta_t rhs_u(u) factored once by the library's batched LU, no line search).
+        Returns v = u + Q du in the array type of f0. A step that does not converge raises
+        RuntimeError where the reference exits."""
+        torch = _torch()
+        on_host = not torch.is_tensor(f0)
+        prof = self.profile_tt_all[grid_idx]
+        prof[pp.SOLVE].start()
+        u = self._dev(f0)
+        P = u.shape[1]
+        rhs, rhs_u = self.get_rhs_and_jacobian(grid_idx, P)
+        Q = self._projected_ops(grid_idx)["Q"]
+        m = Q.shape[1]
+        dt = float(delta_t)
+        J = torch.eye(m, dtype=torch.float64, device="cuda").expand(P, m, m) - dt * rhs_u(u, time, dt)
+        Jinv = self.batched_inv(grid_idx, J)
+
+        def residual(du):
+            return du - dt * rhs(u + Q @ du, time + dt, dt)
+
+        x = torch.zeros((m, P), dtype=torch.float64, device="cuda")
+        norm_r0 = torch.linalg.norm(residual(x), dim=0)
+        norm_rr = norm_r0
+        count = 0
+        converged = bool(((norm_rr / norm_r0) < rtol).all() or (norm_rr < atol).all())
+        while not converged and count < max_iter:
+            rr = residual(x)
+            norm_rr = torch.linalg.norm(rr, dim=0)
+            converged = bool(((norm_rr / norm_r0) < rtol).all() or (norm_rr < atol).all())
+            x = x + torch.einsum("ijk,ki->ji", Jinv, -rr)
+            count += 1
+        prof[pp.SOLVE].stop()
+        if not converged:
+            raise RuntimeError("step at time %.3e did not converge in %d iterations: max ||res|| = %.3e, max "
+                               "||res||/||res0|| = %.3e" % (time, count, float(norm_rr.max()),
+                                                            float((norm_rr / norm_r0).max())))
+        v = u + Q @ x
+        return v.cpu().numpy() if on_host else v
 
     # ------------------------------------------------------------------ helpers
     def _dev(self, v, shape=None):

@@ -271,9 +271,24 @@ struct Bte1d {
     long long launches = 0;
 };
 
-static std::string g_err1d;
+static thread_local std::string g_err1d;
 
 #define CK1(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) { g_err1d = std::string(#x) + ": " + cudaGetErrorString(_e); return BTE_ERR_CUDA; } } while (0)
+
+// after the per-point FP32 block factorization: a zero pivot in any block is an error (its
+// substitution would spread Inf/NaN into the step while GMRES could still report convergence)
+static int check_blocks(Bte1d* h, cudaStream_t s) {
+    std::vector<int32_t> info((size_t)h->Nx);
+    CK1(cudaMemcpyAsync(info.data(), h->Vinfo, info.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    CK1(cudaStreamSynchronize(s));
+    for (int x = 0; x < h->Nx; ++x)
+        if (info[(size_t)x] != 0) {
+            g_err1d = "singular v-space block at x point " + std::to_string(x) + " (zero pivot " +
+                      std::to_string(info[(size_t)x]) + ")";
+            return BTE_ERR_STATE;
+        }
+    return BTE_OK;
+}
 
 static int alloc1d(Bte1d* h, void** p, size_t bytes) {
     if (cudaMalloc(p, std::max<size_t>(bytes, 8)) != cudaSuccess) { g_err1d = "device allocation failed"; return BTE_ERR_ALLOC; }
@@ -448,6 +463,7 @@ int bte1d_step_v(Bte1d* h, double dt, const double* E, double* V, double rtol, d
     CK1(cudaGetLastError());
     CK1(bte_lu_factor_t<float>(Nx, n, n, h->VB, h->vld, vs, h->Vpiv, h->Vinfo, s, 0));
     L += 3;
+    if (int rc = check_blocks(h, s)) return rc;
     double bnorm = 0.0;
     CK1(dots(1, h->U, h->U, &bnorm));
     bnorm = std::sqrt(bnorm);
@@ -509,7 +525,7 @@ int bte1d_step_v(Bte1d* h, double dt, const double* E, double* V, double rtol, d
         for (int i = k - 1; i >= 0; --i) {
             double acc = g[i];
             for (int j = i + 1; j < k; ++j) acc -= H[(size_t)i * m + j] * y[j];
-            y[i] = acc / H[(size_t)i * m + i];
+            y[i] = H[(size_t)i * m + i] != 0.0 ? acc / H[(size_t)i * m + i] : 0.0;  // Krylov breakdown
         }
         CK1(cudaMemcpyAsync(h->hd, y.data(), k * 8, cudaMemcpyHostToDevice, s));
         k_combo<<<nb(N, 256), 256, 0, s>>>(N, k, h->Kr, N, h->hd, h->T);
@@ -542,6 +558,7 @@ int bte1d_block_solve(Bte1d* h, double dt, const double* E, const double* X, dou
                                                                                         h->VB, h->vld, vs);
     CK1(cudaGetLastError());
     CK1(bte_lu_factor_t<float>(Nx, n, n, h->VB, h->vld, vs, h->Vpiv, h->Vinfo, s, 0));
+    if (int rc = check_blocks(h, s)) return rc;
     k_to_f32<<<nb(N, 256), 256, 0, s>>>(N, X, h->Zf);
     CK1(bte_lu_solve_t<float>(Nx, n, h->VB, h->vld, vs, h->Vpiv, h->Zf, 0, s));
     k_to_f64<<<nb(N, 256), 256, 0, s>>>(N, h->Zf, Y);

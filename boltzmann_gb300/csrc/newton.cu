@@ -1311,7 +1311,7 @@ void bte_work_release(BteWork* w) {
 // ---------------------------------------------------------------------------------
 // Library-wide launch counter and per-family CUDA-event timing (off unless enabled).
 // ---------------------------------------------------------------------------------
-enum { PF_RESIDUAL = 0, PF_JACOBIAN, PF_LU, PF_LUSOLVE, PF_REFINE, PF_OTHER, PF_COUNT };
+enum { PF_RESIDUAL = 0, PF_JACOBIAN, PF_LU, PF_LUSOLVE, PF_REFINE, PF_OTHER, PF_LU64, PF_COUNT };
 struct Profiler {
     // shared by every solve and serving engine of the process; engines driven from several
     // host threads record into it concurrently, so every member is guarded by `mu`
@@ -1394,9 +1394,9 @@ extern "C" int bte_stats_reset(int enable_timing) {
 }
 
 // out[0] = kernel launches since the last reset; then for each family f in
-// {residual, jacobian, lu_factor, lu_solve, refine, other}: launches, total ms (CUDA
-// events, 0 when timing is off), algorithmic flops, algorithmic bytes; last: points of the
-// mixed form re-solved in FP64 -> 2 + 4 * 6 doubles.
+// {residual, jacobian, lu_factor, lu_solve, refine, other, lu_factor_fp64}: launches, total
+// ms (CUDA events, 0 when timing is off), algorithmic flops, algorithmic bytes; then the
+// points of the mixed form re-solved in FP64 -> 2 + 4 * 7 doubles (+ 5 hand-over reasons).
 extern "C" int bte_stats(double* out, int count) {
     if (!out || count < 2 + 4 * PF_COUNT) return BTE_ERR_ARG;
     cudaDeviceSynchronize();
@@ -1654,7 +1654,7 @@ static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
                                                                   (double*)L.J, ld, jstride, beta_scale, L.rowscale,
                                                                   jm.stage, 1.0, 0.0, nullptr);
             }));
-            CKR(pf.run(PF_LU, s, nact * lu_flops(N), lub, 1, [&] {
+            CKR(pf.run(PF_LU64, s, nact * lu_flops(N), lub, 1, [&] {
                 le = bte_lu_factor_t<double>(nact, N, N + 1, (double*)L.J, ld, jstride, L.piv, L.info, s, 0);
             }));
             CKR(le);

@@ -295,9 +295,18 @@ class BteServer:
             with self._cv:
                 w.dead = repr(e)
                 self.errors.append("%s: %r" % (w.key, e))
-                for r in list(w.queue) + w.admitting + list({id(r): r for r in w.owner.values()}.values()):
+                # requests admitted on this grid (in admission or owning slots) give their HBM
+                # reservation back, each once, so that other grids' requests are not held back
+                held = {id(r): r for r in w.admitting}
+                held.update({id(r): r for r in w.owner.values()})
+                for r in held.values():
+                    self.used -= int(r.P * be.bytes_per_slot)
+                w.admitting, w.running = [], 0
+                w.owner.clear()
+                for r in list(w.queue) + list(held.values()):
                     r.error = repr(e)
                     r.done.set()
+                w.queue.clear()
                 self._cv.notify_all()
 
     def _loop(self, w: _Worker):

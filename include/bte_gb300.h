@@ -203,8 +203,8 @@ int bte_qoi(const bte_grid* g, int P, const double* f, const double* n0, const d
 int bte_lu_factor(int dtype, int P, int N, void* A, int ld, long long stride, int32_t* piv, int32_t* info,
                   void* stream);
 
-/* As bte_lu_factor with an explicit kernel: 0 = automatic (FP32: left-looking with blocks
- * resident in registers for N <= 512, right-looking above; FP64: right-looking),
+/* As bte_lu_factor with an explicit kernel: 0 = automatic (FP32: tensor-core kernel for
+ * N <= 512, right-looking above; FP64: right-looking),
  * 1 = right-looking for every N, 2 = FP32 only, N <= 512: trailing updates on the tcgen05
  * tensor cores in split TF32 (FP32-accurate factors), 3 = left-looking (N <= 512).
  * No counterpart in the reference; used to cross-check the factorizations. */
@@ -228,9 +228,10 @@ int bte_radial_components(const bte_grid* g, int P, const double* f, int n_ev, c
 int bte_stats_reset(int enable_timing);
 
 /* Statistics since the last reset: out[0] = kernel launches; then per family
- * {residual, jacobian, lu_factor, lu_solve, refine, other}: launches, device ms,
- * algorithmic flops, algorithmic bytes; out[25] = points of the mixed form that did not
- * converge and were re-solved from their initial state in FP64 (count >= 26 doubles).
+ * {residual, jacobian, lu_factor (FP32), lu_solve, refine, other, lu_factor_fp64}: launches,
+ * device ms, algorithmic flops, algorithmic bytes; out[29] = points of the mixed form handed
+ * to the FP64 path (count >= 30 doubles); out[30..34] = their reasons {max_iter, line
+ * search, non-finite, singular, refinement} when count >= 35.
  * Replaces bte_0d3v_batched.profile_stats (bte_0d3v_batched.py:1248-1315). */
 int bte_stats(double* out, int count);
 

@@ -698,6 +698,19 @@ def steady_state_solve(ops: Operators, prm: Params, f0, atol, rtol, max_iter, ee
                        alpha_min=1e-16, alpha_rho=0.01, line_search_c=1e-3, log=None):
     """steady_state_solve, bte_0d3v_batched.py:882-979 (the batch-global loop, per-point
     Armijo backtracking and final normalisation). Returns (ff, qoi, info)."""
+    gen = steady_state_iterations(ops, prm, f0, atol, rtol, max_iter, ee, alpha_min, alpha_rho, line_search_c, log)
+    while True:
+        try:
+            next(gen)
+        except StopIteration as stop:
+            return stop.value
+
+
+def steady_state_iterations(ops: Operators, prm: Params, f0, atol, rtol, max_iter, ee,
+                            alpha_min=1e-16, alpha_rho=0.01, line_search_c=1e-3, log=None):
+    """steady_state_solve as a generator that yields after every Newton iteration of the
+    batch-global loop (so a caller can time bounded slices of one solve) and returns
+    (ff, qoi, info) when the reference's loop would end."""
     n_pts = f0.shape[1]
     u = ops.u
     Q, R = ops.Qmat, ops.Rmat
@@ -738,6 +751,7 @@ def steady_state_solve(ops: Operators, prm: Params, f0, atol, rtol, max_iter, ee
                 log(it, abs_error, abs_error / r0)
         h_prev = h_curr
         it += 1
+        yield it
     else:
         status = "converged" if not (abs_error > atol + rtol * r0).any() else "max_iter"
     abs_error = np.linalg.norm(res(h_curr), axis=0)

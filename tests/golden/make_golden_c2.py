@@ -19,7 +19,16 @@ evaluated with the reference's own `get_rhs_and_jacobian` residual
 can tell a converged point from one where the reference stopped at its line-search break
 (`:947-956`).
 
-Usage:  python tests/golden/make_golden_c2.py [c2|c5]   (both when no argument is given)
+With --perturbed (run after the plain run), the same solves are repeated with the
+reference's operators perturbed at the rounding level (4 ulps, seeded), and the fixture gains
+`ff_perturbed` and `resolution`, the per-point relative L2 shift of the EDF: how precisely
+FP64 arithmetic determines the reference's own answer at that point.
+
+With --perturbed-mass, the perturbation is one rounding unit on each mass-matrix entry,
+carried through the reference's M^-1 scaling of its operators; the fixture gains
+`ff_perturbed_mass` and `resolution_mass`.
+
+Usage:  python tests/golden/make_golden_c2.py [c2|c5] [--perturbed | --perturbed-mass]
 """
 import os
 import sys
@@ -61,10 +70,50 @@ def _initial_state(s, f0):
     return f1[:, None] + np.dot(s._op_qmat[0], np.dot(s._op_rmat[0], h))
 
 
-def run(m, xs, name, n_sp, l_max, points):
+def _perturb(s, seed, ulps=4.0):
+    """Multiply every entry of the reference's assembled collision, gas-temperature, advection
+    and Coulomb operators by (1 + ulps * eps * u), u uniform in [-1, 1]: a change smaller than
+    the rounding any FP64 assembly of those operators carries (quadrature sums, the Cholesky
+    inverse of the mass matrix)."""
+    rng = np.random.default_rng(seed)
+    eps = np.finfo(np.float64).eps
+    for name in ("_op_col_en", "_op_col_gT", "_op_advection", "_op_col_ee"):
+        op = getattr(s, name)[0]
+        if op is None or np.ndim(op) == 0:
+            continue
+        getattr(s, name)[0] = op * (1.0 + ulps * eps * rng.uniform(-1.0, 1.0, np.shape(op)))
+
+
+def _perturb_mass(s, seed):
+    """Change the mass matrix by one rounding unit per entry (symmetric, seeded) and carry it
+    through the reference's M^-1 scaling of every operator, to first order:
+    op <- op - M^-1 (dM op). The reference's operators are M^-1 times raw integrals, and M^-1
+    inherits the mass matrix's conditioning; this is the size of perturbation that any FP64
+    assembly of M (a quadrature sum) leaves in them."""
+    rng = np.random.default_rng(seed)
+    eps = np.finfo(np.float64).eps
+    M = s._op_mass_mat[0]
+    u = rng.uniform(-1.0, 1.0, M.shape)
+    dM = eps * np.abs(M) * np.triu(u) + (eps * np.abs(M) * np.triu(u, 1)).T
+    Minv = s._op_spec_sp[0].inverse_mass_mat(Mmat=M)
+    for name in ("_op_col_en", "_op_col_gT", "_op_advection", "_op_col_ee"):
+        op = getattr(s, name)[0]
+        if op is None or np.ndim(op) == 0:
+            continue
+        if name == "_op_col_en":  # (species, n, n)
+            new = np.stack([o - Minv @ (dM @ o) for o in op])
+        else:                     # (n, n) or (n, n, n): M^-1 acts on the first index
+            flat = op.reshape(op.shape[0], -1)
+            new = (flat - Minv @ (dM @ flat)).reshape(op.shape)
+        getattr(s, name)[0] = new
+
+
+def run(m, xs, name, n_sp, l_max, points, perturb_seed=None, mode="ulps"):
     P = len(points)
     t0 = time.time()
     s, args = G.make_solver(m, xs, n_sp, l_max, True, P)
+    if perturb_seed is not None:
+        (_perturb_mass if mode == "mass" else _perturb)(s, perturb_seed)
     t_setup = time.time() - t0
     ebyn = np.array([p[0] for p in points])
     ion = np.array([p[1] for p in points])
@@ -85,6 +134,16 @@ def run(m, xs, name, n_sp, l_max, points):
     r0 = np.linalg.norm(res_func(_initial_state(s, ffw), 0, 0), axis=0)
     hf, _ = _state_of(s, ff)
     r1 = np.linalg.norm(res_func(hf, 0, 0), axis=0)
+    if perturb_seed is not None:
+        # a second solve of the same points with operators perturbed at the rounding level:
+        # how far the reference's own answer moves under FP64-level changes of its operators
+        g = dict(np.load(os.path.join(HERE, name)))
+        sfx = "_mass" if mode == "mass" else ""
+        g["ff_perturbed" + sfx] = ff
+        g["resolution" + sfx] = np.linalg.norm(ff - g["ff"], axis=0) / np.linalg.norm(g["ff"], axis=0)
+        np.savez_compressed(os.path.join(HERE, name), **g)
+        print("%s: resolution%s %s" % (name, sfx, np.array2string(g["resolution" + sfx], precision=2)), flush=True)
+        return
     out = dict(n_sp=n_sp, l_max=l_max, EbyN=ebyn, ion_deg=ion, f0=f0, ff_warm=ffw, ff=ff,
                energy=qoi["energy"], mobility=qoi["mobility"], diffusion=qoi["diffusion"], rates=qoi["rates"],
                abs_error=r1, rel_error=r1 / r0, setup_s=t_setup, solve_s=np.array([t2 - t1, t3 - t2]), **prm)
@@ -94,15 +153,17 @@ def run(m, xs, name, n_sp, l_max, points):
 
 
 def main():
-    which = sys.argv[1:] or ["c2", "c5"]
+    which = [w for w in sys.argv[1:] if not w.startswith("--")] or ["c2", "c5"]
+    seed = 7 if ("--perturbed" in sys.argv or "--perturbed-mass" in sys.argv) else None
+    mode = "mass" if "--perturbed-mass" in sys.argv else "ulps"
     xs = write_synthetic_lxcat(os.path.join("/tmp", "eAr_golden_%d.lxcat" % os.getpid()))
     cwd = os.getcwd()
     m = import_reference()
     try:
         if "c2" in which:
-            run(m, xs, "c2_shape_reference.npz", 128, 2, C2_POINTS)
+            run(m, xs, "c2_shape_reference.npz", 128, 2, C2_POINTS, seed, mode)
         if "c5" in which:
-            run(m, xs, "c5_reduced_reference.npz", 64, 4, C5_POINTS)
+            run(m, xs, "c5_reduced_reference.npz", 64, 4, C5_POINTS, seed, mode)
     finally:
         os.chdir(cwd)
         os.unlink(xs)

@@ -13,7 +13,7 @@ class FakeEngine:
     """Each point finishes after a number of steps set by its E (1 + int(E) % 4); its result is
     a deterministic function of its own parameters, as a real per-point solve is."""
 
-    def __init__(self, key, capacity=64, bytes_per_slot=1000, step_s=0.002, fail_on=None):
+    def __init__(self, key, capacity=64, bytes_per_slot=1000, step_s=0.002, fail_on=None, fail_step=False):
         self.key = key
         self.capacity = capacity
         self.bytes_per_slot = bytes_per_slot
@@ -22,6 +22,7 @@ class FakeEngine:
         self.left = {}
         self.points = {}
         self.fail_on = fail_on
+        self.fail_step = fail_step
         self.steps = 0
         self.max_running = 0
         self.lock = threading.Lock()
@@ -42,6 +43,8 @@ class FakeEngine:
 
     def step(self):
         time.sleep(self.step_s)
+        if self.fail_step:
+            raise RuntimeError("planted step failure")
         self.steps += 1
         done = []
         for s in list(self.left):
@@ -168,4 +171,23 @@ def test_cancel_a_queued_request():
         wait_all([big, b], timeout=10)
         assert big.error is None and b.error is None and b.ff is not None
         assert not srv.cancel(b)                       # finished
+        assert srv.used == 0
+
+
+def test_failed_grid_returns_its_hbm_reservation():
+    """A grid whose engine fails in a step after admitting a request gives that request's HBM
+    reservation back: a request on another grid that needs more than the budget left beside
+    the failed request's footprint is still admitted and finishes."""
+    rng = np.random.default_rng(9)
+
+    def factory(k):
+        return FakeEngine(k, capacity=32, bytes_per_slot=1000, step_s=0.02, fail_step=(k == (64, 1)))
+
+    with BteServer(None, [(64, 1), (96, 2)], hbm_budget_bytes=20_000, backend_factory=factory) as srv:
+        bad = srv.submit(make_req(rng, 64, 1, P=15))
+        with pytest.raises(RuntimeError, match="planted step"):
+            wait_all([bad], timeout=10)
+        other = srv.submit(make_req(rng, 96, 2, P=10))
+        wait_all([other], timeout=10)
+        assert other.ff is not None and other.error is None
         assert srv.used == 0
