@@ -25,7 +25,8 @@ EXPORTED = ["bte_grid_create", "bte_grid_destroy", "bte_grid_info", "bte_grid_ex
             "bte_radial_components", "bte_stats_reset", "bte_stats", "bte_solve_info", "bte_lu_factor_ex",
             "bte_engine_create", "bte_engine_destroy", "bte_engine_admit", "bte_engine_step", "bte_engine_collect",
             "bte_engine_info", "bte_solve_transient", "bte1d_create", "bte1d_destroy", "bte1d_step_x", "bte1d_step_v", "bte1d_lmat", "bte1d_block_solve",
-            "bte1d_ords_to_lm", "bte1d_lm_to_ords", "bte1d_launches", "bte1d_last_error",
+            "bte1d_ords_to_lm", "bte1d_lm_to_ords", "bte1d_launches", "bte1d_last_error", "bte1d_fim_matvec",
+            "bte1d_step_fim",
             "bte_bidiag_solve", "bte_banded_tri_solve", "bte_banded_tri_mv", "bte_adv_be_sweep",
             "bte_bsr_upper_unit_solve", "bte_sweep_last_error", "bte_dgemm_nn", "bte_permute3",
             "bte_fvm_inflow_zero", "bte_fvm_create", "bte_fvm_destroy", "bte_fvm_set_collision_inverse",
@@ -111,6 +112,8 @@ def load() -> C.CDLL:
     lib.bte1d_step_v.argtypes = [vp, C.c_double, vp, vp, C.c_double, C.c_double, C.c_int, dp, vp]
     lib.bte1d_lmat.argtypes = [vp, C.c_double, vp, vp, vp, vp]
     lib.bte1d_block_solve.argtypes = [vp, C.c_double, vp, vp, vp, vp]
+    lib.bte1d_fim_matvec.argtypes = [vp, C.c_double, vp, vp, vp, vp]
+    lib.bte1d_step_fim.argtypes = [vp, C.c_double, vp, vp, C.c_double, C.c_double, C.c_int, C.c_int, dp, vp]
     lib.bte1d_ords_to_lm.argtypes = [vp, vp, vp, vp]
     lib.bte1d_lm_to_ords.argtypes = [vp, vp, vp, vp]
     lib.bte1d_launches.argtypes = [vp]

@@ -199,6 +199,13 @@ class bte_1d3v:
             raise RuntimeError("bte1d_create failed (%d): %s" % (rc, lib.bte1d_last_error().decode()))
         self._h = h
         self.mass_op = s.export_operator(0, "MASS_VEC")
+        st = str(getattr(p, "solver_type", "strang")).lower()
+        if st in ("2", "fully_implicit"):
+            self.solver = "fully_implicit"
+        elif st in ("0", "strang", "xvx_strang_split", "none"):
+            self.solver = "strang"
+        else:
+            raise NotImplementedError("solver_type must be the Strang split or fully_implicit for the spectral v-space")
         self.op_qoi = None   # the QoI rows, built on the first compute_qoi
         self.gmres_info = None
 
@@ -281,10 +288,52 @@ class bte_1d3v:
         return V
 
     def step(self, E, v, dv, time, dt, verbose=0):
-        """One Strang-split step (:1885-1889): x over dt/2, v over dt, x over dt/2."""
+        """One step of the configured solver: the Strang split (:1885-1889: x over dt/2, v over
+        dt, x over dt/2), or with solver_type "fully_implicit" one backward-Euler step of the
+        coupled v-space and x-advection operator (step_fim)."""
+        if self.solver == "fully_implicit":
+            return self.step_fim(E, v, time, dt)
         v = self.step_bte_x(v, time, 0.5 * dt)
         v = self.step_bte_v(E, v, None, time, dt)
         return self.step_bte_x(v, time + 0.5 * dt, 0.5 * dt)
+
+    def fim_mvec(self, E, v, dt):
+        """The fully implicit step's operator on ordinates v (Nr * Nvt, Nx):
+        v - dt (P_sh2o (Cv + E_x Av) P_o2sh v - (adv_x (x) cos theta) v D^T), identity rows on the
+        inflow boundary. The reference's fully implicit solver takes only the finite-volume
+        v-space (:1891); this operator composes its spectral operators (Lmat_mvec, :1051-1055,
+        and step_bte_x's BE Chebyshev advection, :912-982) as its matvec test composes them
+        (test_bte_1d_matvec.py:19-83)."""
+        V = self._dev(v, (self.dof_vr * self.dof_vt, self.dof_x))
+        Ed = self._dev(E, (self.dof_x,))
+        Y = self.torch.empty_like(V)
+        self._check(_lib.load().bte1d_fim_matvec(self._h, float(dt), _lib.ptr(Ed), _lib.ptr(V), _lib.ptr(Y),
+                                                 self._s()), "bte1d_fim_matvec")
+        return Y
+
+    def step_fim(self, E, v, time, dt, atol=None, rtol=None, max_iter=None, pc=None):
+        """One fully implicit step over dt at field E: fim_mvec(v_new) = v (inflow values 0) by
+        right-preconditioned GMRES(gmres_rsrt) to rtol (params rtol, 1e-10 in the 1D3V tables);
+        the preconditioner is a Lie split, the per-point v-space block inverse (FP32 factors)
+        then the backward-Euler x-advection over dt (pc "split", default), or the v blocks alone
+        (pc "vblock"). gmres_info holds the iterations and residuals."""
+        p = self.params
+        pc = getattr(p, "fim_pc", "split") if pc is None else pc
+        if pc not in ("split", "vblock"):
+            raise ValueError("pc must be 'split' or 'vblock'")
+        V = self._dev(v, (self.dof_vr * self.dof_vt, self.dof_x)).clone()
+        Ed = self._dev(E, (self.dof_x,))
+        info = (C.c_double * 4)()
+        rc = _lib.load().bte1d_step_fim(self._h, float(dt), _lib.ptr(Ed), _lib.ptr(V),
+                                         float(p.rtol if rtol is None else rtol), float(p.atol if atol is None else atol),
+                                         int(p.gmres_maxiter if max_iter is None else max_iter),
+                                         0 if pc == "split" else 1, info, self._s())
+        self._check(rc, "bte1d_step_fim")
+        self.gmres_info = {"iterations": int(info[0]), "residual_abs": info[1], "residual_rel": info[2],
+                           "status": int(info[3])}
+        if info[3] != 0:
+            raise RuntimeError("GMRES did not converge: iterations=%d ||res||/||b||=%.4e" % (info[0], info[2]))
+        return V
 
     def initial_condition(self, type=0):
         """initial_condition(type=0) (:1274-1286, maxwellian_eedf :1217-1272): a Maxwellian at the

@@ -241,6 +241,134 @@ __global__ void k_sub(size_t m, const double* __restrict__ a, const double* __re
 
 inline unsigned nb(size_t m, int b) { return (unsigned)((m + b - 1) / b); }
 
+// ---- fully implicit spectral step ------------------------------------------------------------
+// T[m][x] = sum_k D[x][k] V[m][k] for each (r, j) line m = r * Nvt + j, with the inflow row of
+// the upwinded derivative zeroed (row 0 for ordinates moving right, D_L; row Nx - 1 otherwise,
+// D_R: bte_1d3v_solver.py:792-800). DT = D transposed, so that the threads (one per output x)
+// read consecutive entries; each entry feeds FD_L lines staged in shared memory.
+constexpr int FD_L = 8;
+__global__ void __launch_bounds__(256)
+k_fim_dx(int Nlines, int Nvt, int Nx, const double* __restrict__ DT, const int8_t* __restrict__ right,
+         const double* __restrict__ V, double* __restrict__ T) {
+    extern __shared__ double sv[];  // [FD_L][Nx]
+    const int l0 = blockIdx.x * FD_L;
+    const int nl = min(FD_L, Nlines - l0);
+    for (int e = threadIdx.x; e < nl * Nx; e += blockDim.x) sv[e] = V[(size_t)l0 * Nx + e];
+    __syncthreads();
+    for (int x = threadIdx.x; x < Nx; x += blockDim.x) {
+        double acc[FD_L];
+#pragma unroll
+        for (int t = 0; t < FD_L; ++t) acc[t] = 0.0;
+        for (int k = 0; k < Nx; ++k) {
+            const double dk = DT[(size_t)k * Nx + x];
+#pragma unroll
+            for (int t = 0; t < FD_L; ++t) acc[t] += dk * sv[(t < nl ? t : 0) * Nx + k];
+        }
+#pragma unroll
+        for (int t = 0; t < FD_L; ++t) {
+            if (t >= nl) break;
+            const int j = (l0 + t) % Nvt;
+            const bool inflow_row = right[j] ? (x == 0) : (x == Nx - 1);
+            T[(size_t)(l0 + t) * Nx + x] = inflow_row ? 0.0 : acc[t];
+        }
+    }
+}
+
+// The backward-Euler operator of the fully implicit step on ordinates, per x point:
+//   Y = V - dt (P_sh2o (Cv + E_x Av) P_o2sh V - cos(theta_j) adv_x T)
+// (T = the x-derivative lines of k_fim_dx; Cv, Av carry tau), with identity rows on the inflow
+// boundary. One CTA per FC_X consecutive x points; V, T, adv_x staged in shared memory.
+constexpr int FC_X = 4;
+__global__ void __launch_bounds__(256)
+k_fim_combine(int Nr, int Nvt, int nsh, int Nx, double dt, const double* __restrict__ Ps,
+              const double* __restrict__ Po, const double* __restrict__ CvT, const double* __restrict__ AvT,
+              const double* __restrict__ AxT, const double* __restrict__ cth, const int8_t* __restrict__ right,
+              const double* __restrict__ E, const double* __restrict__ V, const double* __restrict__ T,
+              double* __restrict__ Y) {
+    extern __shared__ double sm[];
+    const int M = Nr * Nvt, n = Nr * nsh;
+    double* sV = sm;                 // [FC_X][M]
+    double* sT = sV + FC_X * M;      // [FC_X][M]
+    double* sU = sT + FC_X * M;      // [FC_X][n]  harmonics
+    double* sW = sU + FC_X * n;      // [FC_X][n]  (Cv + E Av) harmonics
+    double* sA = sW + FC_X * n;      // [Nr][Nr]   adv_x transposed
+    const int x0 = blockIdx.x * FC_X;
+    const int nx = min(FC_X, Nx - x0);
+    for (int e = threadIdx.x; e < M * FC_X; e += blockDim.x) {
+        const int m = e / FC_X, t = e % FC_X;
+        const bool ok = t < nx;
+        sV[t * M + m] = ok ? V[(size_t)m * Nx + x0 + t] : 0.0;
+        sT[t * M + m] = ok ? T[(size_t)m * Nx + x0 + t] : 0.0;
+    }
+    for (int e = threadIdx.x; e < Nr * Nr; e += blockDim.x) sA[e] = AxT[e];
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * FC_X; e += blockDim.x) {
+        const int a = e % n, t = e / n, r = a / nsh, l = a % nsh;
+        double u = 0.0;
+        for (int j = 0; j < Nvt; ++j) u += Ps[l * Nvt + j] * sV[t * M + r * Nvt + j];
+        sU[t * n + a] = u;
+    }
+    __syncthreads();
+    for (int a = threadIdx.x; a < n; a += blockDim.x) {
+        double c[FC_X], v[FC_X];
+#pragma unroll
+        for (int t = 0; t < FC_X; ++t) { c[t] = 0.0; v[t] = 0.0; }
+        for (int b = 0; b < n; ++b) {
+            const double cb = CvT[(size_t)b * n + a], ab = AvT[(size_t)b * n + a];
+#pragma unroll
+            for (int t = 0; t < FC_X; ++t) {
+                c[t] += cb * sU[t * n + b];
+                v[t] += ab * sU[t * n + b];
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < FC_X; ++t) sW[t * n + a] = c[t] + ((t < nx) ? E[x0 + t] : 0.0) * v[t];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < M * FC_X; e += blockDim.x) {
+        const int t = e / M, m = e % M, r = m / Nvt, j = m % Nvt;
+        if (t >= nx) continue;
+        const int x = x0 + t;
+        const double vx = sV[t * M + m];
+        const bool inflow_row = right[j] ? (x == 0) : (x == Nx - 1);
+        double y = vx;
+        if (!inflow_row) {
+            double yv = 0.0;
+            for (int l = 0; l < nsh; ++l) yv += Po[j * nsh + l] * sW[t * n + r * nsh + l];
+            double yx = 0.0;
+            for (int k = 0; k < Nr; ++k) yx += sA[k * Nr + r] * sT[t * M + k * Nvt + j];
+            y = vx - dt * (yv - cth[j] * yx);
+        }
+        Y[(size_t)m * Nx + x] = y;
+    }
+}
+
+// out = in + P_sh2o (Z - U): the exact inverse of I - dt P_sh2o L_v P_o2sh on ordinates from the
+// per-point inverse Z = (I - dt L_v)^-1 U of the harmonics U = P_o2sh in (P_o2sh P_sh2o = I)
+__global__ void k_lm_correct(int Nr, int Nvt, int nsh, int Nx, const double* __restrict__ Po,
+                             const double* __restrict__ in, const double* __restrict__ Z,
+                             const double* __restrict__ U, double* __restrict__ out) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= Nr * Nvt * Nx) return;
+    const int x = e % Nx, rj = e / Nx, r = rj / Nvt, j = rj % Nvt;
+    double s = in[e];
+    for (int l = 0; l < nsh; ++l) {
+        const size_t a = (size_t)x * (Nr * nsh) + r * nsh + l;
+        s += Po[j * nsh + l] * (Z[a] - U[a]);
+    }
+    out[e] = s;
+}
+
+// copy with the inflow boundary values set to 0
+__global__ void k_copy_zero_inflow(int Nr, int Nvt, int Nx, const int8_t* __restrict__ right,
+                                   const double* __restrict__ in, double* __restrict__ out) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= Nr * Nvt * Nx) return;
+    const int x = e % Nx, j = (e / Nx) % Nvt;
+    const bool inflow = right[j] ? (x == 0) : (x == Nx - 1);
+    out[e] = inflow ? 0.0 : in[e];
+}
+
 }  // namespace
 
 struct Bte1d {
@@ -267,6 +395,12 @@ struct Bte1d {
     double *part = nullptr, *hd = nullptr;
     double* Vt = nullptr;  // ordinates scratch
     double* Vt2 = nullptr;
+    // fully implicit step: adv_x transposed, D transposed, and the ordinates-space GMRES buffers
+    // (allocated on first use)
+    double *AxT = nullptr, *DT = nullptr;
+    double *Fk = nullptr, *Fr = nullptr, *Fw = nullptr, *Fz = nullptr, *Fx = nullptr, *Fb = nullptr, *Ft = nullptr;
+    double *Fpart = nullptr;
+    int fcap = 0;
     std::vector<void*> allocs;
     long long launches = 0;
 };
@@ -342,7 +476,27 @@ int bte1d_create(int device, int Nr, int nsh, int Nvt, int Nx, const double* Q, 
     A((void**)&h->part, (size_t)(restart + 1) * RED_BLOCKS * 8); A((void**)&h->hd, (size_t)(restart + 1) * 8);
     A((void**)&h->Vt, nv * 8);
     A((void**)&h->Vt2, nv * 8);
+    A((void**)&h->AxT, (size_t)Nr * Nr * 8); A((void**)&h->DT, (size_t)Nx * Nx * 8);
     if (rc != BTE_OK) { free1d(h); delete h; return rc; }
+    // adv_x = Q diag(d) Q^-1 (transposed), and D transposed, for the fully implicit step
+    {
+        std::vector<double> AxT((size_t)Nr * Nr), DT((size_t)Nx * Nx);
+        for (int r = 0; r < Nr; ++r)
+            for (int k = 0; k < Nr; ++k) {
+                double v = 0.0;
+                for (int i = 0; i < Nr; ++i) v += Q[(size_t)r * Nr + i] * d[i] * Qinv[(size_t)i * Nr + k];
+                AxT[(size_t)k * Nr + r] = v;
+            }
+        for (int a = 0; a < Nx; ++a)
+            for (int b = 0; b < Nx; ++b) DT[(size_t)b * Nx + a] = D[(size_t)a * Nx + b];
+        if (cudaMemcpy(h->AxT, AxT.data(), AxT.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(h->DT, DT.data(), DT.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess) {
+            g_err1d = "copy of the setup operators failed";
+            free1d(h);
+            delete h;
+            return BTE_ERR_CUDA;
+        }
+    }
     // transposed v-space operators; inflow side of each ordinate
     std::vector<double> CvT((size_t)n * n), AvT((size_t)n * n);
     for (int a = 0; a < n; ++a)
@@ -585,6 +739,159 @@ int bte1d_lm_to_ords(Bte1d* h, const double* U, double* V, void* stream) {
     return BTE_OK;
 }
 
+// ---- fully implicit spectral step ------------------------------------------------------------
+static int fim_matvec(Bte1d* h, double dt, const double* E, const double* V, double* Y, cudaStream_t s) {
+    const int Nr = h->Nr, Nvt = h->Nvt, Nx = h->Nx, M = Nr * Nvt;
+    if (!h->Ft && alloc1d(h, (void**)&h->Ft, (size_t)M * Nx * 8) != BTE_OK) return BTE_ERR_ALLOC;
+    const size_t sdx = (size_t)FD_L * Nx * 8;
+    const size_t scb = ((size_t)2 * FC_X * M + 2 * FC_X * h->n + (size_t)Nr * Nr) * 8;
+    CK1(bte_raise_smem_limit((const void*)k_fim_dx, sdx));
+    CK1(bte_raise_smem_limit((const void*)k_fim_combine, scb));
+    k_fim_dx<<<nb(M, FD_L), 256, sdx, s>>>(M, Nvt, Nx, h->DT, h->right, V, h->Ft);
+    k_fim_combine<<<nb(Nx, FC_X), 256, scb, s>>>(Nr, Nvt, h->nsh, Nx, dt, h->Ps, h->Po, h->CvT, h->AvT, h->AxT,
+                                                 h->cth, h->right, E, V, h->Ft, Y);
+    CK1(cudaGetLastError());
+    h->launches += 2;
+    return BTE_OK;
+}
+
+int bte1d_fim_matvec(Bte1d* h, double dt, const double* E, const double* V, double* Y, void* stream) {
+    if (!h || !E || !V || !Y) { g_err1d = "null argument"; return BTE_ERR_ARG; }
+    cudaSetDevice(h->device);
+    return fim_matvec(h, dt, E, V, Y, (cudaStream_t)stream);
+}
+
+int bte1d_step_fim(Bte1d* h, double dt, const double* E, double* V, double rtol, double atol, int max_iter, int pc,
+                   double* info4, void* stream) {
+    if (!h || !E || !V || !info4) { g_err1d = "null argument"; return BTE_ERR_ARG; }
+    if (pc < 0 || pc > 1 || max_iter < 1) { g_err1d = "pc must be 0 (split) or 1 (v-blocks); max_iter >= 1"; return BTE_ERR_ARG; }
+    cudaSetDevice(h->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    const int Nr = h->Nr, Nvt = h->Nvt, Nx = h->Nx, n = h->n, m = h->kcap;
+    const size_t N = (size_t)Nr * Nvt * Nx, Nu = (size_t)n * Nx;
+    const long long vs = (long long)n * h->vld;
+    if (h->fcap == 0) {
+        int rc = BTE_OK;
+        auto A = [&](void** p, size_t b) { if (rc == BTE_OK) rc = alloc1d(h, p, b); };
+        A((void**)&h->Fk, (size_t)(m + 1) * N * 8);
+        A((void**)&h->Fr, N * 8); A((void**)&h->Fw, N * 8); A((void**)&h->Fz, N * 8); A((void**)&h->Fx, N * 8);
+        A((void**)&h->Fb, N * 8);
+        A((void**)&h->Fpart, (size_t)(m + 1) * RED_BLOCKS * 8);
+        if (rc != BTE_OK) return rc;
+        h->fcap = m;
+    }
+    long long L = 0;
+    // the per-point FP32 blocks I - dt (Cv + E_x Av) of the preconditioner's v part
+    k_build_vblocks<<<dim3(std::min<unsigned>(nb((size_t)n * n, 256), 32), Nx), 256, 0, s>>>(n, Nx, dt, h->CvT, h->AvT, E,
+                                                                                        h->VB, h->vld, vs);
+    CK1(cudaGetLastError());
+    CK1(bte_lu_factor_t<float>(Nx, n, n, h->VB, h->vld, vs, h->Vpiv, h->Vinfo, s, 0));
+    L += 2;
+    if (int rc = check_blocks(h, s)) return rc;
+    auto precond = [&](const double* x, double* y) -> int {
+        // v part: y = x + P_sh2o ((I - dt L_v)^-1 - I) P_o2sh x, per point, FP32 factors
+        k_ords_to_lm<<<nb(Nu, 256), 256, 0, s>>>(Nr, Nvt, h->nsh, Nx, h->Ps, x, h->U);
+        k_to_f32<<<nb(Nu, 256), 256, 0, s>>>(Nu, h->U, h->Zf);
+        CK1(bte_lu_solve_t<float>(Nx, n, h->VB, h->vld, vs, h->Vpiv, h->Zf, 0, s));
+        k_to_f64<<<nb(Nu, 256), 256, 0, s>>>(Nu, h->Zf, h->Z);
+        k_lm_correct<<<nb(N, 256), 256, 0, s>>>(Nr, Nvt, h->nsh, Nx, h->Po, x, h->Z, h->U, y);
+        CK1(cudaGetLastError());
+        L += 5;
+        // x part (pc 0): the backward-Euler x-advection over dt
+        if (pc == 0) {
+            int rc = bte1d_step_x(h, dt, y, s);
+            if (rc) return rc;
+        }
+        return BTE_OK;
+    };
+    auto dots = [&](int k, const double* Vb, const double* w, double* host_out) -> cudaError_t {
+        k_dots_partial<<<dim3(RED_BLOCKS, k), 256, 0, s>>>(N, k, Vb, N, w, h->Fpart);
+        k_dots_final<<<k, 256, 0, s>>>(k, RED_BLOCKS, h->Fpart, h->hd);
+        L += 2;
+        cudaError_t e = cudaMemcpyAsync(host_out, h->hd, k * 8, cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) return e;
+        return cudaStreamSynchronize(s);
+    };
+    // b = V with the inflow values set to 0 (the boundary condition); x0 = P^-1 b
+    k_copy_zero_inflow<<<nb(N, 256), 256, 0, s>>>(Nr, Nvt, Nx, h->right, V, h->Fb);
+    ++L;
+    double bnorm = 0.0;
+    CK1(dots(1, h->Fb, h->Fb, &bnorm));
+    bnorm = std::sqrt(bnorm);
+    const double tol = std::max(atol, rtol * bnorm);
+    if (int rc = precond(h->Fb, h->Fx)) return rc;
+    int it = 0;
+    double rnorm = 0.0;
+    bool conv = false;
+    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), hh(m + 1), y(m);
+    while (true) {
+        if (int rc = fim_matvec(h, dt, E, h->Fx, h->Fw, s)) return rc;
+        k_sub<<<nb(N, 256), 256, 0, s>>>(N, h->Fb, h->Fw, h->Fr);
+        ++L;
+        CK1(dots(1, h->Fr, h->Fr, &rnorm));
+        rnorm = std::sqrt(rnorm);
+        if (rnorm <= tol) { conv = true; break; }
+        if (it >= max_iter) break;
+        k_scale<<<nb(N, 256), 256, 0, s>>>(N, 1.0 / rnorm, h->Fr, h->Fk);
+        ++L;
+        std::fill(g.begin(), g.end(), 0.0);
+        g[0] = rnorm;
+        int k = 0;
+        for (; k < m && it < max_iter; ++k, ++it) {
+            double* vk = h->Fk + (size_t)k * N;
+            double* vk1 = h->Fk + (size_t)(k + 1) * N;
+            if (int rc = precond(vk, h->Fz)) return rc;
+            if (int rc = fim_matvec(h, dt, E, h->Fz, vk1, s)) return rc;
+            for (int pass = 0; pass < 2; ++pass) {  // classical Gram-Schmidt, applied twice
+                CK1(dots(k + 1, h->Fk, vk1, hh.data()));
+                CK1(cudaMemcpyAsync(h->hd, hh.data(), (k + 1) * 8, cudaMemcpyHostToDevice, s));
+                k_sub_combo<<<nb(N, 256), 256, 0, s>>>(N, k + 1, h->Fk, N, h->hd, vk1);
+                ++L;
+                for (int j = 0; j <= k; ++j) H[(size_t)j * m + k] = (pass == 0 ? 0.0 : H[(size_t)j * m + k]) + hh[j];
+            }
+            double nn = 0.0;
+            CK1(dots(1, vk1, vk1, &nn));
+            nn = std::sqrt(nn);
+            H[(size_t)(k + 1) * m + k] = nn;
+            if (nn > 0) { k_scale<<<nb(N, 256), 256, 0, s>>>(N, 1.0 / nn, vk1, vk1); ++L; }
+            for (int j = 0; j < k; ++j) {  // Givens rotations on column k
+                const double a = H[(size_t)j * m + k], b = H[(size_t)(j + 1) * m + k];
+                H[(size_t)j * m + k] = cs[j] * a + sn[j] * b;
+                H[(size_t)(j + 1) * m + k] = -sn[j] * a + cs[j] * b;
+            }
+            const double a = H[(size_t)k * m + k], b = H[(size_t)(k + 1) * m + k];
+            const double rr = std::hypot(a, b);
+            cs[k] = rr > 0 ? a / rr : 1.0;
+            sn[k] = rr > 0 ? b / rr : 0.0;
+            H[(size_t)k * m + k] = rr;
+            H[(size_t)(k + 1) * m + k] = 0.0;
+            g[k + 1] = -sn[k] * g[k];
+            g[k] = cs[k] * g[k];
+            if (std::fabs(g[k + 1]) <= tol || nn == 0.0) { ++k; ++it; break; }
+        }
+        for (int i = k - 1; i >= 0; --i) {  // y = H^-1 g, then x += P^-1 (V y)
+            double acc = g[i];
+            for (int j = i + 1; j < k; ++j) acc -= H[(size_t)i * m + j] * y[j];
+            y[i] = H[(size_t)i * m + i] != 0.0 ? acc / H[(size_t)i * m + i] : 0.0;
+        }
+        CK1(cudaMemcpyAsync(h->hd, y.data(), k * 8, cudaMemcpyHostToDevice, s));
+        k_combo<<<nb(N, 256), 256, 0, s>>>(N, k, h->Fk, N, h->hd, h->Fr);
+        ++L;
+        if (int rc = precond(h->Fr, h->Fz)) return rc;
+        k_axpy<<<nb(N, 256), 256, 0, s>>>(N, 1.0, h->Fz, h->Fx);
+        ++L;
+    }
+    CK1(cudaMemcpyAsync(V, h->Fx, N * 8, cudaMemcpyDeviceToDevice, s));
+    CK1(cudaStreamSynchronize(s));
+    h->launches += L;
+    info4[0] = it;
+    info4[1] = rnorm;
+    info4[2] = bnorm > 0 ? rnorm / bnorm : 0.0;
+    info4[3] = conv ? 0.0 : 1.0;
+    return BTE_OK;
+}
+
 long long bte1d_launches(const Bte1d* h) { return h ? h->launches : 0; }
+
 
 }  // extern "C"

@@ -59,6 +59,25 @@ int bte1d_block_solve(bte1d* h, double dt, const double* E, const double* X, dou
 int bte1d_ords_to_lm(bte1d* h, const double* V, double* U, void* stream);
 int bte1d_lm_to_ords(bte1d* h, const double* U, double* V, void* stream);
 
+/* The backward-Euler operator of the fully implicit spectral step on ordinates (layout above):
+ *   Y = V - dt (P_sh2o (Cv + E_x Av) P_o2sh V - (adv_x (x) diag(cos theta_j)) V D_X^T)
+ * with D_X the upwinded Chebyshev derivative (D_L for cos(theta_j) >= 0, D_R otherwise) and
+ * identity rows on the inflow boundary. The reference has no fully implicit solver for the
+ * spectral v-space (bte_1d3v_solver.py:1891 asserts the finite-volume one); this operator is
+ * composed from its operators as its matvec test composes them (test_bte_1d_matvec.py:19-83):
+ * Lmat_mvec (bte_1d3v_solver.py:1051-1055) plus step_bte_x's BE Chebyshev advection (:912-982). */
+int bte1d_fim_matvec(bte1d* h, double dt, const double* E, const double* V, double* Y, void* stream);
+
+/* One fully implicit step of size dt at field E [Nx]: V <- the solution of
+ * bte1d_fim_matvec(V_new) = V with the inflow values of the right-hand side set to 0, by
+ * right-preconditioned restarted GMRES (restart = the handle's, utils.py:1172-1262) to
+ * ||r|| <= max(atol, rtol ||b||). pc 0: the preconditioner is a Lie split, the exact per-point
+ * v-space inverse (FP32 block factors) followed by the backward-Euler x-advection over dt;
+ * pc 1: the v-space blocks alone. info4 (host) = {iterations, ||r||, ||r|| / ||b||,
+ * 0 converged / 1 not}. */
+int bte1d_step_fim(bte1d* h, double dt, const double* E, double* V, double rtol, double atol, int max_iter, int pc,
+                   double* info4, void* stream);
+
 /* Kernel launches made through this handle since it was created. */
 long long bte1d_launches(const bte1d* h);
 

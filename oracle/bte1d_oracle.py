@@ -15,7 +15,12 @@ reference's 0D3V goldens); this module adds the 1D3V pieces:
   applied through explicit inverses as the reference does;
 * step_bte_v (bte_1d3v_solver.py:984-1137) solved exactly per x point (the reference's GMRES
   converges to this solution within its tolerance);
-* initial_condition(type=0) (bte_1d3v_solver.py:1217-1286).
+* initial_condition(type=0) (bte_1d3v_solver.py:1217-1286);
+* the fully implicit spectral step: the reference has no such solver (its fully implicit
+  step asserts the finite-volume v-space, bte_1d3v_solver.py:1891), so it is composed here
+  from the reference's operators as its matvec test composes the coupled operator
+  (test_bte_1d_matvec.py:19-83), checked matrix-free against the Kronecker assembly, and
+  solved directly at small sizes (or by GMRES, the CPU baseline at full size).
 """
 from __future__ import annotations
 
@@ -143,6 +148,114 @@ class Oracle1D:
         for x in range(self.Np):
             w[:, x] = np.linalg.solve(I - dt * (self.Cv + E[x] * self.Av), u[:, x])
         return self.sph_to_ords(w)
+
+    # ---- fully implicit spectral step (composed from the reference's operators) -------------
+    def inflow_rows(self):
+        """Ordinate indices whose inflow boundary is x = -1 (cos(theta) >= 0) and x = +1 (the
+        others), bte_1d3v_solver.py:376-377,936-937."""
+        left = np.where(self.xp_vt <= 0.5 * np.pi)[0]
+        right = np.where(self.xp_vt > 0.5 * np.pi)[0]
+        return left, right
+
+    def _upwinded_d(self):
+        """D_L (row 0 zeroed) and D_R (row Np - 1 zeroed), bte_1d3v_solver.py:792-800."""
+        Np = self.Np
+        DpL = np.zeros((Np, Np))
+        DpR = np.zeros((Np, Np))
+        DpL[1:, :] = self.Dp[1:, :]
+        DpR[:-1, :] = self.Dp[:-1, :]
+        return DpL, DpR
+
+    def rhs_vx(self, E, v):
+        """The coupled operator of the fully implicit spectral step on ordinates v
+        (Nr * Nvt, Np), composed as the reference's matvec test composes it
+        (test_bte_1d_matvec.py:19-28): Po (Cv + E_x Av) Ps v - Ax v D^T, with the v-space
+        operators of Lmat_mvec (bte_1d3v_solver.py:1051-1055), Ax = adv_x (x) diag(cos theta_j)
+        and the upwinded Chebyshev derivative of step_bte_x's set-up (D_L where cos theta_j >= 0,
+        D_R otherwise, bte_1d3v_solver.py:792-800,832-839); rows on the inflow boundary are 0."""
+        Nr, Nvt, Np = self.Nr, self.Nvt, self.Np
+        u = self.ords_to_sph(v)
+        yv = self.sph_to_ords(self.Cv @ u + E[None, :] * (self.Av @ u)).reshape((Nr, Nvt, Np))
+        DpL, DpR = self._upwinded_d()
+        V = v.reshape((Nr, Nvt, Np))
+        left, right = self.inflow_rows()
+        T = np.zeros_like(V)
+        T[:, left] = V[:, left] @ DpL.T
+        T[:, right] = V[:, right] @ DpR.T
+        yx = np.einsum("rs,j,sjx->rjx", self.op_adv_x, np.cos(self.xp_vt), T)
+        y = yv - yx
+        y[:, left, 0] = 0.0
+        y[:, right, -1] = 0.0
+        return y.reshape((Nr * Nvt, Np))
+
+    def fim_operator(self, E, dt):
+        """The backward-Euler matrix I - dt L of the fully implicit step, assembled with
+        Kronecker products as test_bte_1d_matvec.py:48-83 assembles L (rows of the flattened
+        (r, theta, x) state; inflow rows are identity rows). Returns (matrix, inflow rows)."""
+        Nr, Nvt, Np = self.Nr, self.Nvt, self.Np
+        Ps = np.kron(np.identity(Nr), self.op_po2sh)          # ordinates -> harmonics
+        Po = np.kron(np.identity(Nr), self.op_psh2o)          # harmonics -> ordinates
+        Cop_o, Av_o = Po @ self.Cv @ Ps, Po @ self.Av @ Ps
+        Lv = np.kron(Cop_o, np.identity(Np)) + np.kron(Av_o, np.diag(E))
+        DpL, DpR = self._upwinded_d()
+        left, right = self.inflow_rows()
+        cos = np.cos(self.xp_vt)
+        Lx = np.zeros((Nr * Nvt * Np, Nr * Nvt * Np))
+        for j in range(Nvt):
+            Dj = DpL if j in left else DpR
+            Sj = np.zeros((Nvt, Nvt))
+            Sj[j, j] = cos[j]
+            Lx -= np.kron(np.kron(self.op_adv_x, Sj), Dj)
+        L = Lv + Lx
+        rows = [(r * Nvt + j) * Np + 0 for r in range(Nr) for j in left]
+        rows += [(r * Nvt + j) * Np + Np - 1 for r in range(Nr) for j in right]
+        L[rows, :] = 0.0
+        return np.identity(L.shape[0]) - dt * L, np.array(rows)
+
+    def step_fim(self, E, v, dt):
+        """One fully implicit step: (I - dt L) v_new = v with the inflow values set to 0 (the
+        boundary condition step_bte_x imposes, bte_1d3v_solver.py:936-937), solved directly."""
+        A, rows = self.fim_operator(E, dt)
+        b = np.array(v, dtype=np.float64).reshape(-1).copy()
+        b[rows] = 0.0
+        return np.linalg.solve(A, b).reshape((self.Nr * self.Nvt, self.Np))
+
+    def step_fim_gmres(self, E, v, dt, rtol=1e-10, restart=30, maxiter=600):
+        """The same fully implicit step solved matrix-free, as the reference solves its implicit
+        systems (restarted GMRES, utils.py:1172-1262, here SciPy's), right-preconditioned by the
+        Lie split the GPU step uses: the exact per-point v-space inverse in FP64, then the
+        backward-Euler x-advection over dt. Returns (v_new, iterations); the CPU baseline of
+        the fully implicit 1D3V workload."""
+        import scipy.sparse.linalg as sla
+        Nr, Nvt, Np = self.Nr, self.Nvt, self.Np
+        N = Nr * Nvt * Np
+        left, right = self.inflow_rows()
+        b = np.array(v, dtype=np.float64).reshape((Nr, Nvt, Np)).copy()
+        b[:, left, 0] = 0.0
+        b[:, right, -1] = 0.0
+        n = Nr * self.nsh
+        I = np.identity(n)
+        blocks = [np.linalg.inv(I - dt * (self.Cv + E[x] * self.Av)) for x in range(Np)]
+
+        def pc(r):
+            r = r.reshape((Nr * Nvt, Np))
+            u = self.ords_to_sph(r)
+            z = np.stack([blocks[x] @ u[:, x] for x in range(Np)], axis=1)
+            y = r + self.sph_to_ords(z - u)
+            return self.step_x(y, dt).reshape(-1)
+
+        def mv(x):
+            x = x.reshape((Nr * Nvt, Np))
+            return (x - dt * self.rhs_vx(E, x)).reshape(-1)
+
+        AP = sla.LinearOperator((N, N), matvec=lambda z: mv(pc(z)))
+        its = [0]
+
+        def count(_):
+            its[0] += 1
+        z, info = sla.gmres(AP, b.reshape(-1), rtol=rtol, restart=restart, maxiter=maxiter, callback=count,
+                            callback_type="pr_norm")
+        return pc(z).reshape((Nr * Nvt, Np)), its[0]
 
     def step(self, E, v, dt):
         """Strang split, bte_1d3v_solver.py:1885-1889."""

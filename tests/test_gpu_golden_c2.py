@@ -80,6 +80,24 @@ def test_fp64_against_reference(synthetic_xs, fixture, n_sp, l_max):
 
 @pytest.mark.parametrize("fixture,n_sp,l_max", [("c2_shape_reference.npz", 128, 2),
                                                 ("c5_reduced_reference.npz", 64, 4)])
+def test_fp64_ee_off_against_reference(synthetic_xs, fixture, n_sp, l_max):
+    """The first phase of the driver sequence alone (e-e off, from the Maxwellian) against the
+    reference's e-e-off EDFs."""
+    g = dict(np.load(os.path.join(GOLDEN, fixture)))
+    P = g["ff"].shape[1]
+    s, args = gpu_solver(synthetic_xs, n_sp, l_max, True, P, "fp64")
+    for k in ["n0", "ne", "ns_by_n0", "Tg", "E"]:
+        s.set_boltzmann_parameter(0, k, g[k])
+    args.ee_collisions = 0
+    ff, q = s.solve(0, s.initialize(0, P), ATOL, RTOL, 100, "steady-state", 1e-16, 0.5, 1e-4)
+    err = rel_l2_cols(ff, g["ff_warm"])
+    print("\n%s fp64 e-e off: EDF err %s" % (fixture, np.array2string(err, precision=2)))
+    assert np.all(np.asarray(q["status"]) <= 1)
+    assert np.all(err < 1e-10), err
+
+
+@pytest.mark.parametrize("fixture,n_sp,l_max", [("c2_shape_reference.npz", 128, 2),
+                                                ("c5_reduced_reference.npz", 64, 4)])
 def test_mixed_against_reference(synthetic_xs, fixture, n_sp, l_max):
     g = dict(np.load(os.path.join(GOLDEN, fixture)))
     P = g["ff"].shape[1]
