@@ -94,6 +94,29 @@ def test_preconditioner_matches_the_reference_op_split_step(harness, case):
     assert np.max(np.abs(Y - g["Mu"])) <= 1e-12 * np.max(np.abs(g["Mu"]))
 
 
+def test_preconditioner_with_half_step_sweeps_matches_the_oracle(harness, case):
+    """gmres_pc_vr = 0.5: the reference's preconditioner takes the three sweeps (v_r, v_theta, x)
+    over alpha dt while the collision solve keeps dt (bte_1d3v_solver.py:1819-1860). The core's
+    preconditioner with hstep = 0.5 dt and the full-step collision factors against the oracle's
+    op-split step at alpha = 0.5 (the oracle is pinned to the reference's step at alpha = 1),
+    and it differs from the full-step preconditioner."""
+    from oracle import bte1d_fvm_oracle as F
+    g = case["g"]
+    gs = dict(np.load(os.path.join(HERE, "golden", "fvm_reference.npz")))
+    a = _Args(case)
+    dt = float(g["dt"])
+    Y = {}
+    for alpha in (0.5, 1.0):
+        y = np.zeros_like(g["u"])
+        harness.fvm_host_precond(*a.common, a.p(case["dinv"]), a.p(case["H"]), C.c_double(case["cE"]),
+                                 C.c_double(case["ax"]), C.c_double(alpha * dt), a.p(g["E"]), a.p(g["u"]),
+                                 y.ctypes.data_as(C.POINTER(C.c_double)))
+        Y[alpha] = y
+    ref = F.op_split_step(gs, g["E"], np.asarray(g["u"]).reshape(-1, int(gs["Nx"])), dt, alpha=0.5).reshape(-1)
+    assert np.max(np.abs(Y[0.5].reshape(-1) - ref)) <= 1e-12 * np.max(np.abs(ref))
+    assert np.max(np.abs(Y[0.5] - Y[1.0])) > 1e-6 * np.max(np.abs(Y[1.0]))
+
+
 @pytest.mark.parametrize("restart,pc_mode,alpha", [(30, 0, 1.0), (4, 0, 1.0), (30, 1, 1.0), (4, 1, 1.0), (30, 2, 1.0),
                                                    (30, 0, 0.5)])
 def test_gmres_step_matches_the_reference(harness, case, restart, pc_mode, alpha):
