@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--c5-plain-points", type=int, default=2048,
                     help="points of the plain FP64 run of the config-5 sample (the same points, for a fair ratio)")
     ap.add_argument("--steps-1d", type=int, default=20)
+    ap.add_argument("--steps-fvm", type=int, default=10)
+    ap.add_argument("--no-fvm", action="store_true", help="skip the finite-volume 1D3V leg")
     ap.add_argument("--lu-kernel", type=int, default=0,
                     help="FP32 factorization of the mixed form: 0 library choice, 2 tensor cores, 3 SIMT left-looking")
     return ap.parse_args()
@@ -547,6 +549,89 @@ def bench_1d(a, peaks):
     return out
 
 
+FVM_C4 = dict(L=2.54e-2, V0=100.0, freq=13.56e6, Tg=300.0, p0=1.0, atol=1e-14, rtol=1e-10, gmres_rsrt=30,
+              gmres_rsrt_iter=20, Np=200, Nr=63, Nvt=16, lmax=1, dt=1e-3, ev_max=80.0, ev_extend=0, sp_order=3,
+              spline_qpts=5, Te=4.0, xspace_type=0, vspace_type=0, solver_type="fully_implicit", adaptive_grid=1,
+              pvr=2, pvt=2, px=2, ic_file="")
+
+
+def bench_fvm(a, peaks):
+    """The finite-volume 1D3V fully implicit step (the reference's solver_type "fully_implicit",
+    bte_1d3v_solver.py:1890-2009) at the 1D3V workload's size: 200 upwind x points, the radial
+    cells of 64 B-splines x 5 Gauss points, 16 ordinates; GMRES(30) rtol 1e-10 preconditioned
+    by the op-split step. Its operator (k_fvm_mvec) is one read and one write of the state."""
+    import torch
+    from boltzmann_gb300.bte_1d3v_fvm import bte_1d3v_fvm
+    from boltzmann_gb300.workloads import write_synthetic_lxcat
+    xs = write_synthetic_lxcat()
+    p = dict(FVM_C4, collisions=xs)
+    try:
+        t0 = time.perf_counter()
+        b = bte_1d3v_fvm(p)
+        dt = p["dt"]
+        b.init(dt)
+        t_setup = time.perf_counter() - t0
+        v = b.initial_condition()
+        t = 0.25
+        for _ in range(3):
+            v = b.step(c4_efield(b.xp, t, p), v, None, t, dt)
+            t += dt
+        torch.cuda.synchronize()
+        s = torch.cuda.current_stream()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        its, L0 = [], b.launches()
+        ev[0].record(s)
+        for _ in range(a.steps_fvm):
+            v = b.step(c4_efield(b.xp, t, p), v, None, t, dt)
+            its.append(b.gmres_info["iterations"])
+            t += dt
+        ev[1].record(s)
+        torch.cuda.synchronize()
+        ms = ev[0].elapsed_time(ev[1]) / a.steps_fvm
+        launches = (b.launches() - L0) / a.steps_fvm
+        E = c4_efield(b.xp, t, p)
+        timing = {}
+        for name, fn in (("matvec", lambda: b.rhs_mvec(E, v, dt)),
+                         ("precond", lambda: b.step_op_split(E, v, None, t, dt))):
+            for _ in range(3):
+                fn()
+            ev[0].record(s)
+            for _ in range(30):
+                fn()
+            ev[1].record(s)
+            torch.cuda.synchronize()
+            timing[name] = ev[0].elapsed_time(ev[1]) / 30
+        vh = v.cpu().numpy()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            vh = b.step(c4_efield(b.xp, t, p), vh, None, t, dt).cpu().numpy()
+        e2e_ms = (time.perf_counter() - t0) / 3 * 1e3
+        N = b.dof_vr * b.dof_vt * b.dof_x
+        hbm = peaks.get("hbm_gbs") or 6800.0
+        mv_bytes = 2.0 * N * 8                # state in, result out
+        pc_bytes = 8.0 * N * 8                # collision solve in/out, three sweeps in place, x rows in/out
+        out = {
+            "workload": "1D3V finite-volume fully implicit step: %d upwind x points x %d radial cells x %d ordinates "
+                        "(%d unknowns), stencil orders 2, GMRES(30) rtol 1e-10, op-split preconditioner"
+                        % (b.dof_x, b.dof_vr, b.dof_vt, N),
+            "value": 1e3 / ms, "unit": "steps/s", "ms_per_step": ms, "setup_s": t_setup,
+            "gmres_iterations": {"mean": float(np.mean(its)), "max": int(np.max(its))},
+            "gpu_launches_per_step": launches, "matvec_ms": timing["matvec"], "precond_ms": timing["precond"],
+            "roofline_matvec": {"kernel": "k_fvm_moment + gain GEMM + k_fvm_mvec", "bound": "hbm",
+                                "achieved": mv_bytes / (timing["matvec"] * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+                                "frac": mv_bytes / (timing["matvec"] * 1e-3) / 1e9 / hbm, "alg_bytes": mv_bytes},
+            "roofline_precond": {"kernel": "collision solve + coalesced v_r, v_theta, x sweeps", "bound": "hbm",
+                                 "achieved": pc_bytes / (timing["precond"] * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+                                 "frac": pc_bytes / (timing["precond"] * 1e-3) / 1e9 / hbm, "alg_bytes": pc_bytes},
+            "e2e": {"value": 1e3 / e2e_ms, "unit": "steps/s", "h2d_bytes_per_step": int(vh.nbytes + b.dof_x * 8),
+                    "d2h_bytes_per_step": int(vh.nbytes), "path": "bte_1d3v_fvm.step() with NumPy host arrays"},
+        }
+    finally:
+        os.unlink(xs)
+    return out
+
+
 # the pipe each kernel family runs on: roofline denominators from MEASURED_PEAKS.json
 # (HBM copy GB/s, dense bf16 TFLOP/s). The FP32 factorization runs its trailing updates as
 # tcgen05 kind::tf32 MMAs, whose dense rate is half the bf16 rate; FP64 families run on the
@@ -734,6 +819,7 @@ def main():
         return
     serve = None if (a.no_serve or ws > 1) else serve_bench(a)
     one_d = None if (a.no_1d or ws > 1) else bench_1d(a, peaks)
+    fvm = None if (a.no_fvm or ws > 1) else bench_fvm(a, peaks)
     c5 = None if (a.c5_points <= 0 or ws > 1) else bench_c5(a)
     cpu = None if a.no_cpu else cpu_baseline_run(a)
     st = r["stats"]
@@ -749,7 +835,7 @@ def main():
         "fp64_fallback_points_per_step": st["fp64_fallback_points"] / a.steps,
         "fp64_fallback_reasons": st["fp64_fallback_reasons"],
         "roofline": roofline(st, peaks), "cpu_baseline": cpu, "clocks": r["clocks"],
-        "plain_fp64": r["plain"], "serving": serve, "bte_1d3v": one_d, "c5_sample": c5, "setup_s": r["setup_s"],
+        "plain_fp64": r["plain"], "serving": serve, "bte_1d3v": one_d, "bte_1d3v_fvm": fvm, "c5_sample": c5, "setup_s": r["setup_s"],
         "newton_iters": {"mean": float(np.mean(r["iters"])), "max": int(np.max(r["iters"]))},
         "status_counts": {str(k): int(v) for k, v in zip(*np.unique(r["status"], return_counts=True))},
     }

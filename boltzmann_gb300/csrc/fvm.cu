@@ -7,9 +7,11 @@
 // (k_fvm_moment) and the gain product G m (FP64 GEMM, Nr x Nr by Nr x Nx). The reference
 // multiplies dense (Nr Nvt)^2 collision and advection matrices instead; here the work per
 // value is O(p + Nr), so the operator is one read and one write of v (HBM-bound).
-// Preconditioner: the collision inverse in closed form, (D^-1 (x) I + H (x) 1 w^T) v, fused with
-// the first layout swap (k_fvm_coll_permute), then the library's v_r, v_theta and x sweeps with
-// their layout swaps (sweeps.cu).
+// Preconditioner: the collision inverse in closed form, (D^-1 (x) I + H (x) 1 w^T) v, then the
+// v_r, v_theta and x sweeps in the natural layout: the v_r and v_theta recurrences run one
+// thread per line with the warp's lanes on consecutive x (coalesced), the x recurrence on rows
+// staged in shared memory; the reference (and the drop-in sweeps of sweeps.cu) swap layouts
+// between the sweeps instead.
 // Solver: restarted right-preconditioned GMRES (fvm_core.h), device vectors, FP64.
 // Semi-Lagrangian step (solver_type "sl_implicit", :2024-2027): one kernel interpolates every
 // value at its departure point (k_fvm_sl), then the closed-form collision inverse.
@@ -114,6 +116,84 @@ __global__ void k_fvm_coll_apply(FvmView v, const double* __restrict__ dinv, con
 }
 
 // Y = the semi-Lagrangian advection of V, one thread per value
+// ---- preconditioner sweeps in the natural (Nr, Nvt, Nx) layout --------------------------------
+// One upwind backward-Euler recurrence (I + a h D) o = b per thread along a line of N values
+// spaced `stride` apart, in place. The bands are the sweeps' column-stored ones (lower
+// D[i][i-k] = L[k][i-k], upper D[i][i+k] = R[k][i+k], rawkernel.py:168-375); the last nd - 1
+// outputs of the line stay in registers. Along v_r (stride Nvt Nx) and v_theta (stride Nx)
+// the threads of a warp take consecutive x, so every step is one coalesced 256-byte access:
+// no layout swaps, unlike the reference's sweeps on permuted copies.
+constexpr int SW_NDMAX = 4;
+__device__ inline void fvm_sweep_line(const double* __restrict__ L, const double* __restrict__ R, int nd, int N,
+                                      double ad, bool ltr, double* __restrict__ v, long long stride) {
+    double prev[SW_NDMAX - 1];
+#pragma unroll
+    for (int k = 0; k < SW_NDMAX - 1; ++k) prev[k] = 0.0;
+    const double* B = ltr ? L : R;
+    for (int step = 0; step < N; ++step) {
+        const int i = ltr ? step : N - 1 - step;
+        double sacc = 0.0;
+#pragma unroll
+        for (int k = 1; k < SW_NDMAX; ++k)
+            if (k < nd && step >= k) sacc += __ldg(B + (size_t)k * N + (ltr ? i - k : i + k)) * prev[k - 1];
+        const double o = (v[(long long)i * stride] - ad * sacc) / (1.0 + ad * __ldg(B + i));
+#pragma unroll
+        for (int k = SW_NDMAX - 2; k > 0; --k) prev[k] = prev[k - 1];
+        prev[0] = o;
+        v[(long long)i * stride] = o;
+    }
+}
+
+// v_r sweep: line (j, x), a = -aE[x] cos(theta_j), left to right when a >= 0 (rawkernel.py:168-230)
+__global__ void k_fvm_sweep_vr(FvmView v, const double* __restrict__ aE, double h, double* __restrict__ V) {
+    const int line = blockIdx.x * blockDim.x + threadIdx.x;
+    if (line >= v.Nvt * v.Nx) return;
+    const int j = line / v.Nx, x = line % v.Nx;
+    const double a = -aE[x] * v.cos_t[j];
+    fvm_sweep_line(v.vrL, v.vrR, v.ndr, v.Nr, a * h, a >= 0.0, V + (size_t)j * v.Nx + x, (long long)v.Nvt * v.Nx);
+}
+
+// v_theta sweep: line (r, x), a = aE[x] / v_r, left to right when -a >= 0 (rawkernel.py:232-296)
+__global__ void k_fvm_sweep_vt(FvmView v, const double* __restrict__ aE, double h, double* __restrict__ V) {
+    const int line = blockIdx.x * blockDim.x + threadIdx.x;
+    if (line >= v.Nr * v.Nx) return;
+    const int r = line / v.Nx, x = line % v.Nx;
+    const double a = aE[x] / v.vr[r];
+    fvm_sweep_line(v.vtL, v.vtR, v.ndt, v.Nvt, a * h, -a >= 0.0, V + (size_t)r * v.Nvt * v.Nx + x, (long long)v.Nx);
+}
+
+// x sweep with the inflow values zeroed first: line (r, j) is a contiguous row of Nx values;
+// a CTA stages XT_L consecutive rows (one contiguous block) in shared memory with coalesced
+// loads, sweeps each row in shared memory (row pitch Nx + 1 against bank conflicts) and
+// writes the block back coalesced. a = ax v_r cos(theta_j), left to right when a >= 0
+// (rawkernel.py:298-375).
+constexpr int XT_L = 64;
+__global__ void __launch_bounds__(XT_L) k_fvm_sweep_x(FvmView v, const double* __restrict__ axvr, double h,
+                                                      const double* __restrict__ B, double* __restrict__ Y) {
+    extern __shared__ double rows[];  // [XT_L][Nx + 1]
+    const int Nx = v.Nx, pitch = Nx + 1;
+    const int nlines = v.Nr * v.Nvt;
+    const int l0 = blockIdx.x * XT_L;
+    const int nl = min(XT_L, nlines - l0);
+    const double* src = B + (size_t)l0 * Nx;
+    for (int e = threadIdx.x; e < nl * Nx; e += blockDim.x) {
+        const int l = e / Nx, x = e % Nx;
+        const int j = (l0 + l) % v.Nvt;
+        const bool inflow = v.north[j] ? (x == 0) : (x == Nx - 1);
+        rows[l * pitch + x] = inflow ? 0.0 : src[e];
+    }
+    __syncthreads();
+    if (threadIdx.x < nl) {
+        const int line = l0 + threadIdx.x;
+        const int r = line / v.Nvt, j = line % v.Nvt;
+        const double a = axvr[r] * v.cos_t[j];
+        fvm_sweep_line(v.xL, v.xR, v.ndx, Nx, a * h, a >= 0.0, rows + threadIdx.x * pitch, 1);
+    }
+    __syncthreads();
+    double* dst = Y + (size_t)l0 * Nx;
+    for (int e = threadIdx.x; e < nl * Nx; e += blockDim.x) dst[e] = rows[(e / Nx) * pitch + e % Nx];
+}
+
 __global__ void k_fvm_sl(FvmSl sl, const double* __restrict__ E, const double* __restrict__ V, double* __restrict__ Y) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t n = (size_t)sl.Nr * sl.Nvt * sl.Nx;
@@ -218,21 +298,38 @@ int fvm_precond(bte_fvm* h, double hstep, const double* X, double* Y, cudaStream
     k_fvm_moment<<<fblocks(nrx), FT, 0, s>>>(v, X, h->M);
     if (int rc = launched("k_fvm_moment")) return rc;
     if (int rc = sweep_rc(bte_dgemm_nn(Nr, Nx, Nr, h->H, Nr, h->M, Nx, h->T, Nx, s), "collision inverse")) return rc;
-    k_fvm_coll_permute<<<fblocks(h->N), FT, 0, s>>>(v, h->dinv, h->T, X, h->A);   // (Nx, Nvt, Nr)
-    if (int rc = launched("k_fvm_coll_permute")) return rc;
-    int rc = sweep_rc(bte_adv_be_sweep(0, h->vrL, h->vrR, h->aE, h->cos_t, hstep, h->A, h->Bf, h->ndr, Nr, Nvt, Nx, s),
-                      "v_r sweep");
-    if (!rc) rc = sweep_rc(bte_permute3(Nx, Nvt, Nr, 0, 2, 1, h->Bf, h->A, s), "layout");   // (Nx, Nr, Nvt)
-    if (!rc)
-        rc = sweep_rc(bte_adv_be_sweep(1, h->vtL, h->vtR, h->aE, h->vr, hstep, h->A, h->Bf, h->ndt, Nr, Nvt, Nx, s),
-                      "v_theta sweep");
-    if (!rc) rc = sweep_rc(bte_permute3(Nx, Nr, Nvt, 1, 2, 0, h->Bf, h->A, s), "layout");   // (Nr, Nvt, Nx)
-    if (!rc) rc = sweep_rc(bte_fvm_inflow_zero(Nr, Nvt, Nx, h->vt, h->A, s), "inflow");
-    if (!rc)
-        rc = sweep_rc(bte_adv_be_sweep(2, h->xL, h->xR, h->axvr, h->cos_t, hstep, h->A, Y, h->ndx, Nr, Nvt, Nx, s),
-                      "x sweep");
-    h->launches += 10;
-    return rc;
+    const size_t xsm = (size_t)XT_L * (Nx + 1) * sizeof(double);
+    if (h->ndr > SW_NDMAX || h->ndt > SW_NDMAX || h->ndx > SW_NDMAX || xsm > 200 * 1024) {
+        // stencils wider than the register recurrence or x lines longer than the staged rows:
+        // the drop-in sweeps on permuted copies
+        k_fvm_coll_permute<<<fblocks(h->N), FT, 0, s>>>(v, h->dinv, h->T, X, h->A);   // (Nx, Nvt, Nr)
+        if (int rc = launched("k_fvm_coll_permute")) return rc;
+        int rc = sweep_rc(bte_adv_be_sweep(0, h->vrL, h->vrR, h->aE, h->cos_t, hstep, h->A, h->Bf, h->ndr, Nr, Nvt, Nx, s),
+                          "v_r sweep");
+        if (!rc) rc = sweep_rc(bte_permute3(Nx, Nvt, Nr, 0, 2, 1, h->Bf, h->A, s), "layout");   // (Nx, Nr, Nvt)
+        if (!rc)
+            rc = sweep_rc(bte_adv_be_sweep(1, h->vtL, h->vtR, h->aE, h->vr, hstep, h->A, h->Bf, h->ndt, Nr, Nvt, Nx, s),
+                          "v_theta sweep");
+        if (!rc) rc = sweep_rc(bte_permute3(Nx, Nr, Nvt, 1, 2, 0, h->Bf, h->A, s), "layout");   // (Nr, Nvt, Nx)
+        if (!rc) rc = sweep_rc(bte_fvm_inflow_zero(Nr, Nvt, Nx, h->vt, h->A, s), "inflow");
+        if (!rc)
+            rc = sweep_rc(bte_adv_be_sweep(2, h->xL, h->xR, h->axvr, h->cos_t, hstep, h->A, Y, h->ndx, Nr, Nvt, Nx, s),
+                          "x sweep");
+        h->launches += 10;
+        return rc;
+    }
+    k_fvm_coll_apply<<<fblocks(h->N), FT, 0, s>>>(v, h->dinv, h->T, X, h->A);   // natural layout
+    if (int rc = launched("k_fvm_coll_apply")) return rc;
+    // the three sweeps in place on the natural layout, coalesced (no layout swaps)
+    k_fvm_sweep_vr<<<fblocks((size_t)Nvt * Nx), FT, 0, s>>>(v, h->aE, hstep, h->A);
+    if (int rc = launched("k_fvm_sweep_vr")) return rc;
+    k_fvm_sweep_vt<<<fblocks((size_t)Nr * Nx), FT, 0, s>>>(v, h->aE, hstep, h->A);
+    if (int rc = launched("k_fvm_sweep_vt")) return rc;
+    if (bte_raise_smem_limit((const void*)k_fvm_sweep_x, xsm) != cudaSuccess)
+        return fvm_fail(BTE_ERR_ARG, "x lines too long for the shared-memory sweep");
+    k_fvm_sweep_x<<<(unsigned)((Nr * Nvt + XT_L - 1) / XT_L), XT_L, xsm, s>>>(v, h->axvr, hstep, h->A, Y);
+    h->launches += 6;
+    return launched("k_fvm_sweep_x");
 }
 
 // aE = cE E on the device, axvr = ax v_r
