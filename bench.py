@@ -779,6 +779,11 @@ def cpu_baseline_run(a, cap_s=600.0):
     return run.summary()
 
 
+def _autotune_report():
+    from boltzmann_gb300 import autotune
+    return {k: v for k, v in autotune.choices().items()}
+
+
 def main():
     a = parse()
     rank, ws = dist_init(a.gpus)
@@ -837,6 +842,7 @@ def main():
         "roofline": roofline(st, peaks), "cpu_baseline": cpu, "clocks": r["clocks"],
         "plain_fp64": r["plain"], "serving": serve, "bte_1d3v": one_d, "bte_1d3v_fvm": fvm, "c5_sample": c5, "setup_s": r["setup_s"],
         "newton_iters": {"mean": float(np.mean(r["iters"])), "max": int(np.max(r["iters"]))},
+        "lu_autotune": _autotune_report(),
         "status_counts": {str(k): int(v) for k, v in zip(*np.unique(r["status"], return_counts=True))},
     }
     print(json.dumps(line))

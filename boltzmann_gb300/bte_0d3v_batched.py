@@ -14,6 +14,9 @@ Differences a caller can observe:
     `qoi["status"]` / `qoi["iters"]` report each point's outcome instead of printing;
   * `args.precision` selects "fp64" (plain, default) or "mixed" (FP32 Jacobian
     factorizations against the FP64 residual);
+  * `args.lu_kernel` picks the mixed form's FP32 factorization kernel (bte_solve_opts); left at
+    0 with `args.autotune` on (the default), boltzmann_gb300.autotune times the candidates
+    for the grid's size once and the fastest is used;
   * `args.krylov` (mixed form) chooses when a point whose FP64 refinement stalls gets
     GMRES on its FP32 factors before it goes to FP64: 0 for bordered sizes above 512
     (default), 1 always, 2 for every point (diagnostics), -1 never;
@@ -519,6 +522,15 @@ class bte_0d3v_batched:
             return self.transient_solve(grid_idx, f0, atol, rtol, max_iter)
         raise NotImplementedError(solver_type)
 
+    def _lu_kernel(self, grid_idx):
+        """bte_solve_opts.lu_kernel: args.lu_kernel when set, else (mixed form, args.autotune on,
+        the default) the autotuner's choice for this grid's bordered size."""
+        k = int(getattr(self._args, "lu_kernel", 0) or 0)
+        if k or self._precision() != _lib.PREC_MIXED or not int(getattr(self._args, "autotune", 1)):
+            return k
+        from . import autotune
+        return autotune.lu_kernel_for(self._grid_info[grid_idx]["n"] + 1, device=self._dev_id)
+
     def _precision(self):
         p = str(getattr(self._args, "precision", "fp64")).lower()
         if p not in ("fp64", "mixed"):
@@ -544,7 +556,7 @@ class bte_0d3v_batched:
                               ee=int(getattr(self._args, "ee_collisions", 0)), precision=self._precision(),
                               refine=int(getattr(self._args, "refine", 4)),
                               krylov=int(getattr(self._args, "krylov", 0)),
-                              lu_kernel=int(getattr(self._args, "lu_kernel", 0)))
+                              lu_kernel=self._lu_kernel(grid_idx))
         stream = torch.cuda.current_stream().cuda_stream
         _lib.check(_lib.load().bte_solve_steady(self._grid[grid_idx], n_pts, _ptr(n0), _ptr(ne), _ptr(ns), _ptr(Tg),
                                                 _ptr(E), _ptr(f), _ptr(status), _ptr(iters), C.byref(opts),

@@ -141,8 +141,8 @@ __device__ inline void put_split4(unsigned char* sm, int m, int k, float a, floa
     *reinterpret_cast<float4*>(sm + TC_TILE_BYTES + o) = lo;
 }
 
-template <int ROWS>
-__global__ void __launch_bounds__(TC_NT, 2)
+template <int ROWS, int OCC>
+__global__ void __launch_bounds__(TC_NT, OCC)
 k_lu_tc(int N, int NC, float* __restrict__ A, int ld, long long stride, int32_t* __restrict__ perm_out,
         int32_t* __restrict__ info, int vec4) {
     extern __shared__ unsigned char smraw[];
@@ -440,14 +440,14 @@ k_lu_tc(int N, int NC, float* __restrict__ A, int ld, long long stride, int32_t*
     if (wid == 0) tmem_dealloc(tbase, TC_TMEM_COLS);
 }
 
-template <int ROWS>
+template <int ROWS, int OCC>
 cudaError_t launch_tc(int P, int N, int NC, float* A, int ld, long long stride, int32_t* piv, int32_t* info,
                       cudaStream_t s) {
     const size_t sm = tc_smem_bytes(N);
-    cudaError_t e = bte_raise_smem_limit((const void*)k_lu_tc<ROWS>, sm);
+    cudaError_t e = bte_raise_smem_limit((const void*)k_lu_tc<ROWS, OCC>, sm);
     if (e != cudaSuccess) return e;
     const int vec4 = (ld % 4 == 0 && stride % 4 == 0 && ((uintptr_t)A & 15) == 0) ? 1 : 0;
-    k_lu_tc<ROWS><<<P, TC_NT, sm, s>>>(N, NC, A, ld, stride, piv, info, vec4);
+    k_lu_tc<ROWS, OCC><<<P, TC_NT, sm, s>>>(N, NC, A, ld, stride, piv, info, vec4);
     return cudaGetLastError();
 }
 
@@ -456,11 +456,17 @@ cudaError_t launch_tc(int P, int N, int NC, float* A, int ld, long long stride, 
 // largest N the tensor-core kernel takes (its panel is two 32-column rows per thread)
 int bte_lu_tc_max_n() { return 2 * TC_NT; }
 
+// occupancy: 2 = two CTAs per SM (the registers of two, 2 x 128 tensor-memory columns), 1 = one
+// CTA per SM (half the matrices in flight, so their trailing updates stay in L2)
 cudaError_t bte_lu_factor_tc(int P, int N, int NC, float* A, int ld, long long stride, int32_t* piv, int32_t* info,
-                             cudaStream_t s) {
+                             cudaStream_t s, int occupancy) {
     if (P <= 0) return cudaSuccess;
     if (N < 1 || N > 2 * TC_NT || NC < N || NC > N + 1 || ld < NC) return cudaErrorInvalidValue;
     if ((long long)N * ld >= (1ll << 31)) return cudaErrorInvalidValue;  // row offsets are 32-bit
-    if (N <= TC_NT) return launch_tc<1>(P, N, NC, A, ld, stride, piv, info, s);
-    return launch_tc<2>(P, N, NC, A, ld, stride, piv, info, s);
+    if (occupancy == 1) {
+        if (N <= TC_NT) return launch_tc<1, 1>(P, N, NC, A, ld, stride, piv, info, s);
+        return launch_tc<2, 1>(P, N, NC, A, ld, stride, piv, info, s);
+    }
+    if (N <= TC_NT) return launch_tc<1, 2>(P, N, NC, A, ld, stride, piv, info, s);
+    return launch_tc<2, 2>(P, N, NC, A, ld, stride, piv, info, s);
 }

@@ -1566,8 +1566,8 @@ static cudaError_t gmres_refine(SolveCtx& c, Lane& L, int nact, bool all) {
 // FP32 factorization kernel for a Newton system of size N (bte_solve_opts.lu_kernel): a
 // kernel that does not take N falls back to the library's choice
 static int lu_kernel_for(int requested, int N) {
-    if ((requested == 2 || requested == 3) && N > 512) return 0;
-    return (requested >= 0 && requested <= 3) ? requested : 0;
+    if ((requested == 2 || requested == 3 || requested == 4) && N > 512) return 0;
+    return (requested >= 0 && requested <= 4) ? requested : 0;
 }
 
 // One Newton iteration (Jacobian, factorization, step, refinement, line search, acceptance,

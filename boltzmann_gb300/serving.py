@@ -171,11 +171,14 @@ class BteServer:
     `backend_factory(key)` may replace the CUDA engine (used by host-only tests). refine and
     krylov are the mixed form's refinement options (bte_solve_opts: FP64 refinement passes;
     GMRES on the FP32 factors for stalled points, 0 = bordered sizes above 512, -1 = never).
+    autotune (mixed form): each grid's FP32 factorization kernel is the one
+    boltzmann_gb300.autotune measured fastest for its bordered size.
     """
 
     def __init__(self, lxcat_file, grids, precision="mixed", hbm_budget_bytes=8 << 30, capacity=1024,
                  fp64_capacity=64, atol=1e-20, rtol=1e-14, max_iter=100, alpha_min=1e-16, alpha_rho=0.5,
-                 line_search_c=1e-4, refine=4, ev_max=80.0, Te=4.0, device=0, backend_factory=None, krylov=0):
+                 line_search_c=1e-4, refine=4, ev_max=80.0, Te=4.0, device=0, backend_factory=None, krylov=0,
+                 autotune=True):
         self.budget = int(hbm_budget_bytes)
         self.used = 0
         self.peak_used = 0
@@ -209,7 +212,12 @@ class BteServer:
                                   precision=_lib.PREC_MIXED if precision == "mixed" else _lib.PREC_FP64,
                                   refine=int(refine), krylov=int(krylov))
             for i, k in enumerate(keys):
-                be = EngineBackend(s._grid[i], s._grid_info[i], capacity, fp64_capacity, opts, device)
+                o = opts
+                if precision == "mixed" and autotune:
+                    from . import autotune as at
+                    o = _lib.SolveOpts.from_buffer_copy(opts)
+                    o.lu_kernel = at.lu_kernel_for(s._grid_info[i]["n"] + 1, device=device)
+                be = EngineBackend(s._grid[i], s._grid_info[i], capacity, fp64_capacity, o, device)
                 self._workers[k] = _Worker(k, be)
         else:
             for k in keys:

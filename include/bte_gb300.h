@@ -78,10 +78,11 @@ typedef struct {
                                      reference, which inverts in FP64                         */
     int lu_kernel;                /* mixed form: FP32 factorization of the Newton systems.
                                      0: the library's choice; 2: split-TF32 trailing updates
-                                     on the tensor cores (bordered sizes n + 1 <= 512);
-                                     3: SIMT left-looking (n + 1 <= 512); 1: SIMT
-                                     right-looking. Sizes a kernel does not take fall back to
-                                     the library's choice                                     */
+                                     on the tensor cores (bordered sizes n + 1 <= 512), two
+                                     CTAs per SM; 4: the same with one CTA per SM; 3: SIMT
+                                     left-looking (n + 1 <= 512); 1: SIMT right-looking.
+                                     Sizes a kernel does not take fall back to the library's
+                                     choice                                                   */
     int reserved[3];
 } bte_solve_opts;
 
@@ -206,7 +207,8 @@ int bte_lu_factor(int dtype, int P, int N, void* A, int ld, long long stride, in
 /* As bte_lu_factor with an explicit kernel: 0 = automatic (FP32: tensor-core kernel for
  * N <= 512, right-looking above; FP64: right-looking),
  * 1 = right-looking for every N, 2 = FP32 only, N <= 512: trailing updates on the tcgen05
- * tensor cores in split TF32 (FP32-accurate factors), 3 = left-looking (N <= 512).
+ * tensor cores in split TF32 (FP32-accurate factors), 3 = left-looking (N <= 512),
+ * 4 = as 2 with one CTA per SM instead of two (fewer matrices in flight, kept in L2).
  * No counterpart in the reference; used to cross-check the factorizations. */
 int bte_lu_factor_ex(int dtype, int P, int N, void* A, int ld, long long stride, int32_t* piv, int32_t* info,
                      int kernel, void* stream);

@@ -9,9 +9,9 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("N", [1, 7, 31, 64, 129, 385, 600, 1281])
 @pytest.mark.parametrize("dtype", ["f64", "f32"])
-@pytest.mark.parametrize("kernel", [0, 1, 2], ids=["auto", "right", "tc"])
+@pytest.mark.parametrize("kernel", [0, 1, 2, 4], ids=["auto", "right", "tc", "tc1"])
 def test_lu_factor_solve(N, dtype, kernel):
-    if kernel == 2 and (dtype == "f64" or N > 512):
+    if kernel in (2, 4) and (dtype == "f64" or N > 512):
         pytest.skip("the tensor-core factorization is FP32 with N <= 512")
     import torch
     from boltzmann_gb300 import _lib
@@ -97,7 +97,7 @@ def test_lu_negative_zero_is_not_a_pivot(dtype, N):
 
 
 @pytest.mark.parametrize("N", [33, 128, 385, 512])
-@pytest.mark.parametrize("kernel", [0, 2], ids=["auto", "tc"])
+@pytest.mark.parametrize("kernel", [0, 2, 4], ids=["auto", "tc", "tc1"])
 def test_lu_padded_rows_against_fp64(N, kernel):
     """FP32 factors with 16-byte aligned rows (the Newton solver's layout, vectorised path of
     the tensor-core kernel): backward error at FP32 level, and the tensor-core factors'
@@ -130,3 +130,18 @@ def test_lu_padded_rows_against_fp64(N, kernel):
                                            + np.linalg.norm(bd, axis=1))
     eps = np.finfo(np.float32).eps
     assert np.max(berr) < 2 * N * eps, (berr, N * eps)
+
+
+def test_autotuner_picks_a_measured_kernel(tmp_path, monkeypatch):
+    """The autotuner times every FP32 candidate for a size, keeps the fastest, and caches the
+    choice on disk; a second call reads it back without timing."""
+    from boltzmann_gb300 import autotune
+    monkeypatch.setenv("BOLTZMANN_GB300_CACHE", str(tmp_path))
+    monkeypatch.setattr(autotune, "_mem", {})
+    rec = autotune.tune_lu(129, P=256)
+    assert rec["kernel"] in autotune.CANDIDATES_SMALL
+    assert rec["ms"][str(rec["kernel"])] == min(rec["ms"].values())
+    assert (tmp_path / "lu_autotune.json").exists()
+    monkeypatch.setattr(autotune, "_mem", {})
+    monkeypatch.setattr(autotune, "time_lu", lambda *a, **k: pytest.fail("timed again"))
+    assert autotune.tune_lu(129)["kernel"] == rec["kernel"]
