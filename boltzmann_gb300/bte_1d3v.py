@@ -16,9 +16,12 @@ Counterpart of the spectral path of the reference's `bte_1d3v`
 
 Differences from the reference, by design: the v-step's GMRES is preconditioned with each
 point's own block (I - dt (Cv + E_x Av))^-1 factored in FP32, where the reference uses the
-inverse of the nearest of `num_pc_ops` E values; the x-step solves its backward-Euler systems
-with LU factors, where the reference multiplies by their explicit inverses. Both reach the
-same solution to the solver tolerance. Only the BE Chebyshev x-space and the spectral v-space
+inverse of the nearest of `num_pc_ops` E values (the parameter is read and ignored: the E-binned
+inverses are not built, :1333-1344, :889-910, and the exact blocks take their place; GMRES then
+converges in a few iterations instead of hundreds, to the same solution within the solver
+tolerance). With `solver_type = "fully_implicit"` the step is one backward-Euler step of the
+coupled v-space and x-advection operator (`step_fim`), which the reference provides only for
+the finite-volume v-space (:1891). Only the BE Chebyshev x-space and the spectral v-space
 (the reference's `xspace_type = 1`, `vspace_type = 1`) are provided.
 """
 from __future__ import annotations
@@ -229,8 +232,9 @@ class bte_1d3v:
 
     # ------------------------------------------------------------------ reference interface
     def init(self, dt):
-        """The reference's init(dt) (:1333-1344) builds the preconditioner matrices; here the
-        per-point blocks are factored inside each v-step, so only dt is recorded."""
+        """The reference's init(dt) (:1333-1344) builds num_pc_ops E-binned preconditioner
+        inverses; here each point's exact block is factored inside each v-step instead
+        (num_pc_ops is ignored), so only dt is recorded."""
         self.params.dt = dt
 
     def ords_to_sph(self, x):
