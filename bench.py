@@ -410,7 +410,14 @@ def bench_c5(a):
         ffp = ffp.cpu().numpy()
         stp = qp["status"].cpu().numpy()
         ok = (stm[:m] <= 1) & (stp <= 1)
-        err = (np.linalg.norm(ffm[:, :m] - ffp, axis=0) / np.linalg.norm(ffp, axis=0))[ok]
+        err_all = np.linalg.norm(ffm[:, :m] - ffp, axis=0) / np.linalg.norm(ffp, axis=0)
+        err = err_all[ok]
+        rem, rep = q["rel_error"].cpu().numpy()[:m], qp["rel_error"].cpu().numpy()
+        worst = [int(i) for i in np.argsort(np.where(ok, err_all, -1.0))[-5:][::-1]]
+        worst = [{"point": i, "EbyN_Td": float(sub["EbyN"][i]), "ion_deg": float(sub["ne"][i] / sub["n0"][i]),
+                  "err": float(err_all[i]), "rel_error_mixed": float(rem[i]), "rel_error_fp64": float(rep[i]),
+                  "iters_mixed": int(q["iters"].cpu().numpy()[i]), "iters_fp64": int(qp["iters"].cpu().numpy()[i])}
+                 for i in worst]
         del sp
         torch.cuda.empty_cache()
     finally:
@@ -424,7 +431,10 @@ def bench_c5(a):
             "plain_fp64": {"points": m, "value": m / (pms / 1e3), "ms_per_step": pms,
                            "edf_rel_err_mixed_vs_fp64": {"max": float(err.max()) if err.size else None,
                                                          "p50": float(np.median(err)) if err.size else None,
-                                                         "points_compared": int(err.size)}}}
+                                                         "p99": float(np.percentile(err, 99)) if err.size else None,
+                                                         "points_above_1e-8": int(np.sum(err > 1e-8)),
+                                                         "points_compared": int(err.size),
+                                                         "worst_points": worst}}}
 
 
 C4 = dict(L=2.54e-2, V0=100.0, freq=13.56e6, Tg=300.0, p0=1.0, atol=1e-14, rtol=1e-10, gmres_rsrt=30,
@@ -483,21 +493,26 @@ def bench_1d(a, peaks):
         ev[1].record(s)
         torch.cuda.synchronize()
         mv_ms = ev[0].elapsed_time(ev[1]) / nmv
-        # the Strang split on the same state (x over dt/2, v over dt, x over dt/2)
+        # the Strang split on the same state (x over dt/2, v over dt, x over dt/2), on its own
+        # solver (the x-step keeps the factors of one step size)
+        bs = bte_1d3v(dict(C4, collisions=xs))
+        for _ in range(2):
+            bs.step(c4_efield(bs.xp, t, p), v, None, t, dt)
         tx = tv = 0.0
         for _ in range(5):
-            E = c4_efield(b.xp, t, p)
+            E = c4_efield(bs.xp, t, p)
             ev[0].record(s)
-            v1 = b.step_bte_x(v, t, 0.5 * dt)
+            v1 = bs.step_bte_x(v, t, 0.5 * dt)
             ev[1].record(s)
-            v2 = b.step_bte_v(E, v1, None, t, dt)
+            v2 = bs.step_bte_v(E, v1, None, t, dt)
             ev[2].record(s)
-            b.step_bte_x(v2, t, 0.5 * dt)
+            bs.step_bte_x(v2, t, 0.5 * dt)
             ev[3].record(s)
             torch.cuda.synchronize()
             tx += ev[0].elapsed_time(ev[1]) + ev[2].elapsed_time(ev[3])
             tv += ev[1].elapsed_time(ev[2])
         tx, tv = tx / 5, tv / 5
+        del bs
         # end to end through the public API with host arrays
         vh = v.cpu().numpy()
         torch.cuda.synchronize()
@@ -770,13 +785,51 @@ class CpuReferenceRun:
                 "seconds": sec, "samples": self.done}
 
 
-def cpu_baseline_run(a, cap_s=600.0):
-    """cpu_baseline of the GPU arm: the CPU reference run until its first sample completes."""
-    run = CpuReferenceRun(a, a.cpu_points)
+# Newton iterations of the reference's batch-global loop on the cpu_baseline sample (the first
+# 4 points of the seeded c2 workload), measured by running it to its stop criterion (the
+# reference arm, --impl reference, does so every time): e-e off converges after 83 iterations,
+# e-e on runs to the 100-iteration cap.
+CPU_SAMPLE_ITERS = {(128, 2, 4): (83, 100)}
+
+
+def cpu_baseline_run(a, iters_per_phase=3):
+    """cpu_baseline of the GPU arm, a bounded sample (the whole solve of the sample takes about
+    ten minutes on the GPU machine's host; the reference arm runs it): `iters_per_phase` Newton
+    iterations of each phase of the same 4-point sample, timed, and scaled by the sample's
+    measured iteration counts (CPU_SAMPLE_ITERS)."""
+    import multiprocessing
+    from oracle import bte_oracle as O
+    from boltzmann_gb300.workloads import write_synthetic_lxcat, batch_parameters, EV_MAX, TE_NORM
+    counts = CPU_SAMPLE_ITERS.get((a.n_sp, a.l_max, a.cpu_points))
+    if counts is None:
+        return CpuReferenceRun(a, a.cpu_points).summary() | {"note": "no measured iteration counts for this sample"}
+    xs = write_synthetic_lxcat()
     t0 = time.perf_counter()
-    while not run.done and time.perf_counter() - t0 < cap_s:
-        run.run_slice(5.0)
-    return run.summary()
+    try:
+        ops = O.Operators(O.processes_from_lxcat(xs), EV_MAX, TE_NORM, a.n_sp, a.l_max, ee=True)
+    finally:
+        os.unlink(xs)
+    t_setup = time.perf_counter() - t0
+    prm = batch_parameters(a.n_pts, a.seed)
+    sl = slice(0, a.cpu_points)
+    P = O.Params(prm["n0"][sl], prm["ne"][sl], prm["Tg"][sl], prm["E"][sl], prm["ns_by_n0"][:, sl])
+    f0 = O.maxwellian_initial(ops, a.cpu_points)
+    per_iter = []
+    for ee in (False, True):
+        gen = O.steady_state_iterations(ops, P, f0, ATOL, RTOL, MAXIT, ee, ALPHA_MIN, ALPHA_RHO, LS_C)
+        next(gen)  # the first iteration includes the closures' set-up
+        t1 = time.perf_counter()
+        for _ in range(iters_per_phase):
+            next(gen)
+        per_iter.append((time.perf_counter() - t1) / iters_per_phase)
+    sec = per_iter[0] * counts[0] + per_iter[1] * counts[1]
+    return {"value": a.cpu_points / sec, "unit": UNIT, "cores": multiprocessing.cpu_count(), "kind": "port",
+            "sample": "%d points of the seeded c2 workload: %d Newton iterations of each phase (e-e off, e-e on) of "
+                      "the oracle port of bte_0d3v_batched (NumPy, OpenBLAS on all host threads) timed, %.2f s and "
+                      "%.2f s per iteration, scaled by the sample's measured iteration counts %s (the reference arm "
+                      "runs the sample to its stop criterion); operator set-up %.1f s not timed"
+                      % (a.cpu_points, iters_per_phase, per_iter[0], per_iter[1], list(counts), t_setup),
+            "seconds_per_iteration": per_iter, "iterations": list(counts)}
 
 
 def _autotune_report():
