@@ -4,6 +4,7 @@ For a bordered system size N the library has several FP32 LU kernels (`bte_lu_fa
   2  split-TF32 trailing updates on the tcgen05 tensor cores, two CTAs per SM;
   4  the same kernel with one CTA per SM (half the matrices in flight, so that their trailing
      matrices stay in L2);
+  5  the same kernel with 128 threads per CTA (4 warps share the per-column pivot search);
   3  the left-looking SIMT kernel (blocks held in registers);
   1  the right-looking SIMT kernel (any N; the only choice above N = 512).
 `tune_lu(N)` times every candidate on seeded synthetic systems of that size (diagonally shifted
@@ -22,7 +23,7 @@ import threading
 
 from . import _lib
 
-CANDIDATES_SMALL = (2, 4, 3, 1)
+CANDIDATES_SMALL = (2, 4, 5, 3, 1)
 CANDIDATES_LARGE = (1,)
 _mem: dict = {}
 _lock = threading.Lock()

@@ -278,7 +278,7 @@ k_fim_dx(int Nlines, int Nvt, int Nx, const double* __restrict__ DT, const int8_
 //   Y = V - dt (P_sh2o (Cv + E_x Av) P_o2sh V - cos(theta_j) adv_x T)
 // (T = the x-derivative lines of k_fim_dx; Cv, Av carry tau), with identity rows on the inflow
 // boundary. One CTA per FC_X consecutive x points; V, T, adv_x staged in shared memory.
-constexpr int FC_X = 4;
+constexpr int FC_X = 1;   // one x point per CTA: Nx CTAs (the radial mixing dominates)
 __global__ void __launch_bounds__(256)
 k_fim_combine(int Nr, int Nvt, int nsh, int Nx, double dt, const double* __restrict__ Ps,
               const double* __restrict__ Po, const double* __restrict__ CvT, const double* __restrict__ AvT,

@@ -124,19 +124,29 @@ __global__ void k_fvm_coll_apply(FvmView v, const double* __restrict__ dinv, con
 // the threads of a warp take consecutive x, so every step is one coalesced 256-byte access:
 // no layout swaps, unlike the reference's sweeps on permuted copies.
 constexpr int SW_NDMAX = 4;
+constexpr int SW_PF = 4;   // right-hand sides loaded ahead of the recurrence
 __device__ inline void fvm_sweep_line(const double* __restrict__ L, const double* __restrict__ R, int nd, int N,
                                       double ad, bool ltr, double* __restrict__ v, long long stride) {
     double prev[SW_NDMAX - 1];
 #pragma unroll
     for (int k = 0; k < SW_NDMAX - 1; ++k) prev[k] = 0.0;
     const double* B = ltr ? L : R;
+    // the loads of b do not depend on the recurrence: keep SW_PF of them in flight
+    double pf[SW_PF];
+#pragma unroll
+    for (int q = 0; q < SW_PF; ++q) pf[q] = (q < N) ? v[(long long)(ltr ? q : N - 1 - q) * stride] : 0.0;
     for (int step = 0; step < N; ++step) {
         const int i = ltr ? step : N - 1 - step;
+        const double bi = pf[0];
+#pragma unroll
+        for (int q = 0; q < SW_PF - 1; ++q) pf[q] = pf[q + 1];
+        const int nxt = step + SW_PF;
+        pf[SW_PF - 1] = (nxt < N) ? v[(long long)(ltr ? nxt : N - 1 - nxt) * stride] : 0.0;
         double sacc = 0.0;
 #pragma unroll
         for (int k = 1; k < SW_NDMAX; ++k)
             if (k < nd && step >= k) sacc += __ldg(B + (size_t)k * N + (ltr ? i - k : i + k)) * prev[k - 1];
-        const double o = (v[(long long)i * stride] - ad * sacc) / (1.0 + ad * __ldg(B + i));
+        const double o = (bi - ad * sacc) / (1.0 + ad * __ldg(B + i));
 #pragma unroll
         for (int k = SW_NDMAX - 2; k > 0; --k) prev[k] = prev[k - 1];
         prev[0] = o;
@@ -167,8 +177,9 @@ __global__ void k_fvm_sweep_vt(FvmView v, const double* __restrict__ aE, double 
 // loads, sweeps each row in shared memory (row pitch Nx + 1 against bank conflicts) and
 // writes the block back coalesced. a = ax v_r cos(theta_j), left to right when a >= 0
 // (rawkernel.py:298-375).
-constexpr int XT_L = 64;
-__global__ void __launch_bounds__(XT_L) k_fvm_sweep_x(FvmView v, const double* __restrict__ axvr, double h,
+constexpr int XT_L = 32;       // rows per CTA
+constexpr int XT_T = 256;      // threads per CTA: all load and store, the first XT_L sweep
+__global__ void __launch_bounds__(XT_T) k_fvm_sweep_x(FvmView v, const double* __restrict__ axvr, double h,
                                                       const double* __restrict__ B, double* __restrict__ Y) {
     extern __shared__ double rows[];  // [XT_L][Nx + 1]
     const int Nx = v.Nx, pitch = Nx + 1;
@@ -321,13 +332,14 @@ int fvm_precond(bte_fvm* h, double hstep, const double* X, double* Y, cudaStream
     k_fvm_coll_apply<<<fblocks(h->N), FT, 0, s>>>(v, h->dinv, h->T, X, h->A);   // natural layout
     if (int rc = launched("k_fvm_coll_apply")) return rc;
     // the three sweeps in place on the natural layout, coalesced (no layout swaps)
-    k_fvm_sweep_vr<<<fblocks((size_t)Nvt * Nx), FT, 0, s>>>(v, h->aE, hstep, h->A);
+    // the v_r lines are few (Nvt Nx) and long: small CTAs spread them over the SMs
+    k_fvm_sweep_vr<<<(unsigned)(((size_t)Nvt * Nx + 31) / 32), 32, 0, s>>>(v, h->aE, hstep, h->A);
     if (int rc = launched("k_fvm_sweep_vr")) return rc;
     k_fvm_sweep_vt<<<fblocks((size_t)Nr * Nx), FT, 0, s>>>(v, h->aE, hstep, h->A);
     if (int rc = launched("k_fvm_sweep_vt")) return rc;
     if (bte_raise_smem_limit((const void*)k_fvm_sweep_x, xsm) != cudaSuccess)
         return fvm_fail(BTE_ERR_ARG, "x lines too long for the shared-memory sweep");
-    k_fvm_sweep_x<<<(unsigned)((Nr * Nvt + XT_L - 1) / XT_L), XT_L, xsm, s>>>(v, h->axvr, hstep, h->A, Y);
+    k_fvm_sweep_x<<<(unsigned)((Nr * Nvt + XT_L - 1) / XT_L), XT_T, xsm, s>>>(v, h->axvr, hstep, h->A, Y);
     h->launches += 6;
     return launched("k_fvm_sweep_x");
 }

@@ -533,13 +533,13 @@ cudaError_t factor_right(int P, int N, int NC, T* A, int ld, long long stride, i
 
 int bte_lu_tc_max_n();
 cudaError_t bte_lu_factor_tc(int P, int N, int NC, float* A, int ld, long long stride, int32_t* piv, int32_t* info,
-                             cudaStream_t s, int occupancy);
+                             cudaStream_t s, int variant);
 
 // Factor P matrices in place; piv[P][N] receives perm (position -> stored row).
 // kernel: 0 = automatic (FP32, N <= 512: tensor cores; FP32 above: right-looking; FP64:
 // right-looking), 1 = right-looking, 2 = FP32 with the trailing updates on the tensor cores
-// (lu_tc.cu; N <= 512; two CTAs per SM), 3 = left-looking SIMT (N <= 512), 4 = as 2 with one
-// CTA per SM.
+// (lu_tc.cu; N <= 512; 256 threads, two CTAs per SM), 3 = left-looking SIMT (N <= 512), 4 = as
+// 2 with one CTA per SM, 5 = as 2 with 128 threads per CTA.
 template <typename T>
 cudaError_t bte_lu_factor_t(int P, int N, int NC, T* A, int ld, long long stride, int32_t* piv, int32_t* info,
                             cudaStream_t s, int kernel) {
@@ -547,9 +547,10 @@ cudaError_t bte_lu_factor_t(int P, int N, int NC, T* A, int ld, long long stride
     if (N < 1 || N > LU_MAX_N || NC < N || NC > N + 1 || ld < NC) return cudaErrorInvalidValue;
     // FP64: the right-looking kernel (the left-looking one serialises FP64 substitutions)
     if (sizeof(T) == 8 && kernel == 0) kernel = 1;
-    if (kernel == 2 || kernel == 4) {
+    if (kernel == 2 || kernel == 4 || kernel == 5) {
         if (sizeof(T) != 4 || N > bte_lu_tc_max_n()) return cudaErrorInvalidValue;
-        return bte_lu_factor_tc(P, N, NC, reinterpret_cast<float*>(A), ld, stride, piv, info, s, kernel == 4 ? 1 : 2);
+        return bte_lu_factor_tc(P, N, NC, reinterpret_cast<float*>(A), ld, stride, piv, info, s,
+                                kernel == 2 ? 0 : (kernel == 4 ? 1 : 2));
     }
     if (kernel == 3) {
         if (N > 512) return cudaErrorInvalidValue;
@@ -557,7 +558,7 @@ cudaError_t bte_lu_factor_t(int P, int N, int NC, T* A, int ld, long long stride
         // FP32 default: the tensor-core kernel, faster than the left-looking SIMT kernel at
         // every measured size from N = 33 to 512 (4096 matrices: 1.1x at N = 33 and 385,
         // 1.3x at N = 129 and 257, 1.7x at N = 512)
-        return bte_lu_factor_tc(P, N, NC, reinterpret_cast<float*>(A), ld, stride, piv, info, s, 2);
+        return bte_lu_factor_tc(P, N, NC, reinterpret_cast<float*>(A), ld, stride, piv, info, s, 0);
     }
     if (kernel == 3) kernel = 0;
     if (kernel == 0 && N <= 128) return launch_left<T, 4>(P, N, NC, A, ld, stride, piv, info, s);

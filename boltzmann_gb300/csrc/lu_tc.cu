@@ -31,8 +31,8 @@
 
 namespace {
 
-constexpr int TC_NT = 256;         // threads per CTA (8 warps)
-constexpr int TC_NW = TC_NT / 32;
+constexpr int TC_NT = 256;         // threads per CTA of the widest variant (8 warps; also 128)
+constexpr int TC_NW = TC_NT / 32;  // shared-memory slots for the warps' pivot candidates
 constexpr int TC_NB = 32;          // panel width = K of one block step
 constexpr int TC_TM = 128;         // trailing columns per tile: MMA M, TMEM lanes
 constexpr int TC_TR = 128;         // trailing rows per tile: MMA N, TMEM columns
@@ -141,8 +141,8 @@ __device__ inline void put_split4(unsigned char* sm, int m, int k, float a, floa
     *reinterpret_cast<float4*>(sm + TC_TILE_BYTES + o) = lo;
 }
 
-template <int ROWS, int OCC>
-__global__ void __launch_bounds__(TC_NT, OCC)
+template <int ROWS, int OCC, int NT>
+__global__ void __launch_bounds__(NT, OCC)
 k_lu_tc(int N, int NC, float* __restrict__ A, int ld, long long stride, int32_t* __restrict__ perm_out,
         int32_t* __restrict__ info, int vec4) {
     extern __shared__ unsigned char smraw[];
@@ -158,7 +158,7 @@ k_lu_tc(int N, int NC, float* __restrict__ A, int ld, long long stride, int32_t*
 
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     float* a = A + (size_t)blockIdx.x * stride;
-    for (int r = tid; r < N; r += TC_NT) perm[r] = r;
+    for (int r = tid; r < N; r += NT) perm[r] = r;
     const uint32_t mb = smem_u32(&mbar);
     if (tid == 0) {
         mbar_init(mb, 1);
@@ -180,7 +180,7 @@ k_lu_tc(int N, int NC, float* __restrict__ A, int ld, long long stride, int32_t*
         float pr[ROWS][TC_NB];
 #pragma unroll
         for (int i = 0; i < ROWS; ++i) {
-            const int s = tid + i * TC_NT;
+            const int s = tid + i * NT;
             const float* row = a + (size_t)perm[k0 + min(s, mrows - 1)] * ld + k0;
             if (vec4 && ncol == TC_NB) {
 #pragma unroll
@@ -209,7 +209,7 @@ k_lu_tc(int N, int NC, float* __restrict__ A, int ld, long long stride, int32_t*
             int bs = INT_MAX;
 #pragma unroll
             for (int i = 0; i < ROWS; ++i) {
-                const int s = tid + i * TC_NT;
+                const int s = tid + i * NT;
                 if (s >= j && s < mrows) {
                     const float v = fabsf(pr[i][j]);
                     const uint32_t key = (v == v) ? __float_as_uint(v) : 0u;
@@ -223,7 +223,7 @@ k_lu_tc(int N, int NC, float* __restrict__ A, int ld, long long stride, int32_t*
             if (smin != 0xffffffffu && (uint32_t)bs == smin) {
 #pragma unroll
                 for (int i = 0; i < ROWS; ++i)
-                    if (tid + i * TC_NT == bs) {
+                    if (tid + i * NT == bs) {
 #pragma unroll
                         for (int c = 0; c < TC_NB; c += 4)
                             *reinterpret_cast<float4*>(myc + c) =
@@ -239,7 +239,7 @@ k_lu_tc(int N, int NC, float* __restrict__ A, int ld, long long stride, int32_t*
             uint32_t K = 0;
             int S = INT_MAX, W = 0;
 #pragma unroll
-            for (int w2 = 0; w2 < TC_NW; ++w2) {
+            for (int w2 = 0; w2 < NT / 32; ++w2) {
                 const uint2 ks = *reinterpret_cast<const uint2*>(cb + w2 * TC_CAND_LD + TC_NB);
                 const int s2 = (int)ks.y;
                 if (s2 != INT_MAX && (S == INT_MAX || ks.x > K || (ks.x == K && s2 < S))) { K = ks.x; S = s2; W = w2; }
@@ -262,7 +262,7 @@ k_lu_tc(int N, int NC, float* __restrict__ A, int ld, long long stride, int32_t*
                 }
 #pragma unroll
                 for (int i = 0; i < ROWS; ++i)
-                    if (tid + i * TC_NT == S) {
+                    if (tid + i * NT == S) {
 #pragma unroll
                         for (int c = 0; c < TC_NB; c += 4) {
                             const float4 v = *reinterpret_cast<const float4*>(jb + c);
@@ -280,7 +280,7 @@ k_lu_tc(int N, int NC, float* __restrict__ A, int ld, long long stride, int32_t*
             const float inv = (d != 0.f) ? __frcp_rn(d) : 0.f;
 #pragma unroll
             for (int i = 0; i < ROWS; ++i) {
-                const int s = tid + i * TC_NT;
+                const int s = tid + i * NT;
                 if (s > j && s < mrows) {
                     const float l = pr[i][j] * inv;
                     pr[i][j] = l;
@@ -293,7 +293,7 @@ k_lu_tc(int N, int NC, float* __restrict__ A, int ld, long long stride, int32_t*
         // write the panel back (each position's data returns to its own stored row) and L11
 #pragma unroll
         for (int i = 0; i < ROWS; ++i) {
-            const int s = tid + i * TC_NT;
+            const int s = tid + i * NT;
             if (s < mrows) {
                 float* row = a + (size_t)perm[k0 + s] * ld + k0;
                 if (vec4 && ncol == TC_NB) {
@@ -316,7 +316,7 @@ k_lu_tc(int N, int NC, float* __restrict__ A, int ld, long long stride, int32_t*
         if (ncols <= 0) break;
         __syncthreads();
         // ---- 2. U12 = L11^-1 A12, one thread per column
-        for (int c = tid; c < ncols; c += TC_NT) {
+        for (int c = tid; c < ncols; c += NT) {
             float x[TC_NB];
 #pragma unroll
             for (int j = 0; j < TC_NB; ++j) x[j] = a[(size_t)perm[k0 + j] * ld + k0 + TC_NB + c];
@@ -341,7 +341,7 @@ k_lu_tc(int N, int NC, float* __restrict__ A, int ld, long long stride, int32_t*
         // ---- 3. A22 -= L21 U12 on the tensor cores
         for (int g0 = 0; g0 < nrows; g0 += TC_TR) {
             // B operand: L21 rows g0.., K = the panel's 32 columns
-            for (int e = tid; e < TC_TR * (TC_NB / 4); e += TC_NT) {
+            for (int e = tid; e < TC_TR * (TC_NB / 4); e += NT) {
                 const int r = e >> 3, k = (e & 7) * 4;
                 float v0 = 0.f, v1 = 0.f, v2 = 0.f, v3 = 0.f;
                 if (g0 + r < nrows) {
@@ -357,7 +357,7 @@ k_lu_tc(int N, int NC, float* __restrict__ A, int ld, long long stride, int32_t*
             }
             for (int c0 = 0; c0 < ncols; c0 += TC_TM) {
                 // A operand: U12^T, row m = column c0 + m of U12, k = pivot row
-                for (int e = tid; e < TC_TM * (TC_NB / 4); e += TC_NT) {
+                for (int e = tid; e < TC_TM * (TC_NB / 4); e += NT) {
                     const int m = e & (TC_TM - 1), k = (e >> 7) * 4;
                     float v[4] = {0.f, 0.f, 0.f, 0.f};
                     if (c0 + m < ncols) {
@@ -390,15 +390,16 @@ k_lu_tc(int N, int NC, float* __restrict__ A, int ld, long long stride, int32_t*
                 __syncthreads();
                 tc_fence_after();
                 if (s_fault) break;
-                // epilogue: warp w reads TMEM lanes 32 (w % 4).. (columns), TMEM columns
-                // 64 (w / 4).. (rows)
+                // epilogue: warp w reads TMEM lanes 32 (w % 4).. (columns) and its share of
+                // the TMEM columns (rows): all 128 with 4 warps, 64 (w / 4).. with 8
                 {
+                    constexpr int RH = TC_TR / (NT / 128);
                     const int q = wid & 3, h = wid >> 2;
                     const int m = 32 * q + lane;
                     const bool colok = (c0 + m) < ncols;
                     float* colp = a + k0 + TC_NB + c0 + m;
 #pragma unroll 1
-                    for (int r0 = 64 * h; r0 < 64 * h + 64; r0 += 16) {
+                    for (int r0 = RH * h; r0 < RH * h + RH; r0 += 16) {
                         if (g0 + r0 >= nrows) break;  // warp-uniform
                         float dv[16];
                         tmem_ld16(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)r0, dv);
@@ -432,7 +433,7 @@ k_lu_tc(int N, int NC, float* __restrict__ A, int ld, long long stride, int32_t*
         }
         __syncthreads();
     }
-    for (int r = tid; r < N; r += TC_NT) perm_out[(size_t)blockIdx.x * N + r] = perm[r];
+    for (int r = tid; r < N; r += NT) perm_out[(size_t)blockIdx.x * N + r] = perm[r];
     if (tid == 0) info[blockIdx.x] = s_fault ? -1 : inf;
     tc_fence_before();
     __syncthreads();
@@ -440,14 +441,14 @@ k_lu_tc(int N, int NC, float* __restrict__ A, int ld, long long stride, int32_t*
     if (wid == 0) tmem_dealloc(tbase, TC_TMEM_COLS);
 }
 
-template <int ROWS, int OCC>
+template <int ROWS, int OCC, int NT>
 cudaError_t launch_tc(int P, int N, int NC, float* A, int ld, long long stride, int32_t* piv, int32_t* info,
                       cudaStream_t s) {
     const size_t sm = tc_smem_bytes(N);
-    cudaError_t e = bte_raise_smem_limit((const void*)k_lu_tc<ROWS, OCC>, sm);
+    cudaError_t e = bte_raise_smem_limit((const void*)k_lu_tc<ROWS, OCC, NT>, sm);
     if (e != cudaSuccess) return e;
     const int vec4 = (ld % 4 == 0 && stride % 4 == 0 && ((uintptr_t)A & 15) == 0) ? 1 : 0;
-    k_lu_tc<ROWS, OCC><<<P, TC_NT, sm, s>>>(N, NC, A, ld, stride, piv, info, vec4);
+    k_lu_tc<ROWS, OCC, NT><<<P, NT, sm, s>>>(N, NC, A, ld, stride, piv, info, vec4);
     return cudaGetLastError();
 }
 
@@ -456,17 +457,25 @@ cudaError_t launch_tc(int P, int N, int NC, float* A, int ld, long long stride, 
 // largest N the tensor-core kernel takes (its panel is two 32-column rows per thread)
 int bte_lu_tc_max_n() { return 2 * TC_NT; }
 
-// occupancy: 2 = two CTAs per SM (the registers of two, 2 x 128 tensor-memory columns), 1 = one
-// CTA per SM (half the matrices in flight, so their trailing updates stay in L2)
+// variant 0: 256 threads, two CTAs per SM (the registers of two, 2 x 128 tensor-memory
+// columns); 1: 256 threads, one CTA per SM (half the matrices in flight, so that their
+// trailing updates stay in L2); 2: 128 threads (4 warps: half the per-column pivot-search work
+// per matrix, up to four panel rows per thread), two CTAs per SM
 cudaError_t bte_lu_factor_tc(int P, int N, int NC, float* A, int ld, long long stride, int32_t* piv, int32_t* info,
-                             cudaStream_t s, int occupancy) {
+                             cudaStream_t s, int variant) {
     if (P <= 0) return cudaSuccess;
     if (N < 1 || N > 2 * TC_NT || NC < N || NC > N + 1 || ld < NC) return cudaErrorInvalidValue;
     if ((long long)N * ld >= (1ll << 31)) return cudaErrorInvalidValue;  // row offsets are 32-bit
-    if (occupancy == 1) {
-        if (N <= TC_NT) return launch_tc<1, 1>(P, N, NC, A, ld, stride, piv, info, s);
-        return launch_tc<2, 1>(P, N, NC, A, ld, stride, piv, info, s);
+    if (variant == 2) {
+        if (N <= 128) return launch_tc<1, 2, 128>(P, N, NC, A, ld, stride, piv, info, s);
+        if (N <= 256) return launch_tc<2, 2, 128>(P, N, NC, A, ld, stride, piv, info, s);
+        if (N <= 384) return launch_tc<3, 2, 128>(P, N, NC, A, ld, stride, piv, info, s);
+        return launch_tc<4, 2, 128>(P, N, NC, A, ld, stride, piv, info, s);
     }
-    if (N <= TC_NT) return launch_tc<1, 2>(P, N, NC, A, ld, stride, piv, info, s);
-    return launch_tc<2, 2>(P, N, NC, A, ld, stride, piv, info, s);
+    if (variant == 1) {
+        if (N <= TC_NT) return launch_tc<1, 1, 256>(P, N, NC, A, ld, stride, piv, info, s);
+        return launch_tc<2, 1, 256>(P, N, NC, A, ld, stride, piv, info, s);
+    }
+    if (N <= TC_NT) return launch_tc<1, 2, 256>(P, N, NC, A, ld, stride, piv, info, s);
+    return launch_tc<2, 2, 256>(P, N, NC, A, ld, stride, piv, info, s);
 }

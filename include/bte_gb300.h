@@ -79,7 +79,8 @@ typedef struct {
     int lu_kernel;                /* mixed form: FP32 factorization of the Newton systems.
                                      0: the library's choice; 2: split-TF32 trailing updates
                                      on the tensor cores (bordered sizes n + 1 <= 512), two
-                                     CTAs per SM; 4: the same with one CTA per SM; 3: SIMT
+                                     CTAs per SM; 4: the same with one CTA per SM; 5: with
+                                     128 threads per CTA; 3: SIMT
                                      left-looking (n + 1 <= 512); 1: SIMT right-looking.
                                      Sizes a kernel does not take fall back to the library's
                                      choice                                                   */
@@ -208,7 +209,8 @@ int bte_lu_factor(int dtype, int P, int N, void* A, int ld, long long stride, in
  * N <= 512, right-looking above; FP64: right-looking),
  * 1 = right-looking for every N, 2 = FP32 only, N <= 512: trailing updates on the tcgen05
  * tensor cores in split TF32 (FP32-accurate factors), 3 = left-looking (N <= 512),
- * 4 = as 2 with one CTA per SM instead of two (fewer matrices in flight, kept in L2).
+ * 4 = as 2 with one CTA per SM instead of two (fewer matrices in flight, kept in L2),
+ * 5 = as 2 with 128 threads per CTA (less pivot-search work per matrix).
  * No counterpart in the reference; used to cross-check the factorizations. */
 int bte_lu_factor_ex(int dtype, int P, int N, void* A, int ld, long long stride, int32_t* piv, int32_t* info,
                      int kernel, void* stream);

@@ -28,7 +28,12 @@ With --perturbed-mass, the perturbation is one rounding unit on each mass-matrix
 carried through the reference's M^-1 scaling of its operators; the fixture gains
 `ff_perturbed_mass` and `resolution_mass`.
 
-Usage:  python tests/golden/make_golden_c2.py [c2|c5] [--perturbed | --perturbed-mass]
+With --swap-rosenbluth=FILE (c2 only; FILE from export_device_rosenbluth.py on a GPU host),
+the reference's Coulomb operator is rebuilt from its own trilinear tensors and the device
+library's Rosenbluth potentials and the c2 points are solved again by the reference; the
+fixture gains `ff_device_rosenbluth` and `rosenbluth_swap_shift`.
+
+Usage:  python tests/golden/make_golden_c2.py [c2|c5] [--perturbed | --perturbed-mass | --swap-rosenbluth=FILE]
 """
 import os
 import sys
@@ -108,12 +113,30 @@ def _perturb_mass(s, seed):
         getattr(s, name)[0] = new
 
 
-def run(m, xs, name, n_sp, l_max, points, perturb_seed=None, mode="ulps"):
+def _swap_rosenbluth(s, path):
+    """Rebuild the reference's Coulomb operator from its own trilinear tensors and the device
+    library's Rosenbluth potentials (export_device_rosenbluth.py), as assemble_operators builds
+    it (bte_0d3v_batched.py:444-476: M^-1 (cc_a . hl + cc_b . gl), qA = I)."""
+    import collision_operator_spherical as cos
+    import utils
+    d = np.load(path)
+    spec = s._op_spec_sp[0]
+    mw = utils.get_maxwellian_3d(s._par_vth[0], 1)
+    cca, ccb = cos.CollisionOpSP(spec).coulomb_collision_op_assembly(mw, s._par_vth[0], mp_pool_sz=1)
+    n = cca.shape[0]
+    Minv = spec.inverse_mass_mat(Mmat=s._op_mass_mat[0])
+    cc = np.dot(cca, d["hl"]) + np.dot(ccb, d["gl"])
+    s._op_col_ee[0] = np.dot(Minv, cc.reshape((n, -1))).reshape((n, n, n))
+
+
+def run(m, xs, name, n_sp, l_max, points, perturb_seed=None, mode="ulps", swap=None):
     P = len(points)
     t0 = time.time()
     s, args = G.make_solver(m, xs, n_sp, l_max, True, P)
     if perturb_seed is not None:
         (_perturb_mass if mode == "mass" else _perturb)(s, perturb_seed)
+    if swap is not None:
+        _swap_rosenbluth(s, swap)
     t_setup = time.time() - t0
     ebyn = np.array([p[0] for p in points])
     ion = np.array([p[1] for p in points])
@@ -134,6 +157,14 @@ def run(m, xs, name, n_sp, l_max, points, perturb_seed=None, mode="ulps"):
     r0 = np.linalg.norm(res_func(_initial_state(s, ffw), 0, 0), axis=0)
     hf, _ = _state_of(s, ff)
     r1 = np.linalg.norm(res_func(hf, 0, 0), axis=0)
+    if swap is not None:
+        g = dict(np.load(os.path.join(HERE, name)))
+        g["ff_device_rosenbluth"] = ff
+        g["rosenbluth_swap_shift"] = np.linalg.norm(ff - g["ff"], axis=0) / np.linalg.norm(g["ff"], axis=0)
+        np.savez_compressed(os.path.join(HERE, name), **g)
+        print("%s: shift with the device potentials %s" % (name, np.array2string(g["rosenbluth_swap_shift"],
+                                                                                  precision=2)), flush=True)
+        return
     if perturb_seed is not None:
         # a second solve of the same points with operators perturbed at the rounding level:
         # how far the reference's own answer moves under FP64-level changes of its operators
@@ -156,12 +187,15 @@ def main():
     which = [w for w in sys.argv[1:] if not w.startswith("--")] or ["c2", "c5"]
     seed = 7 if ("--perturbed" in sys.argv or "--perturbed-mass" in sys.argv) else None
     mode = "mass" if "--perturbed-mass" in sys.argv else "ulps"
+    swap = next((a.split("=", 1)[1] for a in sys.argv if a.startswith("--swap-rosenbluth=")), None)
+    if swap is not None:
+        swap = os.path.abspath(swap)
     xs = write_synthetic_lxcat(os.path.join("/tmp", "eAr_golden_%d.lxcat" % os.getpid()))
     cwd = os.getcwd()
     m = import_reference()
     try:
         if "c2" in which:
-            run(m, xs, "c2_shape_reference.npz", 128, 2, C2_POINTS, seed, mode)
+            run(m, xs, "c2_shape_reference.npz", 128, 2, C2_POINTS, seed, mode, swap)
         if "c5" in which:
             run(m, xs, "c5_reduced_reference.npz", 64, 4, C5_POINTS, seed, mode)
     finally:

@@ -9,7 +9,7 @@ def test_fastest_candidate_is_kept_and_cached(tmp_path, monkeypatch):
     monkeypatch.setenv("BOLTZMANN_GB300_CACHE", str(tmp_path))
     monkeypatch.setattr(autotune, "_mem", {})
     monkeypatch.setattr(autotune, "_key", lambda N, device: "fake-gpu|N=%d" % N)
-    fake_ms = {2: 3.0, 4: 2.5, 3: 4.0, 1: 9.0}
+    fake_ms = {2: 3.0, 4: 2.5, 5: 2.8, 3: 4.0, 1: 9.0}
     calls = []
 
     def fake_time(N, kernel, **kw):
@@ -18,7 +18,7 @@ def test_fastest_candidate_is_kept_and_cached(tmp_path, monkeypatch):
 
     monkeypatch.setattr(autotune, "time_lu", fake_time)
     rec = autotune.tune_lu(385)
-    assert rec["kernel"] == 4 and sorted(k for _, k in calls) == [1, 2, 3, 4]
+    assert rec["kernel"] == 4 and sorted(k for _, k in calls) == [1, 2, 3, 4, 5]
     data = json.load(open(tmp_path / "lu_autotune.json"))
     assert data["fake-gpu|N=385"]["kernel"] == 4
     # sizes above 512: the right-looking kernel is the only candidate

@@ -9,9 +9,9 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("N", [1, 7, 31, 64, 129, 385, 600, 1281])
 @pytest.mark.parametrize("dtype", ["f64", "f32"])
-@pytest.mark.parametrize("kernel", [0, 1, 2, 4], ids=["auto", "right", "tc", "tc1"])
+@pytest.mark.parametrize("kernel", [0, 1, 2, 4, 5], ids=["auto", "right", "tc", "tc1", "tc128"])
 def test_lu_factor_solve(N, dtype, kernel):
-    if kernel in (2, 4) and (dtype == "f64" or N > 512):
+    if kernel in (2, 4, 5) and (dtype == "f64" or N > 512):
         pytest.skip("the tensor-core factorization is FP32 with N <= 512")
     import torch
     from boltzmann_gb300 import _lib
@@ -97,7 +97,7 @@ def test_lu_negative_zero_is_not_a_pivot(dtype, N):
 
 
 @pytest.mark.parametrize("N", [33, 128, 385, 512])
-@pytest.mark.parametrize("kernel", [0, 2, 4], ids=["auto", "tc", "tc1"])
+@pytest.mark.parametrize("kernel", [0, 2, 4, 5], ids=["auto", "tc", "tc1", "tc128"])
 def test_lu_padded_rows_against_fp64(N, kernel):
     """FP32 factors with 16-byte aligned rows (the Newton solver's layout, vectorised path of
     the tensor-core kernel): backward error at FP32 level, and the tensor-core factors'
