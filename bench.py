@@ -54,6 +54,8 @@ def parse():
                          "first requests of the 2000-request stream")
     ap.add_argument("--serve-loads", default="0.5,0.8,1.0",
                     help="Poisson offered loads of the lambda sweep, as fractions of the plain FP64 capacity")
+    ap.add_argument("--serve-saturation-only", action="store_true",
+                    help="serving: only the saturation runs (every request queued at t = 0), no Poisson sweep")
     ap.add_argument("--serve-budget-gb", type=float, default=16.0, help="HBM budget of admitted points")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-1d", action="store_true", help="skip the 1D3V (config 4) leg")
@@ -320,6 +322,11 @@ def serve_bench(a):
             sat[prec] = summ
             torch.cuda.empty_cache()
         cap_fp64 = sat["fp64"]["solves_per_s"]
+        if a.serve_saturation_only:
+            return {"workload": "the first %d requests of the seeded 2000-request stream, all queued at t = 0; %d points"
+                                % (len(specs), pts), "hbm_budget_gb": a.serve_budget_gb,
+                    "saturation": {"mixed": sat["mixed"], "fp64": sat["fp64"],
+                                   "mixed_over_fp64": sat["mixed"]["solves_per_s"] / cap_fp64}}
         # lambda sweep: Poisson arrivals at fractions of the plain FP64 capacity, both forms;
         # the 0.8 point is the one the error comparison uses
         loads = [float(x) for x in a.serve_loads.split(",") if x.strip()]
