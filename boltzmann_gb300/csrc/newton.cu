@@ -420,7 +420,7 @@ k_refine_residual(GridView g, PointParams pp, int ee, const int* __restrict__ ac
 // x[pt] += sigma * y[slot]; corr[pt] = ||sigma * y|| / ||x|| of this pass
 __global__ void k_refine_update(int nact, const int* __restrict__ act, int N, const float* __restrict__ y,
                                 const double* __restrict__ sigma, double* x, int ldd, double* corr,
-                                const int* __restrict__ done, double* lastc) {
+                                const int* __restrict__ done) {
     __shared__ double red[32];
     int slot = blockIdx.x;
     if (slot >= nact) return;
@@ -437,10 +437,7 @@ __global__ void k_refine_update(int nact, const int* __restrict__ act, int N, co
     }
     cc = block_sum(cc, red);
     xx = block_sum(xx, red);
-    if (threadIdx.x == 0) {
-        corr[pt] = sqrt(cc / fmax(xx, 1e-300));
-        lastc[pt] = corr[pt];
-    }
+    if (threadIdx.x == 0) corr[pt] = sqrt(cc / fmax(xx, 1e-300));
 }
 
 // After refinement pass p >= 1 (0-based), per point: a correction at round-off or 4x
@@ -502,7 +499,7 @@ constexpr double GM_ACCEPT = 1e-8;
 
 // all: every running point as well (the diagnostic mode krylov = 2), first batch only
 __global__ void k_gm_collect(int nact, const int* __restrict__ act, int* status, int* list, int* cnt, int cap,
-                             bool all, double* lastc) {
+                             bool all) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= nact) return;
     const int pt = act[slot];
@@ -511,7 +508,6 @@ __global__ void k_gm_collect(int nact, const int* __restrict__ act, int* status,
     if (i < cap) {
         list[i] = slot;
         status[pt] = -1;
-        lastc[pt] = 0.0;  // GMRES solves the step to GM_TOL or hands the point over
     }
 }
 
@@ -1046,15 +1042,10 @@ __global__ void k_store_solution(int P_act, const T* __restrict__ xs, int N, con
 // noise-level decrease passes the test at a vanishing step.
 constexpr double STALL_ALPHA = 1.0 / 64.0;
 constexpr double STALL_RTOL = 1e-6;
-// A mixed-form point that reaches its round-off stop while its last step was refined only to a
-// relative correction above MIXED_ROUNDOFF_CORR has a floor set by its FP32 factors, not by
-// FP64 arithmetic: it goes to the FP64 form (from this iterate) instead of stopping.
-constexpr double MIXED_ROUNDOFF_CORR = 1e-3;
 __global__ void k_armijo(int nact, const int* __restrict__ act, int* searching, double* alpha,
                          const double* __restrict__ r, const double* __restrict__ rt, double c, double rho,
                          double amin, int* status, int* nsearch, int* accepted, const double* __restrict__ r0,
-                         double stagnate_rtol, const double* __restrict__ srel, double step_rtol, int stall_status,
-                         const double* __restrict__ lastc) {
+                         double stagnate_rtol, const double* __restrict__ srel, double step_rtol, int stall_status) {
     int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= nact) return;
     int pt = act[slot];
@@ -1064,18 +1055,17 @@ __global__ void k_armijo(int nact, const int* __restrict__ act, int* searching, 
     bool ok = (0.5 * rn * rn <= 0.5 * rr * rr - c * al * rr * rr);
     if (!isfinite(rn)) ok = false;
     const bool tiny = srel[pt] <= step_rtol;
-    const int roundoff = (lastc && lastc[pt] > MIXED_ROUNDOFF_CORR) ? BTE_ST_NEED_FP64 : BTE_ST_ROUNDOFF;
     if (ok) {
         searching[pt] = 0;
         accepted[pt] = 1;
         // a step that barely contracts the merit at round-off level ends the solve after it is taken
-        if (rn > 0.5 * rr && (rn <= stagnate_rtol * r0[pt] || srel[pt] <= 1e-2 * step_rtol)) status[pt] = roundoff;
+        if (rn > 0.5 * rr && (rn <= stagnate_rtol * r0[pt] || srel[pt] <= 1e-2 * step_rtol)) status[pt] = BTE_ST_ROUNDOFF;
         return;
     }
     if (al == 1.0 && (rr <= stagnate_rtol * r0[pt] || tiny)) {
         searching[pt] = 0;
         accepted[pt] = 0;
-        status[pt] = roundoff;
+        status[pt] = BTE_ST_ROUNDOFF;
         return;
     }
     al *= rho;
@@ -1178,7 +1168,6 @@ struct BteWork {
     double* h0 = nullptr;     // initial state (restart of points that fall back to FP64), P x n
     double *ref_r = nullptr, *ref_r0 = nullptr;  // the reference's merit at the end / start, P
     double *corr0 = nullptr, *corr1 = nullptr;   // relative refinement corrections, first / last pass
-    double* lastc = nullptr;                     // the last refinement correction of the current Newton step
     int32_t* reason = nullptr;                   // mixed-form status of each point before the FP64 pass
     int32_t* refdone = nullptr;                  // refinement finished for the point in this Newton step
     int32_t* nit = nullptr;                      // Newton iterations of each point in its current solve
@@ -1199,7 +1188,7 @@ struct BteWork {
 };
 
 static void free_work(BteWork* w) {
-    void* ptrs[] = {w->nit, w->refdone, w->reason, w->corr0, w->corr1, w->lastc, w->ref_r, w->ref_r0, w->rowscale, w->h0, w->srel, w->sigma, w->xs, w->h, w->ht, w->F, w->Ft, w->aux, w->auxt, w->scal, w->scalt, w->dh, w->r, w->rt, w->r0,
+    void* ptrs[] = {w->nit, w->refdone, w->reason, w->corr0, w->corr1, w->ref_r, w->ref_r0, w->rowscale, w->h0, w->srel, w->sigma, w->xs, w->h, w->ht, w->F, w->Ft, w->aux, w->auxt, w->scal, w->scalt, w->dh, w->r, w->rt, w->r0,
                     w->alpha, w->J, w->kc, w->gm_V, w->gm_Z, w->gm_W, w->gm_H, w->gm_cs, w->gm_sn, w->gm_g, w->gm_bn,
                     w->gm_sig, w->gm_xf, w->gm_list, w->gm_on, w->gm_cnt, w->piv, w->info, w->act, w->act2, w->cnt, w->searching, w->accepted};
     for (void* p : ptrs)
@@ -1255,7 +1244,6 @@ static int ensure_work(BteWork* w, const BteGrid* g, int P, int prec, int krylov
               A((void**)&w->rowscale, (size_t)P * (N + 1) * sizeof(double)) && A((void**)&w->h0, pn) &&
               A((void**)&w->ref_r, (size_t)P * sizeof(double)) && A((void**)&w->ref_r0, (size_t)P * sizeof(double)) &&
               A((void**)&w->corr0, (size_t)P * sizeof(double)) && A((void**)&w->corr1, (size_t)P * sizeof(double)) &&
-              A((void**)&w->lastc, (size_t)P * sizeof(double)) &&
               A((void**)&w->reason, (size_t)P * sizeof(int32_t)) && A((void**)&w->refdone, (size_t)P * sizeof(int32_t)) &&
               A((void**)&w->nit, (size_t)P * sizeof(int32_t)) && A((void**)&w->r, P * sizeof(double)) &&
               A((void**)&w->rt, P * sizeof(double)) && A((void**)&w->r0, P * sizeof(double)) &&
@@ -1529,7 +1517,7 @@ static cudaError_t gmres_refine(SolveCtx& c, Lane& L, int nact, bool all) {
     for (int round = 0; round < 64; ++round) {
         GMCK(cudaMemsetAsync(w->gm_cnt, 0, 2 * sizeof(int32_t), s), "clear counters");
         k_gm_collect<<<nblk(nact, 256), 256, 0, s>>>(nact, L.act, c.status, w->gm_list, w->gm_cnt, w->gm_cap,
-                                                     all && round == 0, w->lastc);
+                                                     all && round == 0);
         GMCK(cudaGetLastError(), "collect");
         int hc[2] = {0, 0};
         GMCK(cudaMemcpyAsync(hc, w->gm_cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, s), "read count");
@@ -1632,7 +1620,6 @@ static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
             CKR(other([&] { k_store_solution<float><<<nact, 128, 0, s>>>(nact, xs, N, L.act, w->dh, ldd); }));
             // FP64 iterative refinement of the step against the matrix-free FP64 Jacobian,
             // per point until its correction contracts (or it is handed to FP64)
-            CKR(other([&] { k_fill_dbl<<<nblk(P, 256), 256, 0, s>>>(w->lastc, 0.0, P); }));
             if (nrefine > 0) CKR(other([&] { k_fill_int<<<nblk(P, 256), 256, 0, s>>>(w->refdone, 0, P); }));
             for (int rf = 0; rf < nrefine; ++rf) {
                 double* cprev = (rf & 1) ? w->corr0 : w->corr1;
@@ -1645,7 +1632,7 @@ static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
                                                                   nullptr);
                     le = bte_lu_solve_t<float>(nact, N, (const float*)L.J, ld, jstride, L.piv, xs, 0, s);
                     k_refine_update<<<nact, 128, 0, s>>>(nact, L.act, N, xs, L.sigma, w->dh, ldd, ccur,
-                                                         w->refdone, w->lastc);
+                                                         w->refdone);
                 }));
                 CKR(le);
                 if (rf == 0)
@@ -1692,8 +1679,7 @@ static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
                 k_armijo<<<nblk(nact, 256), 256, 0, s>>>(nact, L.act, w->searching, w->alpha, w->r, w->rt,
                                                         o->line_search_c, o->alpha_rho, amin, status, w->cnt,
                                                         w->accepted, w->r0, 1e-9, w->srel, 1e-8,
-                                                        prec == BTE_PREC_MIXED ? BTE_ST_NEED_FP64 : BTE_ST_ROUNDOFF,
-                                                        prec == BTE_PREC_MIXED ? w->lastc : nullptr);
+                                                        prec == BTE_PREC_MIXED ? BTE_ST_NEED_FP64 : BTE_ST_ROUNDOFF);
             }));
             int hc = 0;
             CKR(cudaMemcpyAsync(&hc, w->cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
