@@ -374,6 +374,38 @@ def serve_bench(a):
     }
 
 
+def bench_reference_points(a):
+    """The mixed and plain forms on the points of the c2-shape reference fixture
+    (tests/golden/c2_shape_reference.npz: 128 B-splines x l_max 2, e-e on, 8 points, three of
+    them at E/N < 10 Td and ionization above 1e-4), each EDF's relative L2 error against the
+    reference's own solution of the same point, with the reference's final residual and the
+    shift of its answer under rounding-level perturbations of its operators."""
+    import torch
+    from boltzmann_gb300.workloads import write_synthetic_lxcat
+    g = dict(np.load(os.path.join(ROOT, "tests", "golden", "c2_shape_reference.npz")))
+    P = g["ff"].shape[1]
+    ns = types.SimpleNamespace(n_sp=int(g["n_sp"]), l_max=int(g["l_max"]), n_pts=P)
+    xs = write_synthetic_lxcat()
+    out = {"points": [{"EbyN_Td": float(e), "ion_deg": float(i)} for e, i in zip(g["EbyN"], g["ion_deg"])],
+           "reference_rel_error": [float(x) for x in g["rel_error"]]}
+    for k in ("resolution", "resolution_mass", "rosenbluth_swap_shift"):
+        if k in g:
+            out["reference_" + k] = [float(x) for x in g[k]]
+    try:
+        for prec in ("mixed", "fp64"):
+            s, args, _ = make_solver(xs, ns, prec, 0)
+            for k in ["n0", "ne", "ns_by_n0", "Tg", "E"]:
+                s.set_boltzmann_parameter(0, k, g[k])
+            ff, q = full_solve(s, args, torch.as_tensor(s.initialize(0, P), device="cuda"))
+            ff = ff.cpu().numpy()
+            out["edf_rel_err_%s" % prec] = [float(x) for x in np.linalg.norm(ff - g["ff"], axis=0)
+                                            / np.linalg.norm(g["ff"], axis=0)]
+            del s
+    finally:
+        os.unlink(xs)
+    return out
+
+
 def bench_c5(a):
     """Config 5 (256 B-splines x l_max 4: n = 1280, 1281 x 1281 bordered systems, e-e on, ionization
     degree 1e-6..1e-2, seed 20261205) on a sample of its 16384 points: one full EDF solve of
@@ -886,6 +918,7 @@ def main():
     one_d = None if (a.no_1d or ws > 1) else bench_1d(a, peaks)
     fvm = None if (a.no_fvm or ws > 1) else bench_fvm(a, peaks)
     c5 = None if (a.c5_points <= 0 or ws > 1) else bench_c5(a)
+    ref_pts = None if ws > 1 else bench_reference_points(a)
     cpu = None if a.no_cpu else cpu_baseline_run(a)
     st = r["stats"]
     steps_ms = sorted(r["steps_ms"])
@@ -900,7 +933,7 @@ def main():
         "fp64_fallback_points_per_step": st["fp64_fallback_points"] / a.steps,
         "fp64_fallback_reasons": st["fp64_fallback_reasons"],
         "roofline": roofline(st, peaks), "cpu_baseline": cpu, "clocks": r["clocks"],
-        "plain_fp64": r["plain"], "serving": serve, "bte_1d3v": one_d, "bte_1d3v_fvm": fvm, "c5_sample": c5, "setup_s": r["setup_s"],
+        "plain_fp64": r["plain"], "serving": serve, "bte_1d3v": one_d, "bte_1d3v_fvm": fvm, "c5_sample": c5, "edf_rel_err_vs_reference": ref_pts, "setup_s": r["setup_s"],
         "newton_iters": {"mean": float(np.mean(r["iters"])), "max": int(np.max(r["iters"]))},
         "lu_autotune": _autotune_report(),
         "status_counts": {str(k): int(v) for k, v in zip(*np.unique(r["status"], return_counts=True))},
