@@ -65,6 +65,11 @@ def parse():
     ap.add_argument("--steps-1d", type=int, default=20)
     ap.add_argument("--steps-fvm", type=int, default=10)
     ap.add_argument("--no-fvm", action="store_true", help="skip the finite-volume 1D3V leg")
+    ap.add_argument("--krylov", type=int, default=0,
+                    help="mixed form: GMRES on the FP32 factors before an FP64 hand-over (bte_solve_opts.krylov)")
+    ap.add_argument("--refine", type=int, default=4, help="mixed form: FP64 refinement passes per Newton step")
+    ap.add_argument("--lu64-kernel", type=int, default=0,
+                    help="FP64 factorizations: 0 library choice, 1 one CTA per system, 6 split over many CTAs")
     ap.add_argument("--lu-kernel", type=int, default=0,
                     help="FP32 factorization of the mixed form: 0 library choice, 2 tensor cores, 3 SIMT left-looking")
     return ap.parse_args()
@@ -80,6 +85,7 @@ def workload_config(a, precision):
         "cache": "inputs larger than L2: each step streams %.1f GB of Jacobians" % (
             a.n_pts * (a.n_sp * (a.l_max + 1) + 1) ** 2 * (4 if precision == "mixed" else 8) / 1e9),
         "parallelism": "points sharded across GPUs, no collective on the data path",
+        "refine": a.refine, "krylov": a.krylov,
     }
 
 
@@ -155,7 +161,8 @@ def make_solver(xs, a, precision, dev):
     args = types.SimpleNamespace(threads=1, sp_order=3, spline_qpts=5, ee_collisions=1, verbose=0, use_gpu=1,
                                  Efreq=0.0, dt=1e-3, cycles=1, solver_type="steady-state", l_max=a.l_max,
                                  Nr=a.n_sp - 1, n_pts=a.n_pts, precision=precision,
-                                 lu_kernel=getattr(a, "lu_kernel", 0))
+                                 lu_kernel=getattr(a, "lu_kernel", 0), krylov=getattr(a, "krylov", 0),
+                                 refine=getattr(a, "refine", 4), lu64_kernel=getattr(a, "lu64_kernel", 0))
     s = bte_0d3v_batched(args, np.array([EV_MAX]), np.array([TE_NORM]), np.array([a.n_sp - 1]),
                          [[[l, 0] for l in range(a.l_max + 1)]], 1, [xs])
     s._dev_id = dev
@@ -805,6 +812,7 @@ class CpuReferenceRun:
                 self.spent += time.perf_counter() - t1
                 i1, i2 = stop.value
                 self.done.append({"points": self.n_pts, "seconds": self.spent, "iters": [i1["iters"], i2["iters"]],
+                                  "res_evals": [i1["res_evals"], i2["res_evals"]],
                                   "stop": [i1["status"], i2["status"]]})
                 self.k += 1
                 self._start()

@@ -53,7 +53,7 @@ class SolveOpts(C.Structure):
         ("atol", C.c_double), ("rtol", C.c_double), ("max_iter", C.c_int),
         ("alpha_min", C.c_double), ("alpha_rho", C.c_double), ("line_search_c", C.c_double),
         ("ee", C.c_int), ("precision", C.c_int), ("refine", C.c_int), ("krylov", C.c_int), ("lu_kernel", C.c_int),
-        ("reserved", C.c_int * 3),
+        ("lu64_kernel", C.c_int), ("reserved", C.c_int * 2),
     ]
 
 

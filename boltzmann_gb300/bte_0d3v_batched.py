@@ -556,7 +556,8 @@ class bte_0d3v_batched:
                               ee=int(getattr(self._args, "ee_collisions", 0)), precision=self._precision(),
                               refine=int(getattr(self._args, "refine", 4)),
                               krylov=int(getattr(self._args, "krylov", 0)),
-                              lu_kernel=self._lu_kernel(grid_idx))
+                              lu_kernel=self._lu_kernel(grid_idx),
+                              lu64_kernel=int(getattr(self._args, "lu64_kernel", 0)))
         stream = torch.cuda.current_stream().cuda_stream
         _lib.check(_lib.load().bte_solve_steady(self._grid[grid_idx], n_pts, _ptr(n0), _ptr(ne), _ptr(ns), _ptr(Tg),
                                                 _ptr(E), _ptr(f), _ptr(status), _ptr(iters), C.byref(opts),

@@ -620,11 +620,12 @@ int bte_lu_factor(int dtype, int P, int N, void* A, int ld, long long stride, in
 int bte_lu_factor_ex(int dtype, int P, int N, void* A, int ld, long long stride, int32_t* piv, int32_t* info,
                      int kernel, void* stream) {
     if (P < 0 || N < 1 || N > 2048 || ld < N || stride < (long long)ld * N || !A || !piv || !info || kernel < 0 ||
-        kernel > 5)
+        kernel > 6)
         return fail(BTE_ERR_ARG, "bad LU arguments");
     if ((kernel == 2 || kernel == 4 || kernel == 5) && (dtype == 0 || N > 512))
         return fail(BTE_ERR_ARG, "the tensor-core LU is FP32 with N <= 512");
     if (kernel == 3 && N > 512) return fail(BTE_ERR_ARG, "the left-looking LU takes N <= 512");
+    if (kernel == 6 && dtype != 0) return fail(BTE_ERR_ARG, "the split LU is FP64");
     cudaError_t e = (dtype == 0)
                         ? bte_lu_factor_t<double>(P, N, N, (double*)A, ld, stride, piv, info, (cudaStream_t)stream, kernel)
                         : bte_lu_factor_t<float>(P, N, N, (float*)A, ld, stride, piv, info, (cudaStream_t)stream, kernel);

@@ -18,6 +18,8 @@
 //               column) and written once. No read-modify-write of a trailing matrix.
 //   k_lu_right  (any N)     right-looking by panels (trailing matrix in global memory),
 //               for the largest systems.
+// (k_lu_tc in lu_tc.cu is the FP32 tensor-core kernel; k_lus_* below split one FP64
+// factorization over many CTAs.)
 #include <cstdint>
 #include <algorithm>
 #include "bte_common.cuh"
@@ -412,6 +414,203 @@ k_lu_right(int N, int NC, T* __restrict__ A, int ld, long long stride, int32_t* 
     if (tid == 0) info[mat] = inf;
 }
 
+// ---------------------------------------------------------------------------------
+// split right-looking kernel (kernel 6, FP64): one factorization spread over many CTAs.
+// Per panel of NB columns, three launches in stream order:
+//   k_lus_panel   one CTA per matrix: partial pivoting of the panel in shared memory
+//                 (perm updated in global memory; rows are never exchanged), panel written back;
+//   k_lus_trsm    one CTA per (matrix, 64 columns right of the panel): U12 = L11^-1 A12;
+//   k_lus_update  one CTA per (matrix, 64 x 64 tile of the trailing matrix): A22 -= L21 U12
+//                 from shared-memory copies of the L21 and U12 tiles, 4 x 4 register tiles.
+// The one-CTA-per-matrix kernels run each matrix on one SM. GB300 issues about 2 DFMA per
+// clock per SM, so a lone FP64 factorization of N = 385 takes milliseconds there and one of
+// N = 1281 a fifth of a second: what the few points of an FP64 lane pay per Newton
+// iteration. Split, the trailing updates of even one matrix spread over the GPU and the
+// serial part is the panels' pivot searches. Same arithmetic for a matrix whatever P is.
+// ---------------------------------------------------------------------------------
+constexpr int SP_T = 64;          // trailing tile edge
+constexpr int SP_LDS = SP_T + 1;  // padded shared-memory row of a tile
+
+__host__ __device__ inline int split_ldp(int mrows) { return mrows | 1; }
+__host__ __device__ inline size_t split_panel_smem(int mrows, int NB, size_t w) {
+    return align16((size_t)mrows * 4) + (size_t)split_ldp(mrows) * NB * w;
+}
+
+template <typename T, int NB, int ROWS>
+__global__ void __launch_bounds__(LU_THREADS)
+k_lus_panel(int N, int k0, T* __restrict__ A, int ld, long long stride, int32_t* __restrict__ perm_g,
+            int32_t* __restrict__ info) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int mrows = N - k0, kb = min(NB, mrows), ldp = split_ldp(mrows);
+    int* ps = reinterpret_cast<int*>(smraw);
+    T* P = reinterpret_cast<T*>(smraw + align16((size_t)mrows * 4));
+    __shared__ T redv[LU_THREADS / 32];
+    __shared__ int redi[LU_THREADS / 32];
+    const int mat = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+    T* a = A + (size_t)mat * stride;
+    int32_t* pg = perm_g + (size_t)mat * N;
+    for (int r = tid; r < mrows; r += nt) ps[r] = (k0 == 0) ? r : pg[k0 + r];
+    __syncthreads();
+    for (int e = tid; e < mrows * kb; e += nt) {
+        const int r = e / kb, c = e % kb;
+        P[c * ldp + r] = a[(size_t)ps[r] * ld + k0 + c];
+    }
+    __syncthreads();
+    int inf = 0;
+    panel_factor<T, ROWS, NB>(P, ldp, mrows, kb, kb, ps, 0, inf, redv, redi);
+    for (int e = tid; e < mrows * kb; e += nt) {
+        const int r = e / kb, c = e % kb;
+        a[(size_t)ps[r] * ld + k0 + c] = P[c * ldp + r];
+    }
+    for (int r = tid; r < mrows; r += nt) pg[k0 + r] = ps[r];
+    if (tid == 0) {
+        int cur = (k0 == 0) ? 0 : info[mat];
+        if (cur == 0 && inf != 0) cur = k0 + inf;
+        info[mat] = cur;
+    }
+}
+
+template <typename T, int NB>
+__global__ void __launch_bounds__(SP_T)
+k_lus_trsm(int N, int NC, int k0, int ncb, T* __restrict__ A, int ld, long long stride,
+           const int32_t* __restrict__ perm_g) {
+    __shared__ T L[NB][NB + 1];
+    __shared__ int pr[NB];
+    const int kb = min(NB, N - k0), c0g = k0 + kb;
+    const int mat = blockIdx.x / ncb, cb = blockIdx.x % ncb;
+    T* a = A + (size_t)mat * stride;
+    const int32_t* pg = perm_g + (size_t)mat * N;
+    const int tid = threadIdx.x;
+    if (tid < NB) pr[tid] = (tid < kb) ? pg[k0 + tid] : 0;
+    __syncthreads();
+    for (int e = tid; e < NB * NB; e += SP_T) {
+        const int i = e / NB, j = e % NB;
+        L[i][j] = (i < kb && j < kb) ? a[(size_t)pr[i] * ld + k0 + j] : T(0);
+    }
+    __syncthreads();
+    const int c = c0g + cb * SP_T + tid;
+    if (c >= NC) return;
+    T x[NB];
+#pragma unroll
+    for (int j = 0; j < NB; ++j) x[j] = (j < kb) ? a[(size_t)pr[j] * ld + c] : T(0);
+#pragma unroll
+    for (int j = 1; j < NB; ++j) {
+#pragma unroll
+        for (int i = 0; i < j; ++i) x[j] -= L[j][i] * x[i];
+    }
+#pragma unroll
+    for (int j = 0; j < NB; ++j)
+        if (j < kb) a[(size_t)pr[j] * ld + c] = x[j];
+}
+
+template <typename T, int NB>
+__global__ void __launch_bounds__(256)
+k_lus_update(int N, int NC, int k0, int nrb, int ncb, T* __restrict__ A, int ld, long long stride,
+             const int32_t* __restrict__ perm_g) {
+    __shared__ T Ls[NB][SP_LDS];  // L21 tile, transposed: Ls[k][r]
+    __shared__ T Us[NB][SP_LDS];  // U12 tile: Us[k][c]
+    __shared__ int prow[SP_T];
+    __shared__ int pk[NB];
+    const int kb = min(NB, N - k0), c0g = k0 + kb;
+    const int mr = N - c0g, ncol = NC - c0g;
+    const int per = nrb * ncb;
+    const int mat = blockIdx.x / per, t = blockIdx.x % per, rb = t / ncb, cb = t % ncb;
+    T* a = A + (size_t)mat * stride;
+    const int32_t* pg = perm_g + (size_t)mat * N;
+    const int tid = threadIdx.x;
+    if (tid < SP_T) {
+        const int r = rb * SP_T + tid;
+        prow[tid] = (r < mr) ? pg[c0g + r] : -1;
+    }
+    if (tid < NB) pk[tid] = (tid < kb) ? pg[k0 + tid] : 0;
+    __syncthreads();
+    for (int e = tid; e < SP_T * NB; e += 256) {
+        const int r = e / NB, k = e % NB;
+        Ls[k][r] = (prow[r] >= 0 && k < kb) ? a[(size_t)prow[r] * ld + k0 + k] : T(0);
+    }
+    for (int e = tid; e < NB * SP_T; e += 256) {
+        const int k = e / SP_T, c = e % SP_T;
+        const int cl = cb * SP_T + c;
+        Us[k][c] = (k < kb && cl < ncol) ? a[(size_t)pk[k] * ld + c0g + cl] : T(0);
+    }
+    __syncthreads();
+    const int tx = tid & 15, ty = tid >> 4;
+    T acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+#pragma unroll 8
+    for (int k = 0; k < NB; ++k) {
+        T av[4], bv[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) av[i] = Ls[k][ty + 16 * i];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) bv[j] = Us[k][tx + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] += av[i] * bv[j];
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int pr = prow[ty + 16 * i];
+        if (pr < 0) continue;
+        T* row = a + (size_t)pr * ld + c0g + cb * SP_T;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int c = tx + 16 * j;
+            if (cb * SP_T + c < ncol) row[c] -= acc[i][j];
+        }
+    }
+}
+
+template <typename T, int NB, int ROWS>
+cudaError_t launch_split_panel(int P, int N, int k0, T* A, int ld, long long stride, int32_t* piv, int32_t* info,
+                               cudaStream_t s) {
+    const size_t sm = split_panel_smem(N - k0, NB, sizeof(T));
+    cudaError_t e = bte_raise_smem_limit((const void*)k_lus_panel<T, NB, ROWS>, sm);
+    if (e != cudaSuccess) return e;
+    k_lus_panel<T, NB, ROWS><<<P, LU_THREADS, sm, s>>>(N, k0, A, ld, stride, piv, info);
+    return cudaGetLastError();
+}
+
+template <typename T, int NB>
+cudaError_t factor_split_nb(int P, int N, int NC, T* A, int ld, long long stride, int32_t* piv, int32_t* info,
+                            cudaStream_t s) {
+    for (int k0 = 0; k0 < N; k0 += NB) {
+        const int mrows = N - k0, kb = std::min(NB, mrows);
+        cudaError_t e;
+        if (mrows <= LU_THREADS) e = launch_split_panel<T, NB, 1>(P, N, k0, A, ld, stride, piv, info, s);
+        else if (mrows <= 2 * LU_THREADS) e = launch_split_panel<T, NB, 2>(P, N, k0, A, ld, stride, piv, info, s);
+        else if (mrows <= 4 * LU_THREADS) e = launch_split_panel<T, NB, 4>(P, N, k0, A, ld, stride, piv, info, s);
+        else e = launch_split_panel<T, NB, 8>(P, N, k0, A, ld, stride, piv, info, s);
+        if (e != cudaSuccess) return e;
+        const int c0g = k0 + kb, ncol = NC - c0g, mr = N - c0g;
+        if (ncol <= 0) break;
+        const int ncb = (ncol + SP_T - 1) / SP_T;
+        k_lus_trsm<T, NB><<<(unsigned)P * ncb, SP_T, 0, s>>>(N, NC, k0, ncb, A, ld, stride, piv);
+        if (mr > 0) {
+            const int nrb = (mr + SP_T - 1) / SP_T;
+            k_lus_update<T, NB><<<(unsigned)P * nrb * ncb, 256, 0, s>>>(N, NC, k0, nrb, ncb, A, ld, stride, piv);
+        }
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// panel width: as wide as the panel's shared memory allows (<= 200 KB)
+template <typename T>
+cudaError_t factor_split(int P, int N, int NC, T* A, int ld, long long stride, int32_t* piv, int32_t* info,
+                         cudaStream_t s) {
+    if (split_panel_smem(N, 32, sizeof(T)) <= 200 * 1024)
+        return factor_split_nb<T, 32>(P, N, NC, A, ld, stride, piv, info, s);
+    if (split_panel_smem(N, 16, sizeof(T)) <= 200 * 1024)
+        return factor_split_nb<T, 16>(P, N, NC, A, ld, stride, piv, info, s);
+    return factor_split_nb<T, 8>(P, N, NC, A, ld, stride, piv, info, s);
+}
+
 // Substitution for one right-hand side per matrix. mode 0: full solve (gather b by perm,
 // unit-lower forward, upper backward); mode 1: backward only (the RHS was eliminated as
 // column N during the factorization). Rows of position r are read from stored row perm[r].
@@ -539,7 +738,8 @@ cudaError_t bte_lu_factor_tc(int P, int N, int NC, float* A, int ld, long long s
 // kernel: 0 = automatic (FP32, N <= 512: tensor cores; FP32 above: right-looking; FP64:
 // right-looking), 1 = right-looking, 2 = FP32 with the trailing updates on the tensor cores
 // (lu_tc.cu; N <= 512; 256 threads, two CTAs per SM), 3 = left-looking SIMT (N <= 512), 4 = as
-// 2 with one CTA per SM, 5 = as 2 with 128 threads per CTA.
+// 2 with one CTA per SM, 5 = as 2 with 128 threads per CTA, 6 = FP64 split over many CTAs per
+// matrix (panel, triangular solve and 64 x 64 trailing tiles as separate launches).
 template <typename T>
 cudaError_t bte_lu_factor_t(int P, int N, int NC, T* A, int ld, long long stride, int32_t* piv, int32_t* info,
                             cudaStream_t s, int kernel) {
@@ -547,6 +747,13 @@ cudaError_t bte_lu_factor_t(int P, int N, int NC, T* A, int ld, long long stride
     if (N < 1 || N > LU_MAX_N || NC < N || NC > N + 1 || ld < NC) return cudaErrorInvalidValue;
     // FP64: the right-looking kernel (the left-looking one serialises FP64 substitutions)
     if (sizeof(T) == 8 && kernel == 0) kernel = 1;
+    if (kernel == 6) {
+        if constexpr (sizeof(T) == 8) {
+            return factor_split<T>(P, N, NC, A, ld, stride, piv, info, s);
+        } else {
+            return cudaErrorInvalidValue;
+        }
+    }
     if (kernel == 2 || kernel == 4 || kernel == 5) {
         if (sizeof(T) != 4 || N > bte_lu_tc_max_n()) return cudaErrorInvalidValue;
         return bte_lu_factor_tc(P, N, NC, reinterpret_cast<float*>(A), ld, stride, piv, info, s,

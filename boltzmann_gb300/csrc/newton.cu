@@ -1570,6 +1570,11 @@ static int lu_kernel_for(int requested, int N) {
     return (requested >= 0 && requested <= 5) ? requested : 0;
 }
 
+// FP64 factorization kernel (bte_solve_opts.lu64_kernel): the split kernel unless the one-CTA
+// kernel is asked for. A point's arithmetic does not depend on how many points share a launch
+// with either kernel.
+static int lu64_kernel_for(int requested) { return requested == 1 ? 1 : 6; }
+
 // One Newton iteration (Jacobian, factorization, step, refinement, line search, acceptance,
 // convergence test) for the `nact` points of lane L whose F, aux, scal and r are current;
 // returns the points still running, whose list is then L.act (the list before the
@@ -1655,7 +1660,8 @@ static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
                                                                   jm.stage, 1.0, 0.0, nullptr);
             }));
             CKR(pf.run(PF_LU64, s, nact * lu_flops(N), lub, 1, [&] {
-                le = bte_lu_factor_t<double>(nact, N, N + 1, (double*)L.J, ld, jstride, L.piv, L.info, s, 0);
+                le = bte_lu_factor_t<double>(nact, N, N + 1, (double*)L.J, ld, jstride, L.piv, L.info, s,
+                                             lu64_kernel_for(o->lu64_kernel));
             }));
             CKR(le);
             CKR(pf.run(PF_LUSOLVE, s, nact * (double)N * N, lsb, 1, [&] {

@@ -84,7 +84,10 @@ typedef struct {
                                      left-looking (n + 1 <= 512); 1: SIMT right-looking.
                                      Sizes a kernel does not take fall back to the library's
                                      choice                                                   */
-    int reserved[3];
+    int lu64_kernel;              /* FP64 factorizations (the plain form, and the mixed form's
+                                     FP64 lane): 0: the library's choice (6); 1: one CTA per
+                                     system; 6: each system split over many CTAs            */
+    int reserved[2];
 } bte_solve_opts;
 
 /* Options of the transient solve (the reference's args.dt / cycles / Efreq). */
@@ -210,7 +213,9 @@ int bte_lu_factor(int dtype, int P, int N, void* A, int ld, long long stride, in
  * 1 = right-looking for every N, 2 = FP32 only, N <= 512: trailing updates on the tcgen05
  * tensor cores in split TF32 (FP32-accurate factors), 3 = left-looking (N <= 512),
  * 4 = as 2 with one CTA per SM instead of two (fewer matrices in flight, kept in L2),
- * 5 = as 2 with 128 threads per CTA (less pivot-search work per matrix).
+ * 5 = as 2 with 128 threads per CTA (less pivot-search work per matrix),
+ * 6 = FP64 only: each factorization split over many CTAs (per panel: pivoting, triangular
+ *     solve, 64 x 64 trailing tiles as separate launches), for few large FP64 systems.
  * No counterpart in the reference; used to cross-check the factorizations. */
 int bte_lu_factor_ex(int dtype, int P, int N, void* A, int ld, long long stride, int32_t* piv, int32_t* info,
                      int kernel, void* stream);

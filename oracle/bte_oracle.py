@@ -722,6 +722,7 @@ def steady_state_iterations(ops: Operators, prm: Params, f0, atol, rtol, max_ite
     r0 = np.linalg.norm(res(h_prev), axis=0, ord=2)
     abs_error = r0.copy()
     it = 0
+    n_res = 1  # residual evaluations (the line search's trial steps dominate late iterations)
     h_curr = h_prev
     status = "max_iter"
     while (abs_error > atol + rtol * r0).any() and it < max_iter:
@@ -734,6 +735,7 @@ def steady_state_iterations(ops: Operators, prm: Params, f0, atol, rtol, max_ite
         alpha = np.ones(n_pts)
         diverged = False
         rf_new = 0.5 * np.linalg.norm(res(h_prev + alpha * p), axis=0, ord=2) ** 2
+        n_res += 2
         while (rf_new > 0.5 * abs_error ** 2 - line_search_c * alpha * abs_error ** 2).any():
             rc = rf_new > 0.5 * abs_error ** 2 - line_search_c * alpha * abs_error ** 2
             alpha[rc] *= alpha_rho
@@ -741,12 +743,14 @@ def steady_state_iterations(ops: Operators, prm: Params, f0, atol, rtol, max_ite
                 diverged = True
                 break
             rf_new = 0.5 * np.linalg.norm(res(h_prev + alpha * p), axis=0, ord=2) ** 2
+            n_res += 1
         if diverged:
             status = "line_search"
             break
         h_curr = h_prev + alpha * p
         if it % 10 == 0:
             abs_error = np.linalg.norm(res(h_curr), axis=0)
+            n_res += 1
             if log:
                 log(it, abs_error, abs_error / r0)
         h_prev = h_curr
@@ -757,7 +761,7 @@ def steady_state_iterations(ops: Operators, prm: Params, f0, atol, rtol, max_ite
     abs_error = np.linalg.norm(res(h_curr), axis=0)
     ff = normalized_distribution(ops, h_curr)
     qoi = compute_qois(ops, prm, ff, effective_mobility=True)
-    return ff, qoi, dict(iters=it, abs_error=abs_error, rel_error=abs_error / r0, status=status)
+    return ff, qoi, dict(iters=it, abs_error=abs_error, rel_error=abs_error / r0, status=status, res_evals=n_res)
 
 
 def processes_from_lxcat(path):

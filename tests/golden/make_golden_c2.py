@@ -33,7 +33,10 @@ the reference's Coulomb operator is rebuilt from its own trilinear tensors and t
 library's Rosenbluth potentials and the c2 points are solved again by the reference; the
 fixture gains `ff_device_rosenbluth` and `rosenbluth_swap_shift`.
 
-Usage:  python tests/golden/make_golden_c2.py [c2|c5] [--perturbed | --perturbed-mass | --swap-rosenbluth=FILE]
+With --exact (after the plain run), `exact()` below adds the exact fixed point of the
+reference's own discrete system: `ff_exact` and `exact_shift`.
+
+Usage:  python tests/golden/make_golden_c2.py [c2|c5] [--perturbed | --perturbed-mass | --swap-rosenbluth=FILE | --exact]
 """
 import os
 import sys
@@ -129,6 +132,63 @@ def _swap_rosenbluth(s, path):
     s._op_col_ee[0] = np.dot(Minv, cc.reshape((n, -1))).reshape((n, n, n))
 
 
+def exact(m, xs, name, n_sp, l_max, iters=6):
+    """The exact fixed point of the reference's own discrete system at the fixture's points.
+
+    The reference's Newton (bte_0d3v_batched.py:882-979) uses a Jacobian without two rank-one
+    terms: the derivative of the growth term's scalar n0 sum_s ns W x and of the Coulomb
+    logarithm (its dgamma_a_df term, :663, is commented out at :750-751 of jac_func). It
+    therefore converges linearly, and where the e-e term dominates its FP64 residual reaches
+    its rounding floor before the iterate reaches the fixed point. Here the reference's own
+    residual closure is evaluated in extended precision (np.longdouble, the operators being
+    the reference's FP64 arrays), and Newton corrections with the full Jacobian (the
+    reference's jac_func plus the two rank-one terms, FP64 solves) start from the reference's
+    stopped solution. The fixture gains `ff_exact`, `exact_shift` (the reference's own
+    distance from that fixed point, relative L2) and `exact_steps` (the last correction)."""
+    import utils as bte_utils
+    import scipy.constants as sc
+    g = dict(np.load(os.path.join(HERE, name)))
+    P = g["ff"].shape[1]
+    s, args = G.make_solver(m, xs, n_sp, l_max, True, P)
+    G.set_params(s, {k: g[k] for k in ("n0", "ne", "Tg", "E", "ns_by_n0")})
+    args.ee_collisions = 1
+    res_func, jac_func = s.get_rhs_and_jacobian(0, P)
+    Q = s._op_qmat[0]
+    vth = s._par_vth[0]
+    mw = bte_utils.get_maxwellian_3d(vth, 1)
+    u = s._op_mass[0] * mw(0) * vth ** 3
+    Wmat = np.einsum("v,svu->su", u, s._op_col_en[0])
+    c_ee = s._op_col_ee[0]
+    Mop, Top = s._op_mass[0], s._op_temp[0]
+    gam_c = sc.e ** 4 / (4 * np.pi * (sc.epsilon_0 * sc.electron_mass) ** 2) / vth ** 3
+    w = (g["n0"] * g["ns_by_n0"]).T @ Wmat  # (P, n): gradient of the growth term's scalar
+    h, _ = _state_of(s, g["ff"])
+    hl = h.astype(np.longdouble)
+    Ql = Q.astype(np.longdouble)
+    steps = None
+    for it in range(iters):
+        r = res_func(hl, 0, 0)
+        x = hl.astype(np.float64)
+        L = jac_func(x, 0, 0)
+        qx = Q.T @ x
+        qc = Q.T @ np.einsum("abc,bc->ac", np.dot(c_ee, x), x)
+        tx, mx = Top @ x, Mop @ x
+        for a in range(P):
+            grad = gam_c * 1.5 * (Top / tx[a] - Mop / mx[a])  # gradient of the Coulomb logarithm factor
+            L[a] = L[a] - np.outer(qx[:, a], Q.T @ w[a]) + g["ne"][a] * np.outer(qc[:, a], Q.T @ grad)
+        pp = np.linalg.solve(L, -np.asarray(r, dtype=np.float64).T[..., None])[..., 0].T
+        hl = hl + Ql @ pp.astype(np.longdouble)
+        steps = np.linalg.norm(pp, axis=0) / np.linalg.norm(h, axis=0)
+        print("%s exact: correction %d %s" % (name, it, np.array2string(steps, precision=2)), flush=True)
+    ffx = s.normalized_distribution(0, hl.astype(np.float64))
+    g["ff_exact"] = ffx
+    g["exact_shift"] = np.linalg.norm(g["ff"] - ffx, axis=0) / np.linalg.norm(ffx, axis=0)
+    g["exact_steps"] = steps
+    np.savez_compressed(os.path.join(HERE, name), **g)
+    print("%s: the reference's distance from the exact fixed point %s" % (
+        name, np.array2string(g["exact_shift"], precision=2)), flush=True)
+
+
 def run(m, xs, name, n_sp, l_max, points, perturb_seed=None, mode="ulps", swap=None):
     P = len(points)
     t0 = time.time()
@@ -194,6 +254,12 @@ def main():
     cwd = os.getcwd()
     m = import_reference()
     try:
+        if "--exact" in sys.argv:
+            if "c2" in which:
+                exact(m, xs, "c2_shape_reference.npz", 128, 2)
+            if "c5" in which:
+                exact(m, xs, "c5_reduced_reference.npz", 64, 4)
+            return
         if "c2" in which:
             run(m, xs, "c2_shape_reference.npz", 128, 2, C2_POINTS, seed, mode, swap)
         if "c5" in which:

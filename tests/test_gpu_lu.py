@@ -9,8 +9,10 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("N", [1, 7, 31, 64, 129, 385, 600, 1281])
 @pytest.mark.parametrize("dtype", ["f64", "f32"])
-@pytest.mark.parametrize("kernel", [0, 1, 2, 4, 5], ids=["auto", "right", "tc", "tc1", "tc128"])
+@pytest.mark.parametrize("kernel", [0, 1, 2, 4, 5, 6], ids=["auto", "right", "tc", "tc1", "tc128", "split"])
 def test_lu_factor_solve(N, dtype, kernel):
+    if kernel == 6 and dtype != "f64":
+        pytest.skip("the split kernel is FP64")
     if kernel in (2, 4, 5) and (dtype == "f64" or N > 512):
         pytest.skip("the tensor-core factorization is FP32 with N <= 512")
     import torch
@@ -63,6 +65,61 @@ def test_lu_zero_pivot_reported():
                                  C.c_void_p(info.data_ptr()), st), "lu_factor")
     torch.cuda.synchronize()
     assert int(info.item()) == 18
+
+
+@pytest.mark.parametrize("kernel", [0, 6], ids=["auto", "split"])
+def test_lu_zero_pivot_reported_fp64_kernels(kernel):
+    """The first zero pivot (1-based) in a later panel, from the one-CTA and the split FP64 kernels."""
+    import torch
+    from boltzmann_gb300 import _lib
+    lib = _lib.load()
+    N = 100
+    A = np.eye(N)
+    A[70, 70] = 0.0
+    dA = torch.as_tensor(np.stack([A, np.eye(N)]), device="cuda").contiguous()
+    piv = torch.empty((2, N), dtype=torch.int32, device="cuda")
+    info = torch.empty(2, dtype=torch.int32, device="cuda")
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.check(lib.bte_lu_factor_ex(0, 2, N, C.c_void_p(dA.data_ptr()), N, N * N, C.c_void_p(piv.data_ptr()),
+                                    C.c_void_p(info.data_ptr()), kernel, st), "lu_factor")
+    torch.cuda.synchronize()
+    assert info.cpu().numpy().tolist() == [71, 0]
+
+
+@pytest.mark.parametrize("N", [129, 385, 1281])
+def test_lu_split_matches_one_cta_kernel(N):
+    """The split FP64 factorization (kernel 6) of many matrices with the solver's padded rows
+    and appended right-hand side (NC = N + 1): the same pivots as the one-CTA kernel on
+    well-separated pivots, and factors that agree to FP64 rounding."""
+    import torch
+    from boltzmann_gb300 import _lib
+    lib = _lib.load()
+    P = 40
+    ld = N + 4
+    rng = np.random.default_rng(N + 5)
+    A = rng.standard_normal((P, N, ld))
+    out = []
+    for kernel in (1, 6):
+        dA = torch.as_tensor(A, device="cuda").contiguous()
+        piv = torch.empty((P, N), dtype=torch.int32, device="cuda")
+        info = torch.empty(P, dtype=torch.int32, device="cuda")
+        st = torch.cuda.current_stream().cuda_stream
+        _lib.check(lib.bte_lu_factor_ex(0, P, N, C.c_void_p(dA.data_ptr()), ld, N * ld, C.c_void_p(piv.data_ptr()),
+                                        C.c_void_p(info.data_ptr()), kernel, C.c_void_p(st)), "lu_factor")
+        torch.cuda.synchronize()
+        assert np.all(info.cpu().numpy() == 0)
+        out.append((dA.cpu().numpy(), piv.cpu().numpy()))
+    (a1, p1), (a6, p6) = out
+    assert np.array_equal(p1, p6)
+    # columns 0..N-1 hold L\U; the appended column is outside the factorization here (NC = N)
+    d = np.abs(a1[:, :, :N] - a6[:, :, :N]).max() / np.abs(a1[:, :, :N]).max()
+    assert d < 1e-11, d
+    for i in range(3):
+        LU = a6[i][p6[i], :N]
+        L = np.tril(LU, -1) + np.eye(N)
+        U = np.triu(LU)
+        berr = np.abs(L @ U - A[i][p6[i], :N]).max() / np.abs(A[i]).max()
+        assert berr < 50 * N * np.finfo(np.float64).eps, berr
 
 
 @pytest.mark.parametrize("dtype", ["f64", "f32"])
