@@ -832,24 +832,26 @@ class CpuReferenceRun:
                 "seconds": sec, "samples": self.done}
 
 
-# Newton iterations of the reference's batch-global loop on the cpu_baseline sample (the first
-# 4 points of the seeded c2 workload), measured by running it to its stop criterion (the
-# reference arm, --impl reference, does so every time): e-e off converges after 83 iterations,
-# e-e on runs to the 100-iteration cap.
-CPU_SAMPLE_ITERS = {(128, 2, 4): (83, 100)}
+# Counts of the reference's batch-global loop on the cpu_baseline sample (the first 4 points of
+# the seeded c2 workload), from running it to its stop criterion on the GPU host's cores (the
+# reference arm, --impl reference, does so every time and reports them): Newton iterations and
+# residual evaluations of the e-e-off and e-e-on phases. Late iterations backtrack their line
+# search many times at the FP64 floor, so most of the e-e-on time is residual evaluations.
+CPU_SAMPLE_COUNTS = {(128, 2, 4): {"iters": (83, 100), "res_evals": (1116, 3161)}}
 
 
-def cpu_baseline_run(a, iters_per_phase=3):
+def cpu_baseline_run(a, reps=3):
     """cpu_baseline of the GPU arm, a bounded sample (the whole solve of the sample takes about
-    ten minutes on the GPU machine's host; the reference arm runs it): `iters_per_phase` Newton
-    iterations of each phase of the same 4-point sample, timed, and scaled by the sample's
-    measured iteration counts (CPU_SAMPLE_ITERS)."""
+    ten minutes on the GPU host; the reference arm runs it): per phase of the same 4-point
+    sample, the closures' set-up, one Newton linear step (Jacobian, batched inverse, product)
+    and one residual evaluation of the oracle port of bte_0d3v_batched are timed, each `reps`
+    times, and combined with the sample's measured counts (CPU_SAMPLE_COUNTS)."""
     import multiprocessing
     from oracle import bte_oracle as O
     from boltzmann_gb300.workloads import write_synthetic_lxcat, batch_parameters, EV_MAX, TE_NORM
-    counts = CPU_SAMPLE_ITERS.get((a.n_sp, a.l_max, a.cpu_points))
+    counts = CPU_SAMPLE_COUNTS.get((a.n_sp, a.l_max, a.cpu_points))
     if counts is None:
-        return CpuReferenceRun(a, a.cpu_points).summary() | {"note": "no measured iteration counts for this sample"}
+        return CpuReferenceRun(a, a.cpu_points).summary() | {"note": "no measured counts for this sample"}
     xs = write_synthetic_lxcat()
     t0 = time.perf_counter()
     try:
@@ -861,22 +863,33 @@ def cpu_baseline_run(a, iters_per_phase=3):
     sl = slice(0, a.cpu_points)
     P = O.Params(prm["n0"][sl], prm["ne"][sl], prm["Tg"][sl], prm["E"][sl], prm["ns_by_n0"][:, sl])
     f0 = O.maxwellian_initial(ops, a.cpu_points)
-    per_iter = []
-    for ee in (False, True):
-        gen = O.steady_state_iterations(ops, P, f0, ATOL, RTOL, MAXIT, ee, ALPHA_MIN, ALPHA_RHO, LS_C)
-        next(gen)  # the first iteration includes the closures' set-up
+    h = f0 / np.dot(ops.u, f0)
+    parts, sec = [], 0.0
+    for k, ee in enumerate((False, True)):
         t1 = time.perf_counter()
-        for _ in range(iters_per_phase):
-            next(gen)
-        per_iter.append((time.perf_counter() - t1) / iters_per_phase)
-    sec = per_iter[0] * counts[0] + per_iter[1] * counts[1]
+        res, jac, _ = O.rhs_and_jacobian(ops, P, ee)
+        t_close = time.perf_counter() - t1
+        r = res(h)
+        t1 = time.perf_counter()
+        for _ in range(reps):
+            Linv = np.linalg.inv(jac(h))
+            np.dot(ops.Qmat, np.einsum("abc,ca->ba", Linv, -r))
+        t_step = (time.perf_counter() - t1) / reps
+        t1 = time.perf_counter()
+        for _ in range(reps):
+            res(h)
+        t_res = (time.perf_counter() - t1) / reps
+        sec += t_close + counts["iters"][k] * t_step + counts["res_evals"][k] * t_res
+        parts.append({"closures_s": t_close, "step_s": t_step, "residual_s": t_res})
     return {"value": a.cpu_points / sec, "unit": UNIT, "cores": multiprocessing.cpu_count(), "kind": "port",
-            "sample": "%d points of the seeded c2 workload: %d Newton iterations of each phase (e-e off, e-e on) of "
-                      "the oracle port of bte_0d3v_batched (NumPy, OpenBLAS on all host threads) timed, %.2f s and "
-                      "%.2f s per iteration, scaled by the sample's measured iteration counts %s (the reference arm "
-                      "runs the sample to its stop criterion); operator set-up %.1f s not timed"
-                      % (a.cpu_points, iters_per_phase, per_iter[0], per_iter[1], list(counts), t_setup),
-            "seconds_per_iteration": per_iter, "iterations": list(counts)}
+            "sample": "%d points of the seeded c2 workload through the oracle port of bte_0d3v_batched (NumPy, "
+                      "OpenBLAS on all host threads): per phase (e-e off, e-e on) the closures' set-up, one Newton "
+                      "step (%.3f s, %.3f s) and one residual evaluation (%.3f s, %.3f s) timed, combined with the "
+                      "sample's measured counts: iterations %s, residual evaluations %s (the reference arm runs the "
+                      "sample to its stop criterion); operator set-up %.1f s not timed"
+                      % (a.cpu_points, parts[0]["step_s"], parts[1]["step_s"], parts[0]["residual_s"],
+                         parts[1]["residual_s"], list(counts["iters"]), list(counts["res_evals"]), t_setup),
+            "seconds_per_sample": sec, "phases": parts, "counts": counts}
 
 
 def _autotune_report():

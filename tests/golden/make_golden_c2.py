@@ -28,13 +28,15 @@ With --perturbed-mass, the perturbation is one rounding unit on each mass-matrix
 carried through the reference's M^-1 scaling of its operators; the fixture gains
 `ff_perturbed_mass` and `resolution_mass`.
 
-With --swap-rosenbluth=FILE (c2 only; FILE from export_device_rosenbluth.py on a GPU host),
-the reference's Coulomb operator is rebuilt from its own trilinear tensors and the device
-library's Rosenbluth potentials and the c2 points are solved again by the reference; the
-fixture gains `ff_device_rosenbluth` and `rosenbluth_swap_shift`.
+With --swap-rosenbluth=FILE (one fixture; FILE from export_device_rosenbluth.py on a GPU host,
+for that fixture's grid), the reference's Coulomb operator is rebuilt from its own trilinear
+tensors and the device library's Rosenbluth potentials and the points are solved again by the
+reference; the fixture gains `ff_device_rosenbluth` and `rosenbluth_swap_shift`.
 
-With --exact (after the plain run), `exact()` below adds the exact fixed point of the
-reference's own discrete system: `ff_exact` and `exact_shift`.
+With --exact (after the plain run), `exact()` below adds the exact fixed points of the
+reference's own discrete systems: `ff_warm_exact`, `ff_exact`, `warm_exact_shift`, `exact_shift`;
+with --exact --swap-rosenbluth=FILE (after --swap-rosenbluth), the e-e-on fixed point of the
+system built with the device potentials: `ff_exact_device_rosenbluth`.
 
 Usage:  python tests/golden/make_golden_c2.py [c2|c5] [--perturbed | --perturbed-mass | --swap-rosenbluth=FILE | --exact]
 """
@@ -132,8 +134,9 @@ def _swap_rosenbluth(s, path):
     s._op_col_ee[0] = np.dot(Minv, cc.reshape((n, -1))).reshape((n, n, n))
 
 
-def exact(m, xs, name, n_sp, l_max, iters=6):
-    """The exact fixed point of the reference's own discrete system at the fixture's points.
+def exact(m, xs, name, n_sp, l_max, iters=6, swap=None):
+    """The exact fixed points of the reference's own discrete systems at the fixture's points,
+    for both phases of the driver sequence (e-e off: `ff_warm`, e-e on: `ff`).
 
     The reference's Newton (bte_0d3v_batched.py:882-979) uses a Jacobian without two rank-one
     terms: the derivative of the growth term's scalar n0 sum_s ns W x and of the Coulomb
@@ -142,17 +145,22 @@ def exact(m, xs, name, n_sp, l_max, iters=6):
     its rounding floor before the iterate reaches the fixed point. Here the reference's own
     residual closure is evaluated in extended precision (np.longdouble, the operators being
     the reference's FP64 arrays), and Newton corrections with the full Jacobian (the
-    reference's jac_func plus the two rank-one terms, FP64 solves) start from the reference's
-    stopped solution. The fixture gains `ff_exact`, `exact_shift` (the reference's own
-    distance from that fixed point, relative L2) and `exact_steps` (the last correction)."""
+    reference's jac_func plus the rank-one terms, FP64 solves) start from the reference's
+    stopped solution. The fixture gains `ff_exact` / `ff_warm_exact`, `exact_shift` /
+    `warm_exact_shift` (the reference's own distance from that fixed point, relative L2) and
+    `exact_steps` / `warm_exact_steps` (the size of the last correction).
+
+    With `swap` (the device library's Rosenbluth potentials, as for --swap-rosenbluth), the
+    e-e-on fixed point of the reference's system built with those potentials is computed from
+    the reference's answer with them (`ff_device_rosenbluth`): `ff_exact_device_rosenbluth`."""
     import utils as bte_utils
     import scipy.constants as sc
     g = dict(np.load(os.path.join(HERE, name)))
     P = g["ff"].shape[1]
     s, args = G.make_solver(m, xs, n_sp, l_max, True, P)
+    if swap is not None:
+        _swap_rosenbluth(s, swap)
     G.set_params(s, {k: g[k] for k in ("n0", "ne", "Tg", "E", "ns_by_n0")})
-    args.ee_collisions = 1
-    res_func, jac_func = s.get_rhs_and_jacobian(0, P)
     Q = s._op_qmat[0]
     vth = s._par_vth[0]
     mw = bte_utils.get_maxwellian_3d(vth, 1)
@@ -162,31 +170,40 @@ def exact(m, xs, name, n_sp, l_max, iters=6):
     Mop, Top = s._op_mass[0], s._op_temp[0]
     gam_c = sc.e ** 4 / (4 * np.pi * (sc.epsilon_0 * sc.electron_mass) ** 2) / vth ** 3
     w = (g["n0"] * g["ns_by_n0"]).T @ Wmat  # (P, n): gradient of the growth term's scalar
-    h, _ = _state_of(s, g["ff"])
-    hl = h.astype(np.longdouble)
-    Ql = Q.astype(np.longdouble)
-    steps = None
-    for it in range(iters):
-        r = res_func(hl, 0, 0)
-        x = hl.astype(np.float64)
-        L = jac_func(x, 0, 0)
-        qx = Q.T @ x
-        qc = Q.T @ np.einsum("abc,bc->ac", np.dot(c_ee, x), x)
-        tx, mx = Top @ x, Mop @ x
-        for a in range(P):
-            grad = gam_c * 1.5 * (Top / tx[a] - Mop / mx[a])  # gradient of the Coulomb logarithm factor
-            L[a] = L[a] - np.outer(qx[:, a], Q.T @ w[a]) + g["ne"][a] * np.outer(qc[:, a], Q.T @ grad)
-        pp = np.linalg.solve(L, -np.asarray(r, dtype=np.float64).T[..., None])[..., 0].T
-        hl = hl + Ql @ pp.astype(np.longdouble)
-        steps = np.linalg.norm(pp, axis=0) / np.linalg.norm(h, axis=0)
-        print("%s exact: correction %d %s" % (name, it, np.array2string(steps, precision=2)), flush=True)
-    ffx = s.normalized_distribution(0, hl.astype(np.float64))
-    g["ff_exact"] = ffx
-    g["exact_shift"] = np.linalg.norm(g["ff"] - ffx, axis=0) / np.linalg.norm(ffx, axis=0)
-    g["exact_steps"] = steps
+    phases = ((0, "ff_warm", "warm_exact"), (1, "ff", "exact"))
+    if swap is not None:
+        phases = ((1, "ff_device_rosenbluth", "exact_device_rosenbluth"),)
+    for ee, key, out in phases:
+        args.ee_collisions = ee
+        res_func, jac_func = s.get_rhs_and_jacobian(0, P)
+        h, _ = _state_of(s, g[key])
+        hl = h.astype(np.longdouble)
+        Ql = Q.astype(np.longdouble)
+        steps = None
+        for it in range(iters):
+            r = res_func(hl, 0, 0)
+            x = hl.astype(np.float64)
+            L = jac_func(x, 0, 0)
+            qx = Q.T @ x
+            if ee:
+                qc = Q.T @ np.einsum("abc,bc->ac", np.dot(c_ee, x), x)
+                tx, mx = Top @ x, Mop @ x
+            for a in range(P):
+                L[a] = L[a] - np.outer(qx[:, a], Q.T @ w[a])
+                if ee:  # gradient of the Coulomb logarithm factor
+                    grad = gam_c * 1.5 * (Top / tx[a] - Mop / mx[a])
+                    L[a] = L[a] + g["ne"][a] * np.outer(qc[:, a], Q.T @ grad)
+            pp = np.linalg.solve(L, -np.asarray(r, dtype=np.float64).T[..., None])[..., 0].T
+            hl = hl + Ql @ pp.astype(np.longdouble)
+            steps = np.linalg.norm(pp, axis=0) / np.linalg.norm(h, axis=0)
+            print("%s %s: correction %d %s" % (name, out, it, np.array2string(steps, precision=2)), flush=True)
+        ffx = s.normalized_distribution(0, hl.astype(np.float64))
+        g[(key + "_exact") if swap is None else "ff_exact_device_rosenbluth"] = ffx
+        g[out + "_shift"] = np.linalg.norm(g[key] - ffx, axis=0) / np.linalg.norm(ffx, axis=0)
+        g[out + "_steps"] = steps
+        print("%s: the reference's distance from the exact fixed point (%s) %s" % (
+            name, key, np.array2string(g[out + "_shift"], precision=2)), flush=True)
     np.savez_compressed(os.path.join(HERE, name), **g)
-    print("%s: the reference's distance from the exact fixed point %s" % (
-        name, np.array2string(g["exact_shift"], precision=2)), flush=True)
 
 
 def run(m, xs, name, n_sp, l_max, points, perturb_seed=None, mode="ulps", swap=None):
@@ -250,20 +267,22 @@ def main():
     swap = next((a.split("=", 1)[1] for a in sys.argv if a.startswith("--swap-rosenbluth=")), None)
     if swap is not None:
         swap = os.path.abspath(swap)
+        if len(which) != 1:
+            raise SystemExit("--swap-rosenbluth takes one fixture (c2 or c5): the potentials are per grid")
     xs = write_synthetic_lxcat(os.path.join("/tmp", "eAr_golden_%d.lxcat" % os.getpid()))
     cwd = os.getcwd()
     m = import_reference()
     try:
         if "--exact" in sys.argv:
             if "c2" in which:
-                exact(m, xs, "c2_shape_reference.npz", 128, 2)
+                exact(m, xs, "c2_shape_reference.npz", 128, 2, swap=swap)
             if "c5" in which:
-                exact(m, xs, "c5_reduced_reference.npz", 64, 4)
+                exact(m, xs, "c5_reduced_reference.npz", 64, 4, swap=swap)
             return
         if "c2" in which:
             run(m, xs, "c2_shape_reference.npz", 128, 2, C2_POINTS, seed, mode, swap)
         if "c5" in which:
-            run(m, xs, "c5_reduced_reference.npz", 64, 4, C5_POINTS, seed, mode)
+            run(m, xs, "c5_reduced_reference.npz", 64, 4, C5_POINTS, seed, mode, swap)
     finally:
         os.chdir(cwd)
         os.unlink(xs)
