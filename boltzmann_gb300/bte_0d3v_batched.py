@@ -19,7 +19,8 @@ Differences a caller can observe:
     for the grid's size once and the fastest is used;
   * `args.krylov` (mixed form) chooses when a point whose FP64 refinement stalls gets
     GMRES on its FP32 factors before it goes to FP64: 0 for bordered sizes above 512
-    (default), 1 always, 2 for every point (diagnostics), -1 never;
+    (default), 1 always, 2 for every point (diagnostics), -1 never; `args.lu64_kernel` the FP64 factorization (0: split
+    over many CTAs per system, 1: one CTA per system);
   * failures raise RuntimeError instead of calling sys.exit.
 """
 from __future__ import annotations

@@ -122,31 +122,56 @@ __global__ void k_fvm_coll_apply(FvmView v, const double* __restrict__ dinv, con
 // D[i][i-k] = L[k][i-k], upper D[i][i+k] = R[k][i+k], rawkernel.py:168-375); the last nd - 1
 // outputs of the line stay in registers. Along v_r (stride Nvt Nx) and v_theta (stride Nx)
 // the threads of a warp take consecutive x, so every step is one coalesced 256-byte access:
-// no layout swaps, unlike the reference's sweeps on permuted copies.
+// no layout swaps, unlike the reference's sweeps on permuted copies. L and R are the calling
+// CTA's shared-memory copies of the bands (stage_bands), so a step waits on no global load but
+// its right-hand side, which is loaded SW_PF steps ahead.
 constexpr int SW_NDMAX = 4;
-constexpr int SW_PF = 4;   // right-hand sides loaded ahead of the recurrence
-__device__ inline void fvm_sweep_line(const double* __restrict__ L, const double* __restrict__ R, int nd, int N,
-                                      double ad, bool ltr, double* __restrict__ v, long long stride) {
+constexpr int SW_PF = 8;   // right-hand sides loaded ahead of the recurrence
+__device__ inline void stage_bands(const double* __restrict__ L, const double* __restrict__ R, int nd, int N,
+                                   double* sL, double* sR) {
+    for (int e = threadIdx.x; e < nd * N; e += blockDim.x) {
+        sL[e] = L[e];
+        sR[e] = R[e];
+    }
+}
+// With rc (the reciprocals of the line's diagonal 1 + ad D[i][i], at the same positions as v,
+// k_fvm_diag_rcp) a step is five FP64 operations instead of a division's dozen: the few long
+// v_r and x lines run one warp per SM, each bound by its SM sub-partition's FP64 issue rate.
+template <bool RC>
+__device__ inline void fvm_sweep_line(const double* L, const double* R, int nd, int N,
+                                      double ad, bool ltr, double* __restrict__ v, long long stride,
+                                      const double* __restrict__ rc = nullptr) {
     double prev[SW_NDMAX - 1];
 #pragma unroll
     for (int k = 0; k < SW_NDMAX - 1; ++k) prev[k] = 0.0;
     const double* B = ltr ? L : R;
-    // the loads of b do not depend on the recurrence: keep SW_PF of them in flight
-    double pf[SW_PF];
+    // the loads of b (and of the reciprocals) do not depend on the recurrence: keep SW_PF of
+    // them in flight
+    double pf[SW_PF], pr[SW_PF];
 #pragma unroll
-    for (int q = 0; q < SW_PF; ++q) pf[q] = (q < N) ? v[(long long)(ltr ? q : N - 1 - q) * stride] : 0.0;
+    for (int q = 0; q < SW_PF; ++q) {
+        const long long o = (long long)(ltr ? q : N - 1 - q) * stride;
+        pf[q] = (q < N) ? v[o] : 0.0;
+        if (RC) pr[q] = (q < N) ? rc[o] : 0.0;
+    }
     for (int step = 0; step < N; ++step) {
         const int i = ltr ? step : N - 1 - step;
         const double bi = pf[0];
+        const double ri = RC ? pr[0] : 0.0;
 #pragma unroll
-        for (int q = 0; q < SW_PF - 1; ++q) pf[q] = pf[q + 1];
+        for (int q = 0; q < SW_PF - 1; ++q) {
+            pf[q] = pf[q + 1];
+            if (RC) pr[q] = pr[q + 1];
+        }
         const int nxt = step + SW_PF;
-        pf[SW_PF - 1] = (nxt < N) ? v[(long long)(ltr ? nxt : N - 1 - nxt) * stride] : 0.0;
+        const long long on = (long long)(ltr ? nxt : N - 1 - nxt) * stride;
+        pf[SW_PF - 1] = (nxt < N) ? v[on] : 0.0;
+        if (RC) pr[SW_PF - 1] = (nxt < N) ? rc[on] : 0.0;
         double sacc = 0.0;
 #pragma unroll
         for (int k = 1; k < SW_NDMAX; ++k)
-            if (k < nd && step >= k) sacc += __ldg(B + (size_t)k * N + (ltr ? i - k : i + k)) * prev[k - 1];
-        const double o = (bi - ad * sacc) / (1.0 + ad * __ldg(B + i));
+            if (k < nd && step >= k) sacc += B[(size_t)k * N + (ltr ? i - k : i + k)] * prev[k - 1];
+        const double o = RC ? (bi - ad * sacc) * ri : (bi - ad * sacc) / (1.0 + ad * B[i]);
 #pragma unroll
         for (int k = SW_NDMAX - 2; k > 0; --k) prev[k] = prev[k - 1];
         prev[0] = o;
@@ -154,22 +179,55 @@ __device__ inline void fvm_sweep_line(const double* __restrict__ L, const double
     }
 }
 
+// Rc = 1 / (1 + a h D[i][i]) at every position of the natural layout, for the v_r sweep
+// (which = 0: a and the band as k_fvm_sweep_vr takes them, i = r) or the x sweep (which = 2:
+// as k_fvm_sweep_x, i = x); all SMs share the divisions the recurrences would serialise
+__global__ void k_fvm_diag_rcp(FvmView v, int which, const double* __restrict__ aE,
+                               const double* __restrict__ axvr, double h, double* __restrict__ Rc) {
+    const size_t o = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t n = (size_t)v.Nr * v.Nvt * v.Nx;
+    if (o >= n) return;
+    const int x = (int)(o % v.Nx);
+    const size_t rj = o / v.Nx;
+    const int j = (int)(rj % v.Nvt), r = (int)(rj / v.Nvt);
+    double a, d;
+    if (which == 0) {
+        a = -aE[x] * v.cos_t[j];
+        d = (a >= 0.0 ? v.vrL : v.vrR)[r];
+    } else {
+        a = axvr[r] * v.cos_t[j];
+        d = (a >= 0.0 ? v.xL : v.xR)[x];
+    }
+    const double ad = a * h;
+    Rc[o] = 1.0 / (1.0 + ad * d);
+}
+
 // v_r sweep: line (j, x), a = -aE[x] cos(theta_j), left to right when a >= 0 (rawkernel.py:168-230)
-__global__ void k_fvm_sweep_vr(FvmView v, const double* __restrict__ aE, double h, double* __restrict__ V) {
+__global__ void k_fvm_sweep_vr(FvmView v, const double* __restrict__ aE, double h, double* __restrict__ V,
+                               const double* __restrict__ Rc) {
+    extern __shared__ double sband[];  // [2][ndr][Nr]
+    double *sL = sband, *sR = sband + (size_t)v.ndr * v.Nr;
+    stage_bands(v.vrL, v.vrR, v.ndr, v.Nr, sL, sR);
+    __syncthreads();
     const int line = blockIdx.x * blockDim.x + threadIdx.x;
     if (line >= v.Nvt * v.Nx) return;
     const int j = line / v.Nx, x = line % v.Nx;
     const double a = -aE[x] * v.cos_t[j];
-    fvm_sweep_line(v.vrL, v.vrR, v.ndr, v.Nr, a * h, a >= 0.0, V + (size_t)j * v.Nx + x, (long long)v.Nvt * v.Nx);
+    fvm_sweep_line<true>(sL, sR, v.ndr, v.Nr, a * h, a >= 0.0, V + (size_t)j * v.Nx + x, (long long)v.Nvt * v.Nx,
+                         Rc + (size_t)j * v.Nx + x);
 }
 
 // v_theta sweep: line (r, x), a = aE[x] / v_r, left to right when -a >= 0 (rawkernel.py:232-296)
 __global__ void k_fvm_sweep_vt(FvmView v, const double* __restrict__ aE, double h, double* __restrict__ V) {
+    extern __shared__ double sband[];  // [2][ndt][Nvt]
+    double *sL = sband, *sR = sband + (size_t)v.ndt * v.Nvt;
+    stage_bands(v.vtL, v.vtR, v.ndt, v.Nvt, sL, sR);
+    __syncthreads();
     const int line = blockIdx.x * blockDim.x + threadIdx.x;
     if (line >= v.Nr * v.Nx) return;
     const int r = line / v.Nx, x = line % v.Nx;
     const double a = aE[x] / v.vr[r];
-    fvm_sweep_line(v.vtL, v.vtR, v.ndt, v.Nvt, a * h, -a >= 0.0, V + (size_t)r * v.Nvt * v.Nx + x, (long long)v.Nx);
+    fvm_sweep_line<false>(sL, sR, v.ndt, v.Nvt, a * h, -a >= 0.0, V + (size_t)r * v.Nvt * v.Nx + x, (long long)v.Nx);
 }
 
 // x sweep with the inflow values zeroed first: line (r, j) is a contiguous row of Nx values;
@@ -180,9 +238,13 @@ __global__ void k_fvm_sweep_vt(FvmView v, const double* __restrict__ aE, double 
 constexpr int XT_L = 32;       // rows per CTA
 constexpr int XT_T = 256;      // threads per CTA: all load and store, the first XT_L sweep
 __global__ void __launch_bounds__(XT_T) k_fvm_sweep_x(FvmView v, const double* __restrict__ axvr, double h,
-                                                      const double* __restrict__ B, double* __restrict__ Y) {
-    extern __shared__ double rows[];  // [XT_L][Nx + 1]
+                                                      const double* __restrict__ B, double* __restrict__ Y,
+                                                      const double* __restrict__ Rc) {
+    extern __shared__ double rows[];  // [XT_L][Nx + 1], then the bands [2][ndx][Nx]
     const int Nx = v.Nx, pitch = Nx + 1;
+    double* sL = rows + (size_t)XT_L * pitch;
+    double* sR = sL + (size_t)v.ndx * Nx;
+    stage_bands(v.xL, v.xR, v.ndx, Nx, sL, sR);
     const int nlines = v.Nr * v.Nvt;
     const int l0 = blockIdx.x * XT_L;
     const int nl = min(XT_L, nlines - l0);
@@ -198,7 +260,8 @@ __global__ void __launch_bounds__(XT_T) k_fvm_sweep_x(FvmView v, const double* _
         const int line = l0 + threadIdx.x;
         const int r = line / v.Nvt, j = line % v.Nvt;
         const double a = axvr[r] * v.cos_t[j];
-        fvm_sweep_line(v.xL, v.xR, v.ndx, Nx, a * h, a >= 0.0, rows + threadIdx.x * pitch, 1);
+        fvm_sweep_line<true>(sL, sR, v.ndx, Nx, a * h, a >= 0.0, rows + threadIdx.x * pitch, 1,
+                             Rc + (size_t)line * Nx);
     }
     __syncthreads();
     double* dst = Y + (size_t)l0 * Nx;
@@ -309,8 +372,10 @@ int fvm_precond(bte_fvm* h, double hstep, const double* X, double* Y, cudaStream
     k_fvm_moment<<<fblocks(nrx), FT, 0, s>>>(v, X, h->M);
     if (int rc = launched("k_fvm_moment")) return rc;
     if (int rc = sweep_rc(bte_dgemm_nn(Nr, Nx, Nr, h->H, Nr, h->M, Nx, h->T, Nx, s), "collision inverse")) return rc;
-    const size_t xsm = (size_t)XT_L * (Nx + 1) * sizeof(double);
-    if (h->ndr > SW_NDMAX || h->ndt > SW_NDMAX || h->ndx > SW_NDMAX || xsm > 200 * 1024) {
+    const size_t xsm = ((size_t)XT_L * (Nx + 1) + 2 * (size_t)h->ndx * Nx) * sizeof(double);
+    const size_t rsm = 2 * (size_t)h->ndr * Nr * sizeof(double), tsm = 2 * (size_t)h->ndt * Nvt * sizeof(double);
+    if (h->ndr > SW_NDMAX || h->ndt > SW_NDMAX || h->ndx > SW_NDMAX || xsm > 200 * 1024 || rsm > 200 * 1024 ||
+        tsm > 200 * 1024) {
         // stencils wider than the register recurrence or x lines longer than the staged rows:
         // the drop-in sweeps on permuted copies
         k_fvm_coll_permute<<<fblocks(h->N), FT, 0, s>>>(v, h->dinv, h->T, X, h->A);   // (Nx, Nvt, Nr)
@@ -333,14 +398,21 @@ int fvm_precond(bte_fvm* h, double hstep, const double* X, double* Y, cudaStream
     if (int rc = launched("k_fvm_coll_apply")) return rc;
     // the three sweeps in place on the natural layout, coalesced (no layout swaps)
     // the v_r lines are few (Nvt Nx) and long: small CTAs spread them over the SMs
-    k_fvm_sweep_vr<<<(unsigned)(((size_t)Nvt * Nx + 31) / 32), 32, 0, s>>>(v, h->aE, hstep, h->A);
+    if (bte_raise_smem_limit((const void*)k_fvm_sweep_vr, rsm) != cudaSuccess ||
+        bte_raise_smem_limit((const void*)k_fvm_sweep_vt, tsm) != cudaSuccess ||
+        bte_raise_smem_limit((const void*)k_fvm_sweep_x, xsm) != cudaSuccess)
+        return fvm_fail(BTE_ERR_ARG, "sweep lines too long for the shared-memory sweeps");
+    // h->Bf (the drop-in path's scratch) holds the diagonal reciprocals of the v_r, then the x sweep
+    k_fvm_diag_rcp<<<fblocks(h->N), FT, 0, s>>>(v, 0, h->aE, h->axvr, hstep, h->Bf);
+    if (int rc = launched("k_fvm_diag_rcp")) return rc;
+    k_fvm_sweep_vr<<<(unsigned)(((size_t)Nvt * Nx + 31) / 32), 32, rsm, s>>>(v, h->aE, hstep, h->A, h->Bf);
     if (int rc = launched("k_fvm_sweep_vr")) return rc;
-    k_fvm_sweep_vt<<<fblocks((size_t)Nr * Nx), FT, 0, s>>>(v, h->aE, hstep, h->A);
+    k_fvm_sweep_vt<<<fblocks((size_t)Nr * Nx), FT, tsm, s>>>(v, h->aE, hstep, h->A);
     if (int rc = launched("k_fvm_sweep_vt")) return rc;
-    if (bte_raise_smem_limit((const void*)k_fvm_sweep_x, xsm) != cudaSuccess)
-        return fvm_fail(BTE_ERR_ARG, "x lines too long for the shared-memory sweep");
-    k_fvm_sweep_x<<<(unsigned)((Nr * Nvt + XT_L - 1) / XT_L), XT_T, xsm, s>>>(v, h->axvr, hstep, h->A, Y);
-    h->launches += 6;
+    k_fvm_diag_rcp<<<fblocks(h->N), FT, 0, s>>>(v, 2, h->aE, h->axvr, hstep, h->Bf);
+    if (int rc = launched("k_fvm_diag_rcp")) return rc;
+    k_fvm_sweep_x<<<(unsigned)((Nr * Nvt + XT_L - 1) / XT_L), XT_T, xsm, s>>>(v, h->axvr, hstep, h->A, Y, h->Bf);
+    h->launches += 8;
     return launched("k_fvm_sweep_x");
 }
 

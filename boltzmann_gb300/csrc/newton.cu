@@ -485,10 +485,12 @@ __global__ void k_refine_first(int nact, const int* __restrict__ act, const doub
 // ---------------------------------------------------------------------------------
 constexpr int GM_M = 20;
 constexpr int GM_CAP = 512;  // points per GMRES batch
-// GMRES refinement runs for bordered sizes above this. At c2's N = 385 it resolved all but
-// 12 of the ~200 stalled points per step but cost more than their FP64 factorizations
-// (7,580 against 8,210 solves/s: the refined points kept the Newton tail longer); an FP64
-// factorization costs N^3 and a GMRES iteration N^2, so above N = 512 it pays.
+// GMRES refinement runs by default for bordered sizes above this. At c2's N = 385 it resolves
+// all but 7 to 10 of the ~207 points per solve whose refinement stalls (9,350 to 9,590 against
+// 9,150 solves/s with their FP64 factorizations), but it left 8 points 1e-7 to 8e-7 from
+// plain FP64 (GM_TOL = 1e-8), where the FP64 hand-over keeps the mixed form's differences
+// within FP64's own spread; a tighter GM_TOL (1e-12) helped at c2 but moved c5 points by up
+// to 4e-2 (over-solving the flexible GMRES past its attainable accuracy).
 constexpr int GM_MIN_N = 513;
 // status of a point GMRES did not resolve, until all batches are done (k_gm_finalize makes it
 // NEED_FP64); not negative, so the point is not running, and not NEED_FP64, so that a later
@@ -1063,6 +1065,9 @@ __global__ void k_armijo(int nact, const int* __restrict__ act, int* searching, 
         return;
     }
     if (al == 1.0 && (rr <= stagnate_rtol * r0[pt] || tiny)) {
+        // the merit no longer resolves the full step's effect: the solve ends without it.
+        // (Taking a tiny last step anyway moved the Coulomb-dominated points of the c2-shape
+        // fixture by their rounding floor, 1e-9, in either direction: no gain.)
         searching[pt] = 0;
         accepted[pt] = 0;
         status[pt] = BTE_ST_ROUNDOFF;
