@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--steps-1d", type=int, default=20)
     ap.add_argument("--steps-fvm", type=int, default=10)
     ap.add_argument("--no-fvm", action="store_true", help="skip the finite-volume 1D3V leg")
+    ap.add_argument("--no-ref-points", action="store_true",
+                    help="skip the errors against the reference's answers at the c2-shape fixture points")
     ap.add_argument("--krylov", type=int, default=0,
                     help="mixed form: GMRES on the FP32 factors before an FP64 hand-over (bte_solve_opts.krylov)")
     ap.add_argument("--refine", type=int, default=4, help="mixed form: FP64 refinement passes per Newton step")
@@ -939,7 +941,7 @@ def main():
     one_d = None if (a.no_1d or ws > 1) else bench_1d(a, peaks)
     fvm = None if (a.no_fvm or ws > 1) else bench_fvm(a, peaks)
     c5 = None if (a.c5_points <= 0 or ws > 1) else bench_c5(a)
-    ref_pts = None if ws > 1 else bench_reference_points(a)
+    ref_pts = None if (ws > 1 or a.no_ref_points) else bench_reference_points(a)
     cpu = None if a.no_cpu else cpu_baseline_run(a)
     st = r["stats"]
     steps_ms = sorted(r["steps_ms"])
