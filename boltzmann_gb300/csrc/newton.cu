@@ -53,6 +53,92 @@ struct PointParams {
 enum { SC_GAMMA = 0, SC_MU, SC_T0, SC_M0, SC_NE, SC_COUNT = 8 };
 
 // ---------------------------------------------------------------------------------
+// Double-double accumulation (the residual of a point at its FP64 rounding floor): an exact
+// product (fma) and a compensated sum per term, rounded once at the end of a row.
+// ---------------------------------------------------------------------------------
+__device__ inline void dd_acc(double& hi, double& lo, double a, double b) {
+    const double pr = a * b, pe = fma(a, b, -pr);
+    const double sm = hi + pr, v = sm - hi, e = (hi - (sm - v)) + (pr - v);
+    hi = sm;
+    lo += e + pe;
+}
+__device__ inline void dd_acc2(double& hi, double& lo, double ahi, double alo, double b) {
+    dd_acc(hi, lo, ahi, b);
+    lo += alo * b;
+}
+
+// One row (mode q, spline p) of F_raw in double-double: the terms of k_residual's FP64 rows
+// (electron-heavy collisions, gas temperature, advection, growth, e-e) with the Rosenbluth
+// products shh/sgg given as hi + lo. Returns the row and its U and M h parts, rounded.
+__device__ void residual_row_dd(const GridView& g, const PointParams& pp, int pt, int ee, int q, int p,
+                                const double* sh, const double* shh, const double* shl, const double* sgg,
+                                const double* sgl, double n0, double Tg, double cadv, double mu, double negam,
+                                double& y, double& Uo, double& mho) {
+    const int nsh = g.nsh, nsp = g.nsp;
+    double yh = 0.0, yl = 0.0;
+    for (int s = 0; s < g.nspecies; ++s) {
+        const double ns = n0 * pp.ns[(size_t)s * pp.P + pt];
+        double ah = 0.0, al = 0.0;
+        if (q == 0) {
+            const double* row = g.q0 + ((size_t)s * nsp + p) * nsp;
+            for (int k = 0; k < nsp; ++k) dd_acc(ah, al, row[k], sh[k * nsh]);
+        } else {
+            const double* row = g.q1 + ((size_t)s * nsp + p) * BTE_NB;
+            for (int dk = -BTE_BAND; dk <= BTE_BAND; ++dk) {
+                const int k = p + dk;
+                if (k >= 0 && k < nsp) dd_acc(ah, al, row[dk + BTE_BAND], sh[k * nsh + q]);
+            }
+        }
+        dd_acc2(yh, yl, ah, al, ns);
+    }
+    double gh = 0.0, gl = 0.0, vh = 0.0, vl = 0.0, mh = 0.0, ml = 0.0;
+    for (int dk = -BTE_BAND; dk <= BTE_BAND; ++dk) {
+        const int k = p + dk;
+        if (k < 0 || k >= nsp) continue;
+        const int bi = p * BTE_NB + dk + BTE_BAND;
+        if (q == 0) dd_acc(gh, gl, g.cgT[bi], sh[k * nsh]);
+        if (q + 1 <= g.lmax) {
+            const double a = g.mm1[bi] * g.adv_coef[q * 4 + 0] + g.adv_coef[q * 4 + 1] * g.mm2[bi];
+            dd_acc(vh, vl, a, sh[k * nsh + q + 1]);
+        }
+        if (q >= 1) {
+            const double a = g.mm1[bi] * g.adv_coef[q * 4 + 2] + g.adv_coef[q * 4 + 3] * g.mm2[bi];
+            dd_acc(vh, vl, a, sh[k * nsh + q - 1]);
+        }
+        dd_acc(mh, ml, g.Mr[bi], sh[k * nsh + q]);
+    }
+    dd_acc2(yh, yl, gh, gl, n0 * Tg);
+    dd_acc2(yh, yl, vh, vl, cadv);
+    dd_acc2(yh, yl, mh, ml, -mu);
+    double Uh = 0.0, Ul = 0.0;
+    if (ee) {
+        for (int t = 0; t < g.ntri; ++t) {
+            if (g.tri[3 * t] != q) continue;
+            const int l = g.tri[3 * t + 1], s = g.tri[3 * t + 2];
+            const double* ca = g.CA + ((size_t)t * nsp + p) * BTE_NB * BTE_NB;
+            const double* cb = g.CB + ((size_t)t * nsp + p) * BTE_NB * BTE_NB;
+            for (int dk = -BTE_BAND; dk <= BTE_BAND; ++dk) {
+                const int k = p + dk;
+                if (k < 0 || k >= nsp) continue;
+                double ih = 0.0, il = 0.0;
+                for (int dr = -BTE_BAND; dr <= BTE_BAND; ++dr) {
+                    const int rr = p + dr;
+                    if (rr < 0 || rr >= nsp) continue;
+                    const int o = (dk + BTE_BAND) * BTE_NB + dr + BTE_BAND;
+                    dd_acc2(ih, il, shh[rr * nsh + s], shl[rr * nsh + s], ca[o]);
+                    dd_acc2(ih, il, sgg[rr * nsh + s], sgl[rr * nsh + s], cb[o]);
+                }
+                dd_acc2(Uh, Ul, ih, il, sh[k * nsh + l]);
+            }
+        }
+        dd_acc2(yh, yl, Uh, Ul, negam);
+    }
+    y = yh + yl;
+    Uo = Uh + Ul;
+    mho = mh + ml;
+}
+
+// ---------------------------------------------------------------------------------
 // Residual F_raw(h) for one point per CTA, plus ||(I - p p^T) M^-1 F_raw||.
 // If dh != nullptr the CTA evaluates at h + alpha * dh and writes that state to hout.
 // aux (if non-null) receives hh = HL h, gg = GL h, U = C_ee(h, h) raw, Mh = M h.
@@ -61,19 +147,23 @@ __global__ void __launch_bounds__(256)
 k_residual(GridView g, PointParams pp, int ee, const int* __restrict__ act, int nact,
            const double* __restrict__ h, const double* __restrict__ dh, int ldd, const double* __restrict__ alpha,
            const int* __restrict__ need, double* hout, double* F, double* aux, double* scal, double* rnorm,
-           double* srel) {
+           double* srel, const int* __restrict__ ddm) {
     extern __shared__ double sm[];
     const int slot = blockIdx.x;
     if (slot >= nact) return;
     const int pt = act[slot];
     if (pp.eept) ee = pp.eept[pt];
     if (need && !need[pt]) return;
+    // a point at its FP64 rounding floor is evaluated in double-double (smem 7 n instead of 5 n)
+    const bool dd = ddm != nullptr && ddm[pt] != 0;
     const int n = g.n, nsh = g.nsh, nsp = g.nsp, tid = threadIdx.x, nt = blockDim.x;
     double* sh = sm;           // h
     double* shh = sm + n;      // HL h
     double* sgg = sm + 2 * n;  // GL h
     double* sF = sm + 3 * n;   // F_raw, later M^-1 F
     double* sR = sm + 4 * n;
+    double* shl = sm + 5 * n;  // low parts of HL h and GL h (double-double points)
+    double* sgl = sm + 6 * n;
     __shared__ double red[32];
 
     const double* hp = h + (size_t)pt * n;
@@ -115,6 +205,19 @@ k_residual(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
             int p = r / nsh, l = r % nsh;
             const double* HLr = g.HL + ((size_t)l * nsp + p) * nsp;
             const double* GLr = g.GL + ((size_t)l * nsp + p) * nsp;
+            if (dd) {
+                double h1 = 0, l1 = 0, h2 = 0, l2 = 0;
+                for (int c = 0; c < nsp; ++c) {
+                    const double hv = sh[c * nsh + l];
+                    dd_acc(h1, l1, HLr[c], hv);
+                    dd_acc(h2, l2, GLr[c], hv);
+                }
+                shh[r] = h1;
+                shl[r] = l1;
+                sgg[r] = h2;
+                sgl[r] = l2;
+                continue;
+            }
             double s1 = 0, s2 = 0;
             for (int c = 0; c < nsp; ++c) {
                 double hv = sh[c * nsh + l];
@@ -137,6 +240,20 @@ k_residual(GridView g, PointParams pp, int ee, const int* __restrict__ act, int 
     for (int rm = tid; rm < n; rm += nt) {
         const int q = rm / nsp, p = rm % nsp;
         const int r = p * nsh + q;
+        if (dd) {
+            double y, U, mh;
+            residual_row_dd(g, pp, pt, ee, q, p, sh, shh, shl, sgg, sgl, n0, Tg, cadv, mu, ne * gam, y, U, mh);
+            sF[r] = y;
+            F[(size_t)pt * n + r] = y;
+            if (aux) {
+                double* ax = aux + (size_t)pt * 4 * n;
+                ax[r] = shh[r] + shl[r];
+                ax[n + r] = sgg[r] + sgl[r];
+                ax[2 * n + r] = U;
+                ax[3 * n + r] = mh;
+            }
+            continue;
+        }
         double y = 0.0;
         // electron-heavy collisions
         for (int s = 0; s < g.nspecies; ++s) {
@@ -1044,10 +1161,21 @@ __global__ void k_store_solution(int P_act, const T* __restrict__ xs, int N, con
 // noise-level decrease passes the test at a vanishing step.
 constexpr double STALL_ALPHA = 1.0 / 64.0;
 constexpr double STALL_RTOL = 1e-6;
+// A point whose merit stops resolving its steps at the FP64 rounding floor (the two ROUNDOFF
+// exits below) while its Newton step is still above DD_STEP_RTOL of the state first switches
+// its residual to double-double (ddm; ddpend asks the next Newton iteration to re-evaluate its
+// state that way) and goes on; it ends at the double-double floor. A point whose step at the
+// floor is already below DD_STEP_RTOL is resolved to FP64 precision in h and ends as before.
+// Measured at c2 (4096 points): the largest mixed-vs-FP64 EDF difference fell from 9.6e-8 to
+// 3.8e-9 (no point above 1e-8, 63 before) and FP64's own spread between two starting points
+// from 9.3e-8 to 3.0e-8, for 18% of the mixed form's throughput (7,505 against 9,155 solves/s;
+// switching every point at the floor cost 30%, a 1e-11 gate 23%).
+constexpr double DD_STEP_RTOL = 1e-10;
 __global__ void k_armijo(int nact, const int* __restrict__ act, int* searching, double* alpha,
                          const double* __restrict__ r, const double* __restrict__ rt, double c, double rho,
                          double amin, int* status, int* nsearch, int* accepted, const double* __restrict__ r0,
-                         double stagnate_rtol, const double* __restrict__ srel, double step_rtol, int stall_status) {
+                         double stagnate_rtol, const double* __restrict__ srel, double step_rtol, int stall_status,
+                         int* ddm, int* ddpend) {
     int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= nact) return;
     int pt = act[slot];
@@ -1061,7 +1189,21 @@ __global__ void k_armijo(int nact, const int* __restrict__ act, int* searching, 
         searching[pt] = 0;
         accepted[pt] = 1;
         // a step that barely contracts the merit at round-off level ends the solve after it is taken
-        if (rn > 0.5 * rr && (rn <= stagnate_rtol * r0[pt] || srel[pt] <= 1e-2 * step_rtol)) status[pt] = BTE_ST_ROUNDOFF;
+        if (rn > 0.5 * rr && (rn <= stagnate_rtol * r0[pt] || srel[pt] <= 1e-2 * step_rtol)) {
+            if (ddm && !ddm[pt] && srel[pt] > DD_STEP_RTOL) {
+                ddm[pt] = 1;
+                ddpend[pt] = 1;
+            } else {
+                status[pt] = BTE_ST_ROUNDOFF;
+            }
+        }
+        return;
+    }
+    if (al == 1.0 && (rr <= stagnate_rtol * r0[pt] || tiny) && ddm && !ddm[pt] && srel[pt] > DD_STEP_RTOL) {
+        searching[pt] = 0;
+        accepted[pt] = 0;
+        ddm[pt] = 1;
+        ddpend[pt] = 1;
         return;
     }
     if (al == 1.0 && (rr <= stagnate_rtol * r0[pt] || tiny)) {
@@ -1142,6 +1284,11 @@ __global__ void k_fill_int(int* p, int v, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) p[i] = v;
 }
+
+__global__ void k_set_list(int m, const int* __restrict__ list, int* a, int v) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m) a[list[i]] = v;
+}
 __global__ void k_iota(int* p, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) p[i] = i;
@@ -1174,6 +1321,7 @@ struct BteWork {
     double *ref_r = nullptr, *ref_r0 = nullptr;  // the reference's merit at the end / start, P
     double *corr0 = nullptr, *corr1 = nullptr;   // relative refinement corrections, first / last pass
     int32_t* reason = nullptr;                   // mixed-form status of each point before the FP64 pass
+    int32_t *ddm = nullptr, *ddpend = nullptr;   // residual in double-double; its state to re-evaluate
     int32_t* refdone = nullptr;                  // refinement finished for the point in this Newton step
     int32_t* nit = nullptr;                      // Newton iterations of each point in its current solve
     void* J = nullptr;
@@ -1193,7 +1341,7 @@ struct BteWork {
 };
 
 static void free_work(BteWork* w) {
-    void* ptrs[] = {w->nit, w->refdone, w->reason, w->corr0, w->corr1, w->ref_r, w->ref_r0, w->rowscale, w->h0, w->srel, w->sigma, w->xs, w->h, w->ht, w->F, w->Ft, w->aux, w->auxt, w->scal, w->scalt, w->dh, w->r, w->rt, w->r0,
+    void* ptrs[] = {w->nit, w->refdone, w->reason, w->ddm, w->ddpend, w->corr0, w->corr1, w->ref_r, w->ref_r0, w->rowscale, w->h0, w->srel, w->sigma, w->xs, w->h, w->ht, w->F, w->Ft, w->aux, w->auxt, w->scal, w->scalt, w->dh, w->r, w->rt, w->r0,
                     w->alpha, w->J, w->kc, w->gm_V, w->gm_Z, w->gm_W, w->gm_H, w->gm_cs, w->gm_sn, w->gm_g, w->gm_bn,
                     w->gm_sig, w->gm_xf, w->gm_list, w->gm_on, w->gm_cnt, w->piv, w->info, w->act, w->act2, w->cnt, w->searching, w->accepted};
     for (void* p : ptrs)
@@ -1249,7 +1397,8 @@ static int ensure_work(BteWork* w, const BteGrid* g, int P, int prec, int krylov
               A((void**)&w->rowscale, (size_t)P * (N + 1) * sizeof(double)) && A((void**)&w->h0, pn) &&
               A((void**)&w->ref_r, (size_t)P * sizeof(double)) && A((void**)&w->ref_r0, (size_t)P * sizeof(double)) &&
               A((void**)&w->corr0, (size_t)P * sizeof(double)) && A((void**)&w->corr1, (size_t)P * sizeof(double)) &&
-              A((void**)&w->reason, (size_t)P * sizeof(int32_t)) && A((void**)&w->refdone, (size_t)P * sizeof(int32_t)) &&
+              A((void**)&w->reason, (size_t)P * sizeof(int32_t)) && A((void**)&w->ddm, (size_t)P * sizeof(int32_t)) &&
+              A((void**)&w->ddpend, (size_t)P * sizeof(int32_t)) && A((void**)&w->refdone, (size_t)P * sizeof(int32_t)) &&
               A((void**)&w->nit, (size_t)P * sizeof(int32_t)) && A((void**)&w->r, P * sizeof(double)) &&
               A((void**)&w->rt, P * sizeof(double)) && A((void**)&w->r0, P * sizeof(double)) &&
               A((void**)&w->alpha, P * sizeof(double)) && A(&w->J, jb) && (kb == 0 || A((void**)&w->kc, kb)) &&
@@ -1603,6 +1752,12 @@ static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
     const double amin = (prec == BTE_PREC_MIXED) ? std::max(o->alpha_min, 1.0 / 8192.0) : o->alpha_min;
     Profiler& pf = g_prof;
     auto other = [&](auto&& fn) { return pf.run(PF_OTHER, s, 0, 0, 1, fn); };
+    // points that switched to the double-double residual: their state's F, aux and merit again
+    CKR(pf.run(PF_RESIDUAL, s, 0, 0, 2, [&] {
+        k_residual<<<nact, 256, res_smem, s>>>(gv, pp, ee, L.act, nact, w->h, nullptr, 0, nullptr, w->ddpend, nullptr,
+                                               w->F, w->aux, w->scal, w->r, nullptr, w->ddm);
+        k_set_list<<<nblk(nact, 256), 256, 0, s>>>(nact, L.act, w->ddpend, 0);
+    }));
     {
         // Jacobian straight into the factorization buffer, then LU of [J | -F] and back substitution
         dim3 gj(nblk(N, JAC_WARPS), nact);
@@ -1683,14 +1838,16 @@ static int newton_iteration(SolveCtx& c, Lane& L, int nact, int prec) {
         for (int ls = 0; ls < 200; ++ls) {
             CKR(pf.run(PF_RESIDUAL, s, nsearch * res_flops_pt(g, ee), nsearch * res_bytes_pt(g, true), 1, [&] {
                 k_residual<<<nact, 256, res_smem, s>>>(gv, pp, ee, L.act, nact, w->h, w->dh, ldd, w->alpha,
-                                                       w->searching, w->ht, w->Ft, w->auxt, w->scalt, w->rt, w->srel);
+                                                       w->searching, w->ht, w->Ft, w->auxt, w->scalt, w->rt, w->srel,
+                                                       w->ddm);
             }));
             CKR(cudaMemsetAsync(w->cnt, 0, sizeof(int32_t), s));
             CKR(other([&] {
                 k_armijo<<<nblk(nact, 256), 256, 0, s>>>(nact, L.act, w->searching, w->alpha, w->r, w->rt,
                                                         o->line_search_c, o->alpha_rho, amin, status, w->cnt,
                                                         w->accepted, w->r0, 1e-9, w->srel, 1e-8,
-                                                        prec == BTE_PREC_MIXED ? BTE_ST_NEED_FP64 : BTE_ST_ROUNDOFF);
+                                                        prec == BTE_PREC_MIXED ? BTE_ST_NEED_FP64 : BTE_ST_ROUNDOFF,
+                                                        w->ddm, w->ddpend);
             }));
             int hc = 0;
             CKR(cudaMemcpyAsync(&hc, w->cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
@@ -1734,7 +1891,7 @@ int bte_solve_impl(BteGrid* g, int P, const double* n0, const double* ne, const 
     c.jstride = (long long)c.N * c.ld;
     // border scale: typical magnitude of the raw collision operator per unit n0
     c.beta_scale = g->q0max / (g->umax > 0 ? g->umax : 1.0);
-    c.res_smem = (size_t)5 * c.n * sizeof(double);
+    c.res_smem = (size_t)7 * c.n * sizeof(double);
     c.ref_smem = (size_t)(5 * c.n + 2) * sizeof(double);  // x, r: n + 1 each; h, HL x, GL x: n each
     c.o = o; c.status = status; c.iters = iters; c.s = s;
     const int n = c.n;
@@ -1746,7 +1903,7 @@ int bte_solve_impl(BteGrid* g, int P, const double* n0, const double* ne, const 
     auto residual_all = [&](int nact) {
         return pf.run(PF_RESIDUAL, s, nact * res_flops_pt(g, c.ee), nact * res_bytes_pt(g, false), 1, [&] {
             k_residual<<<nact, 256, c.res_smem, s>>>(c.gv, c.pp, c.ee, L.act, nact, w->h, nullptr, 0, nullptr,
-                                                     nullptr, nullptr, w->F, w->aux, w->scal, w->r, nullptr);
+                                                     nullptr, nullptr, w->F, w->aux, w->scal, w->r, nullptr, w->ddm);
         });
     };
 
@@ -1755,6 +1912,8 @@ int bte_solve_impl(BteGrid* g, int P, const double* n0, const double* ne, const 
     CKR(other([&] { k_fill_int<<<nblk(P, 256), 256, 0, s>>>(status, -1, P); }));
     CKR(other([&] { k_fill_int<<<nblk(P, 256), 256, 0, s>>>(iters, 0, P); }));
     CKR(other([&] { k_fill_int<<<nblk(P, 256), 256, 0, s>>>(w->nit, 0, P); }));
+    CKR(other([&] { k_fill_int<<<nblk(P, 256), 256, 0, s>>>(w->ddm, 0, P); }));
+    CKR(other([&] { k_fill_int<<<nblk(P, 256), 256, 0, s>>>(w->ddpend, 0, P); }));
     CKR(other([&] { k_iota<<<nblk(P, 256), 256, 0, s>>>(L.act, P); }));
     CKR(residual_all(P));
     CKR(cudaMemcpyAsync(w->r0, w->r, P * sizeof(double), cudaMemcpyDeviceToDevice, s));
@@ -1792,6 +1951,7 @@ int bte_solve_impl(BteGrid* g, int P, const double* n0, const double* ne, const 
             int m = std::min(chunk, nf - c0);
             CKR(cudaMemcpyAsync(L.act, failed.data() + c0, m * sizeof(int32_t), cudaMemcpyHostToDevice, s));
             CKR(other([&] { k_restore<<<m, 256, 0, s>>>(n, m, L.act, w->reason, w->h0, w->h, w->nit, w->r, w->r0); }));
+            CKR(other([&] { k_set_list<<<nblk(m, 256), 256, 0, s>>>(m, L.act, w->ddm, 0); }));
             CKR(residual_all(m));
             for (int it = 0, nact = m; it < o->max_iter && nact > 0; ++it) {
                 nact = newton_iteration(c, L, nact, BTE_PREC_FP64);
@@ -1966,7 +2126,7 @@ static SolveCtx engine_ctx(BteEngine* e, cudaStream_t s) {
     c.ee = g->ee ? 1 : 0;  // per point: the slot's phase
     c.jstride = (long long)c.N * c.ld;
     c.beta_scale = g->q0max / (g->umax > 0 ? g->umax : 1.0);
-    c.res_smem = (size_t)5 * c.n * sizeof(double);
+    c.res_smem = (size_t)7 * c.n * sizeof(double);
     c.ref_smem = (size_t)(5 * c.n + 2) * sizeof(double);  // x, r: n + 1 each; h, HL x, GL x: n each
     c.o = &e->opts; c.status = e->status; c.iters = e->iters; c.s = s;
     return c;
@@ -2038,9 +2198,11 @@ static int engine_start_phase(BteEngine* e, SolveCtx& c, const int* list, int m,
     Profiler& pf = g_prof;
     CKR(pf.run(PF_RESIDUAL, s, m * res_flops_pt(g, c.ee), m * res_bytes_pt(g, false), 1, [&] {
         k_residual<<<m, 256, c.res_smem, s>>>(c.gv, c.pp, c.ee, list, m, w->h, nullptr, 0, nullptr, nullptr, nullptr,
-                                              w->F, w->aux, w->scal, w->r, nullptr);
+                                              w->F, w->aux, w->scal, w->r, nullptr, nullptr);
     }));
-    CKR(pf.run(PF_OTHER, s, 0, 0, 2, [&] {
+    CKR(pf.run(PF_OTHER, s, 0, 0, 4, [&] {
+        k_set_list<<<nblk(m, 256), 256, 0, s>>>(m, list, w->ddm, 0);
+        k_set_list<<<nblk(m, 256), 256, 0, s>>>(m, list, w->ddpend, 0);
         k_copy_list<<<nblk(m, 256), 256, 0, s>>>(m, list, w->r, w->r0);
         k_ref_merit<<<m, 256, (size_t)2 * n * sizeof(double), s>>>(c.gv, m, list, w->F, w->ref_r0);
     }));
@@ -2092,8 +2254,9 @@ int bte_engine_step_impl(BteEngine* e, int* n_done, int32_t* done_out, cudaStrea
             k_engine_to_fp64<<<k, 256, 0, s>>>(k, e->l_in, n, e->status, w->reason, w->nit, w->h0, w->h, w->r, w->r0);
         }));
         CKR(pf.run(PF_RESIDUAL, s, k * res_flops_pt(g, c.ee), k * res_bytes_pt(g, false), 1, [&] {
+            k_set_list<<<nblk(k, 256), 256, 0, s>>>(k, e->l_in, w->ddm, 0);
             k_residual<<<k, 256, c.res_smem, s>>>(c.gv, c.pp, c.ee, e->l_in, k, w->h, nullptr, 0, nullptr, nullptr,
-                                                  nullptr, w->F, w->aux, w->scal, w->r, nullptr);
+                                                  nullptr, w->F, w->aux, w->scal, w->r, nullptr, nullptr);
         }));
         CKR(cudaMemcpyAsync(e->f64.act + e->nf64, e->l_in, k * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
         CKR(cudaStreamSynchronize(s));  // `mv` is read by the copy above
@@ -2302,7 +2465,7 @@ int bte_transient_impl(BteGrid* g, int P, const double* n0, const double* ne, co
     c.ee = (o->ee && g->ee) ? 1 : 0;
     c.jstride = (long long)N * c.ld;
     c.beta_scale = g->q0max / (g->umax > 0 ? g->umax : 1.0);
-    c.res_smem = (size_t)5 * n * sizeof(double);
+    c.res_smem = (size_t)7 * n * sizeof(double);
     c.o = &so; c.status = status; c.iters = iters; c.s = s;
     CKR(bte_raise_smem_limit((const void*)k_residual, c.res_smem));
     const size_t rm_smem = (size_t)2 * n * sizeof(double);
@@ -2343,7 +2506,7 @@ int bte_transient_impl(BteGrid* g, int P, const double* n0, const double* ne, co
         // the step's Jacobian at the current state, factored once
         CKR(pf.run(PF_RESIDUAL, s, 0, 0, 1, [&] {
             k_residual<<<P, 256, c.res_smem, s>>>(c.gv, c.pp, c.ee, all, P, w->h, nullptr, 0, nullptr, nullptr, nullptr,
-                                                  w->F, w->aux, w->scal, w->r, nullptr);
+                                                  w->F, w->aux, w->scal, w->r, nullptr, nullptr);
         }));
         dim3 gj(nblk(N, JAC_WARPS), P);
         cudaError_t le = cudaSuccess;
@@ -2376,7 +2539,8 @@ int bte_transient_impl(BteGrid* g, int P, const double* n0, const double* ne, co
         for (int it = 0;; ++it) {
             CKR(pf.run(PF_RESIDUAL, s, 0, 0, 1, [&] {
                 k_residual<<<nact, 256, c.res_smem, s>>>(c.gv, c.pp, c.ee, w->act, nact, w->h, w->dh, ldd, w->alpha,
-                                                         nullptr, w->ht, w->Ft, w->auxt, w->scalt, w->rt, nullptr);
+                                                         nullptr, w->ht, w->Ft, w->auxt, w->scalt, w->rt, nullptr,
+                                                         nullptr);
             }));
             CKR(other([&] {
                 k_transient_G<<<nact, 256, 0, s>>>(c.gv, nact, w->act, w->dh, ldd, w->Ft, cdt, G);
