@@ -948,7 +948,8 @@ def main():
     line = {
         "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "mixed: f32 Jacobian+LU, f64 residual/state", "data": "synthetic",
+        "dtype": "mixed: f32 Jacobian+LU (tf32 tensor-core updates), f64 residual/state, double-double "
+                 "residual at the f64 floor", "data": "synthetic",
         "config": workload_config(a, "mixed"),
         "latency_ms": {"p50": float(np.percentile(steps_ms, 50)), "p99": float(np.percentile(steps_ms, 99)),
                        "unit": "batch solve of %d points" % a.n_pts},
