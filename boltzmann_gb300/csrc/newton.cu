@@ -1219,6 +1219,13 @@ __global__ void k_armijo(int nact, const int* __restrict__ act, int* searching, 
     if (al < STALL_ALPHA && rr <= STALL_RTOL * r0[pt]) {
         searching[pt] = 0;
         accepted[pt] = 0;
+        // a stalled search near the root may be the FP64 merit's noise: the point first goes
+        // on with the double-double residual, as at the two ROUNDOFF exits
+        if (ddm && !ddm[pt] && srel[pt] > DD_STEP_RTOL) {
+            ddm[pt] = 1;
+            ddpend[pt] = 1;
+            return;
+        }
         status[pt] = stall_status;
         return;
     }
