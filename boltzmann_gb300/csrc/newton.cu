@@ -1666,7 +1666,6 @@ static cudaError_t gmres_refine(SolveCtx& c, Lane& L, int nact, bool all) {
     const int N = c.N, ld = c.ld, ldd = c.ldd, ee = c.ee;
     cudaStream_t s = c.s;
     Profiler& pf = g_prof;
-    cudaError_t e = cudaSuccess;
 #define GMCK(x, what)                                                                            \
     do {                                                                                         \
         cudaError_t _e = (x);                                                                    \
