@@ -22,6 +22,7 @@
 #include <cmath>
 #include "bte_common.cuh"
 #include "bte_grid.h"
+#include "dd_arith.h"
 
 template <typename T>
 cudaError_t bte_lu_factor_t(int P, int N, int NC, T* A, int ld, long long stride, int32_t* piv, int32_t* info,
@@ -52,20 +53,8 @@ struct PointParams {
 // per-point scalar slots
 enum { SC_GAMMA = 0, SC_MU, SC_T0, SC_M0, SC_NE, SC_COUNT = 8 };
 
-// ---------------------------------------------------------------------------------
 // Double-double accumulation (the residual of a point at its FP64 rounding floor): an exact
-// product (fma) and a compensated sum per term, rounded once at the end of a row.
-// ---------------------------------------------------------------------------------
-__device__ inline void dd_acc(double& hi, double& lo, double a, double b) {
-    const double pr = a * b, pe = fma(a, b, -pr);
-    const double sm = hi + pr, v = sm - hi, e = (hi - (sm - v)) + (pr - v);
-    hi = sm;
-    lo += e + pe;
-}
-__device__ inline void dd_acc2(double& hi, double& lo, double ahi, double alo, double b) {
-    dd_acc(hi, lo, ahi, b);
-    lo += alo * b;
-}
+// product (fma) and a compensated sum per term, rounded once at the end of a row (dd_arith.h).
 
 // One row (mode q, spline p) of F_raw in double-double: the terms of k_residual's FP64 rows
 // (electron-heavy collisions, gas temperature, advection, growth, e-e) with the Rosenbluth
